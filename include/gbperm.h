@@ -1,0 +1,104 @@
+/*
+ * gbperm.h -- C ABI of the GB300 permanent library (libgbperm.so).
+ *
+ * Every function returns an int status (GBPERM_OK == 0); on failure
+ * gbperm_last_error() returns a message for the calling thread.  Nothing is
+ * thrown across the ABI and nothing calls exit().
+ *
+ * Matrices are complex128: interleaved (re, im) doubles, row-major, with a
+ * leading dimension `ld` counted in complex elements (ld >= cols).  Results
+ * are complex128 written as two doubles {re, im}; where an `out_dd` pointer is
+ * accepted it receives {re_hi, im_hi, re_lo, im_lo}, the double-double value
+ * of the result before rounding to double.
+ *
+ * Functions without a `_dev` suffix take HOST pointers: the library copies the
+ * inputs to the current CUDA device, computes, copies the result back and
+ * synchronises.  `_dev` functions take DEVICE pointers, a caller-provided
+ * device workspace and a cudaStream_t (passed as void*), enqueue the work and
+ * return without synchronising.
+ *
+ * Thread safety: host-pointer functions use a per-thread stream and a
+ * per-thread device workspace, so concurrent calls from different threads
+ * do not share buffers.
+ */
+#ifndef GBPERM_H
+#define GBPERM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBPERM_OK 0
+#define GBPERM_ERR_ARG 1         /* bad pointer, shape, stride or option */
+#define GBPERM_ERR_STATE_SUM 2   /* sum(input_state) != sum(output_state) */
+#define GBPERM_ERR_TOO_LARGE 3   /* beyond the supported sizes */
+#define GBPERM_ERR_CUDA 4        /* a CUDA runtime call failed */
+#define GBPERM_ERR_LIB 5         /* unknown calculator library id */
+#define GBPERM_ERR_NO_DEVICE 6   /* no CUDA device visible */
+
+/* Largest supported matrix side (columns of the product, rows of the Gray code). */
+#define GBPERM_MAX_DIM 64
+
+typedef struct gbperm_stats {
+    double kernel_ms;      /* device time of the compute launches (CUDA events) */
+    double steps;          /* Gray-code steps evaluated (terms of the sum) */
+    double flops;          /* algorithmic FP64 flops: 8 n per plain step, see DESIGN */
+    int32_t launches;      /* kernels launched by the call */
+    int32_t grid;          /* blocks of the main launch */
+    int32_t seg_log2;      /* log2 of the Gray segment length (plain / grad) */
+    int32_t reserved;
+} gbperm_stats;
+
+/* ------------------------------------------------------------- library */
+int gbperm_version(void);
+const char* gbperm_last_error(void);
+/* Number of visible CUDA devices (0 when none); never fails. */
+int gbperm_device_count(void);
+/* Tuning knobs (process-wide).  Keys:
+ *   "plain.seg_log2"      force log2 segment length of the plain kernel (-1 = auto)
+ *   "plain.grid"          force the plain grid size (0 = auto)
+ *   "repeated.low_digits" force the digits handled inside a repeated segment (-1 = auto)
+ *   "batched.threads"     force threads per instance of the batched kernel (0 = autotuned)
+ */
+int gbperm_set_option(const char* key, int64_t value);
+int64_t gbperm_get_option(const char* key);
+
+/* ------------------------------------------------------ plain permanent */
+/* Glynn / BBFG permanent of a rows x cols matrix.  Replaces
+ * BBFGPermanentCalculator::calculate (piquassoboost/sampling/source/
+ * BBFGPermanentCalculator.cpp:89-126) and GlynnPermanentCalculator::calculate
+ * (GlynnPermanentCalculator.hpp:47-57); semantics: rows == 0 or cols == 0 -> 1,
+ * rows >= cols + 2 -> 0. */
+int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, double* out,
+                double* out_dd, gbperm_stats* stats);
+
+/* Device-pointer form.  dA: device complex128 matrix; d_out: 2 doubles on the
+ * device; d_out_dd: NULL or 4 doubles on the device.  The workspace must hold
+ * gbperm_perm_workspace_size(rows, cols) bytes, 256-byte aligned. */
+size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols);
+int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, void* d_out,
+                    void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream);
+
+/* --------------------------------------------------- repeated permanent */
+/* Permanent of the matrix whose row i is repeated row_mult[i] times and
+ * column j col_mult[j] times (without expanding it).  Replaces
+ * BBFGPermanentCalculatorRepeated::calculate (piquassoboost/sampling/source/
+ * BBFGPermanentCalculatorRepeated.cpp:75-98) and GlynnPermanentCalculator
+ * Repeated::calculate (GlynnPermanentCalculatorRepeated.hpp:48-74).
+ * col_mult is the INPUT state and row_mult the OUTPUT state, as in the
+ * reference wrapper (ChinHuhPermanentCalculator_Wrapper.hpp:367-375).
+ * Only the first nrow rows / ncol columns take part (nrow <= rows,
+ * ncol <= cols).  rows == 0 or a zero photon count -> 1;
+ * sum(col_mult) != sum(row_mult) -> GBPERM_ERR_STATE_SUM. */
+int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
+                         const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
+                         int64_t nrow, double* out, double* out_dd, gbperm_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPERM_H */

@@ -1,0 +1,526 @@
+/*
+ * CPU oracle for the Glynn / BBFG permanent calculators.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * calculators (piquassoboost, sampling/source/ permanent calculators), used by
+ * the tests as the checker and by bench.py as the CPU baseline.  The product
+ * library never links or calls it.
+ *
+ * Parity pin: tests/test_oracle.py checks every entry point against the golden
+ * values of the reference's unittests/test_permanent.py:47-251 and against
+ * fixtures generated by running the reference's own C++ calculators
+ * (tests/golden/make_golden.py, oracle/build_ref.sh).
+ *
+ * Two precisions are built from one body (perm_oracle_body.h):
+ *   _d : IEEE double, the reference's lib 6/7 arithmetic;
+ *   _q : IEEE binary128 (113-bit significand) -- __float128 on x86-64 and
+ *        long double on AArch64, where long double is binary128.  This is the
+ *        extended-precision oracle.  (The reference's own "long double" is the
+ *        x87 64-bit-significand type on x86; binary128 is strictly wider.)
+ * Results are returned as double-double pairs so that the extended oracle
+ * keeps its extra digits: out = {re_hi, im_hi, re_lo, im_lo}.
+ *
+ * Threading mirrors the reference's work split (BBFGPermanentCalculator.hpp
+ * :119-134): the Gray range is cut into 4 x threads contiguous segments; each
+ * segment's partial sum is stored by segment index and the partials are added
+ * in index order, so results do not depend on thread timing.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#if defined(__x86_64__) || defined(__i386__)
+typedef __float128 quad_t_;
+#elif defined(__aarch64__)
+typedef long double quad_t_;
+_Static_assert(sizeof(long double) == 16, "AArch64 long double must be binary128");
+#else
+#error "binary128 type unknown for this architecture"
+#endif
+
+static __thread char g_err[256];
+
+const char* orc_last_error(void) { return g_err; }
+
+static int set_err(int code, const char* msg) {
+    snprintf(g_err, sizeof(g_err), "%s", msg);
+    return code;
+}
+
+/* Exact binomial coefficient, common_functionalities.cpp:131-160 (Pascal row). */
+static __int128 orc_binom128(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    __int128 C[130];
+    if (k > 128) return 0;
+    memset(C, 0, sizeof(C));
+    C[0] = 1;
+    for (int i = 1; i <= n; i++)
+        for (int j = (i < k ? i : k); j > 0; j--) C[j] = C[j] + C[j - 1];
+    return C[k];
+}
+
+#define R double
+#define CX cx_d
+#define SFX(x) x##_d
+#include "perm_oracle_body.h"
+#undef R
+#undef CX
+#undef SFX
+
+#define R quad_t_
+#define CX cx_q
+#define SFX(x) x##_q
+#include "perm_oracle_body.h"
+#undef R
+#undef CX
+#undef SFX
+
+static void put_d(cx_d v, double* out) {
+    out[0] = v.re;
+    out[1] = v.im;
+    out[2] = 0.0;
+    out[3] = 0.0;
+}
+
+static void put_q(cx_q v, double* out) {
+    double rh = (double)v.re, ih = (double)v.im;
+    out[0] = rh;
+    out[1] = ih;
+    out[2] = (double)(v.re - (quad_t_)rh);
+    out[3] = (double)(v.im - (quad_t_)ih);
+}
+
+static int hw_threads(int nthreads) {
+    if (nthreads > 0) return nthreads;
+    long n = sysconf(_SC_NPROCESSORS_ONLN);
+    return n > 0 ? (int)n : 1;
+}
+
+/* ---------------------------------------------------------------- pool */
+typedef struct {
+    int kind;   /* 0 plain, 1 repeated */
+    int prec;   /* 0 double, 1 quad */
+    const double* A;
+    int64_t rows, cols, ld;
+    const void* A1;
+    const void* A2;
+    const int* rm;
+    int64_t nrm;
+    const int* cm;
+    int64_t ncm;
+    uint64_t total;    /* plain: Idx_max; repeated: Idx_max */
+    int64_t njobs;
+    atomic_llong next;
+    cx_d* part_d;
+    cx_q* part_q;
+} job_t;
+
+static void run_job(job_t* J, int64_t j) {
+    uint64_t wb = J->total / (uint64_t)J->njobs;
+    uint64_t o0 = (uint64_t)j * wb;
+    if (J->kind == 0) {
+        uint64_t o1 = (j == J->njobs - 1) ? J->total : (uint64_t)(j + 1) * wb;
+        if (J->prec == 0)
+            J->part_d[j] = bbfg_segment_d((const cx_d*)J->A1, (const cx_d*)J->A2, J->rows, J->cols, o0, o1);
+        else
+            J->part_q[j] = bbfg_segment_q((const cx_q*)J->A1, (const cx_q*)J->A2, J->rows, J->cols, o0, o1);
+    } else {
+        uint64_t o1 = (j == J->njobs - 1) ? J->total - 1 : (uint64_t)(j + 1) * wb - 1;
+        if (J->prec == 0)
+            J->part_d[j] = rep_segment_d(J->A, J->ld, J->rm, J->nrm, J->cm, J->ncm, o0, o1);
+        else
+            J->part_q[j] = rep_segment_q(J->A, J->ld, J->rm, J->nrm, J->cm, J->ncm, o0, o1);
+    }
+}
+
+static void* worker(void* arg) {
+    job_t* J = (job_t*)arg;
+    for (;;) {
+        long long j = atomic_fetch_add(&J->next, 1);
+        if (j >= J->njobs) break;
+        run_job(J, (int64_t)j);
+    }
+    return NULL;
+}
+
+static void run_pool(job_t* J, int nthreads) {
+    int nt = nthreads < J->njobs ? nthreads : (int)J->njobs;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)(nt > 0 ? nt : 1));
+    atomic_store(&J->next, 0);
+    for (int t = 1; t < nt; ++t) pthread_create(&th[t], NULL, worker, J);
+    worker(J);
+    for (int t = 1; t < nt; ++t) pthread_join(th[t], NULL);
+    free(th);
+}
+
+/* ------------------------------------------------------------ plain BBFG */
+/* BBFGPermanentCalculator::calculate, BBFGPermanentCalculator.cpp:89-126 and
+ * BBFGPermanentCalculator.hpp:87-235.  prec: 0 double, 1 binary128. */
+int orc_bbfg(const double* A, int64_t rows, int64_t cols, int64_t ld, int prec, int nthreads,
+             double* out) {
+    if (rows == 0 || cols == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        return 0;
+    }
+    if (rows >= cols + 2) {
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return 0;
+    }
+    if (rows > 63) return set_err(3, "orc_bbfg: too many rows");
+    int nt = hw_threads(nthreads);
+    job_t J;
+    memset(&J, 0, sizeof(J));
+    J.kind = 0; J.prec = prec; J.A = A; J.rows = rows; J.cols = cols; J.ld = ld;
+    J.total = 1ULL << (rows - 1);
+    int64_t conc = 4 * (int64_t)nt;
+    J.njobs = conc < (int64_t)J.total ? conc : (int64_t)J.total;
+    if (prec == 0) {
+        cx_d *A1, *A2;
+        make_a12_d(A, rows, cols, ld, &A1, &A2);
+        J.A1 = A1; J.A2 = A2;
+        J.part_d = (cx_d*)calloc((size_t)J.njobs, sizeof(cx_d));
+        run_pool(&J, nt);
+        free(A1); free(A2);
+        acc_t_d acc = {0, 0, 0, 0};
+        for (int64_t j = 0; j < J.njobs; ++j) acc_add_d(&acc, J.part_d[j]);
+        cx_d r = acc_get_d(&acc);
+        double s = pow2_neg_d(rows - 1);
+        r.re *= s; r.im *= s;
+        put_d(r, out);
+        free(J.part_d);
+    } else {
+        cx_q *A1, *A2;
+        make_a12_q(A, rows, cols, ld, &A1, &A2);
+        J.A1 = A1; J.A2 = A2;
+        J.part_q = (cx_q*)calloc((size_t)J.njobs, sizeof(cx_q));
+        run_pool(&J, nt);
+        free(A1); free(A2);
+        acc_t_q acc = {0, 0, 0, 0};
+        for (int64_t j = 0; j < J.njobs; ++j) acc_add_q(&acc, J.part_q[j]);
+        cx_q r = acc_get_q(&acc);
+        quad_t_ s = pow2_neg_q(rows - 1);
+        r.re *= s; r.im *= s;
+        put_q(r, out);
+        free(J.part_q);
+    }
+    return 0;
+}
+
+/* --------------------------------------------------------- repeated BBFG */
+/* BBFGPermanentCalculatorRepeated::calculate, BBFGPermanentCalculatorRepeated
+ * .cpp:75-141 and _Tasks ctor/calculate, .hpp:74-307.
+ * col_mult = the input state, row_mult = the output state. */
+int orc_bbfg_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
+                      const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
+                      int64_t nrow, int prec, int nthreads, double* out) {
+    if (rows == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        return 0;
+    }
+    if (nrow > rows) return set_err(1, "orc_bbfg_repeated: more row multiplicities than rows");
+    if (ncol > cols) return set_err(1, "orc_bbfg_repeated: more column multiplicities than columns");
+    int* rin = (int*)malloc(sizeof(int) * (size_t)(nrow + 1));
+    int* cm = (int*)malloc(sizeof(int) * (size_t)(ncol + 1));
+    for (int64_t i = 0; i < nrow; ++i) rin[i] = (int)row_mult[i];
+    for (int64_t j = 0; j < ncol; ++j) cm[j] = (int)col_mult[j];
+    /* ctor: prepend the first row of smallest nonzero multiplicity with
+     * multiplicity 1 (BBFGPermanentCalculatorRepeated.hpp:78-94). */
+    int64_t imin = -1;
+    for (int64_t i = 0; i < nrow; ++i)
+        if (rin[i] != 0 && (imin < 0 || rin[i] < rin[imin])) imin = i;
+    int* rm;
+    int64_t nrm;
+    double* M;
+    int64_t Mld, Mrows;
+    if (nrow > 0 && imin >= 0) {
+        nrm = nrow + 1;
+        rm = (int*)malloc(sizeof(int) * (size_t)nrm);
+        rm[0] = 1;
+        for (int64_t i = 0; i < nrow; ++i) rm[i + 1] = rin[i];
+        rm[1 + imin]--;
+        Mrows = rows + 1;
+        Mld = cols;
+        M = (double*)malloc(sizeof(double) * 2 * (size_t)(Mrows * cols));
+        for (int64_t j = 0; j < cols; ++j) {
+            M[2 * j] = A[2 * (imin * ld + j)];
+            M[2 * j + 1] = A[2 * (imin * ld + j) + 1];
+        }
+        for (int64_t i = 0; i < rows; ++i)
+            for (int64_t j = 0; j < cols; ++j) {
+                M[2 * ((i + 1) * Mld + j)] = A[2 * (i * ld + j)];
+                M[2 * ((i + 1) * Mld + j) + 1] = A[2 * (i * ld + j) + 1];
+            }
+    } else {
+        nrm = nrow;
+        rm = (int*)malloc(sizeof(int) * (size_t)(nrm + 1));
+        for (int64_t i = 0; i < nrow; ++i) rm[i] = rin[i];
+        Mrows = rows;
+        Mld = cols;
+        M = (double*)malloc(sizeof(double) * 2 * (size_t)(rows * cols));
+        for (int64_t i = 0; i < rows; ++i)
+            for (int64_t j = 0; j < cols; ++j) {
+                M[2 * (i * Mld + j)] = A[2 * (i * ld + j)];
+                M[2 * (i * Mld + j) + 1] = A[2 * (i * ld + j) + 1];
+            }
+    }
+    free(rin);
+    int rc = 0;
+    int64_t sr = 0, sc = 0;
+    for (int64_t i = 0; i < nrm; ++i) sr += rm[i];
+    for (int64_t j = 0; j < ncol; ++j) sc += cm[j];
+    if (sr != sc) {
+        rc = set_err(2, "BBFGPermanentCalculatorRepeated_Tasks::calculate:  Number of input and output states should be equal");
+        goto done;
+    }
+    if (Mrows == 0 || cols == 0 || sr == 0 || sc == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        goto done;
+    }
+    if (Mrows == 1) {
+        /* BBFGPermanentCalculatorRepeated.hpp:130-140 */
+        if (prec == 0) {
+            cx_d p = {1.0, 0.0};
+            for (int64_t j = 0; j < ncol; ++j)
+                for (int k = 0; k < cm[j]; ++k) p = cx_mul_d(p, ld_d(M, Mld, 0, j));
+            put_d(p, out);
+        } else {
+            cx_q p = {1, 0};
+            for (int64_t j = 0; j < ncol; ++j)
+                for (int k = 0; k < cm[j]; ++k) p = cx_mul_q(p, ld_q(M, Mld, 0, j));
+            put_q(p, out);
+        }
+        goto done;
+    }
+    {
+        if (sr > 64) { rc = set_err(3, "orc_bbfg_repeated: too many photons"); goto done; }
+        uint64_t total = 1;
+        for (int64_t i = 1; i < nrm; ++i) {
+            uint64_t l = (uint64_t)(rm[i] + 1);
+            if (total > (UINT64_MAX >> 1) / l) { rc = set_err(3, "orc_bbfg_repeated: Gray range too large"); goto done; }
+            total *= l;
+        }
+        int nt = hw_threads(nthreads);
+        job_t J;
+        memset(&J, 0, sizeof(J));
+        J.kind = 1; J.prec = prec; J.A = M; J.ld = Mld; J.rm = rm; J.nrm = nrm; J.cm = cm;
+        J.ncm = ncol; J.total = total;
+        int64_t conc = 4 * (int64_t)nt;
+        J.njobs = conc < (int64_t)total ? conc : (int64_t)total;
+        if (prec == 0) {
+            J.part_d = (cx_d*)calloc((size_t)J.njobs, sizeof(cx_d));
+            run_pool(&J, nt);
+            acc_t_d acc = {0, 0, 0, 0};
+            for (int64_t j = 0; j < J.njobs; ++j) acc_add_d(&acc, J.part_d[j]);
+            cx_d r = acc_get_d(&acc);
+            double s = pow2_neg_d(sr - 1);
+            r.re *= s; r.im *= s;
+            put_d(r, out);
+            free(J.part_d);
+        } else {
+            J.part_q = (cx_q*)calloc((size_t)J.njobs, sizeof(cx_q));
+            run_pool(&J, nt);
+            acc_t_q acc = {0, 0, 0, 0};
+            for (int64_t j = 0; j < J.njobs; ++j) acc_add_q(&acc, J.part_q[j]);
+            cx_q r = acc_get_q(&acc);
+            quad_t_ s = pow2_neg_q(sr - 1);
+            r.re *= s; r.im *= s;
+            put_q(r, out);
+            free(J.part_q);
+        }
+    }
+done:
+    free(rm);
+    free(cm);
+    free(M);
+    return rc;
+}
+
+/* ------------------------------------------------------- recursive Glynn */
+/* GlynnPermanentCalculator<..>::calculate, GlynnPermanentCalculator.hpp
+ * :47-136: the initial column sums take every row with delta = +1. */
+int orc_glynn_recursive(const double* A, int64_t rows, int64_t cols, int64_t ld, int prec,
+                        double* out) {
+    if (rows == 0 || cols == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        return 0;
+    }
+    if (rows >= cols + 2) {
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return 0;
+    }
+    if (rows > 40) return set_err(3, "orc_glynn_recursive: too many rows");
+    if (prec == 0) {
+        cx_d* cs = (cx_d*)calloc((size_t)cols, sizeof(cx_d));
+        for (int64_t j = 0; j < cols; ++j)
+            for (int64_t i = 0; i < rows; ++i) {
+                cx_d a = ld_d(A, ld, i, j);
+                cs[j].re += a.re;
+                cs[j].im += a.im;
+            }
+        acc_t_d acc = {0, 0, 0, 0};
+        glynn_rec_d(A, rows, cols, ld, cs, 1, 1, &acc);
+        cx_d r = acc_get_d(&acc);
+        double s = pow2_neg_d(rows - 1);
+        r.re *= s; r.im *= s;
+        put_d(r, out);
+        free(cs);
+    } else {
+        cx_q* cs = (cx_q*)calloc((size_t)cols, sizeof(cx_q));
+        for (int64_t j = 0; j < cols; ++j)
+            for (int64_t i = 0; i < rows; ++i) {
+                cx_q a = ld_q(A, ld, i, j);
+                cs[j].re += a.re;
+                cs[j].im += a.im;
+            }
+        acc_t_q acc = {0, 0, 0, 0};
+        glynn_rec_q(A, rows, cols, ld, cs, 1, 1, &acc);
+        cx_q r = acc_get_q(&acc);
+        quad_t_ s = pow2_neg_q(rows - 1);
+        r.re *= s; r.im *= s;
+        put_q(r, out);
+        free(cs);
+    }
+    return 0;
+}
+
+/* ---------------------------------------------- recursive repeated Glynn */
+/* GlynnPermanentCalculatorRepeated<..>::calculate and Task, Glynn
+ * PermanentCalculatorRepeated.hpp:48-193: the first nonzero row keeps one
+ * copy fixed at +1 (its delta limit is multiplicity - 1). */
+int orc_glynn_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
+                       const int64_t* col_mult, const int64_t* row_mult, int prec, double* out) {
+    int64_t sin_ = 0, sout = 0;
+    for (int64_t j = 0; j < cols; ++j) sin_ += col_mult[j];
+    for (int64_t i = 0; i < rows; ++i) sout += row_mult[i];
+    if (sin_ != sout)
+        return set_err(2, "GlynnPermanentCalculatorRepeated::calculate:  Number of input and output states should be equal");
+    if (rows == 0 || sin_ == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        return 0;
+    }
+    if (sout > 40) return set_err(3, "orc_glynn_repeated: too many photons");
+    int* lim = (int*)malloc(sizeof(int) * (size_t)rows);
+    int* cm = (int*)malloc(sizeof(int) * (size_t)(cols > 0 ? cols : 1));
+    for (int64_t j = 0; j < cols; ++j) cm[j] = (int)col_mult[j];
+    int64_t imin = rows;
+    for (int64_t i = 0; i < rows; ++i) {
+        if (row_mult[i] > 0) {
+            if (imin > i) { lim[i] = (int)row_mult[i] - 1; imin = i; }
+            else lim[i] = (int)row_mult[i];
+        } else lim[i] = 0;
+    }
+    if (imin == rows) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        free(lim); free(cm);
+        return 0;
+    }
+    if (prec == 0) {
+        cx_d* cs = (cx_d*)calloc((size_t)(cols > 0 ? cols : 1), sizeof(cx_d));
+        for (int64_t j = 0; j < cols; ++j)
+            for (int64_t i = 0; i < rows; ++i) {
+                cx_d a = ld_d(A, ld, i, j);
+                cs[j].re += (double)row_mult[i] * a.re;
+                cs[j].im += (double)row_mult[i] * a.im;
+            }
+        acc_t_d acc = {0, 0, 0, 0};
+        glynn_rep_rec_d(A, rows, cols, ld, lim, cm, cs, 1, imin, 1, &acc);
+        cx_d r = acc_get_d(&acc);
+        double s = pow2_neg_d(sout - 1);
+        r.re *= s; r.im *= s;
+        put_d(r, out);
+        free(cs);
+    } else {
+        cx_q* cs = (cx_q*)calloc((size_t)(cols > 0 ? cols : 1), sizeof(cx_q));
+        for (int64_t j = 0; j < cols; ++j)
+            for (int64_t i = 0; i < rows; ++i) {
+                cx_q a = ld_q(A, ld, i, j);
+                cs[j].re += (quad_t_)row_mult[i] * a.re;
+                cs[j].im += (quad_t_)row_mult[i] * a.im;
+            }
+        acc_t_q acc = {0, 0, 0, 0};
+        glynn_rep_rec_q(A, rows, cols, ld, lim, cm, cs, 1, imin, 1, &acc);
+        cx_q r = acc_get_q(&acc);
+        quad_t_ s = pow2_neg_q(sout - 1);
+        r.re *= s; r.im *= s;
+        put_q(r, out);
+        free(cs);
+    }
+    free(lim);
+    free(cm);
+    return 0;
+}
+
+/* ---------------------------------------------------------- simple Glynn */
+/* GlynnPermanentCalculatorSimple.hpp:61-168.  Non-square input returns 0
+ * (the reference prints a message and returns 0). */
+int orc_glynn_simple(const double* A, int64_t rows, int64_t cols, int64_t ld, int prec,
+                     double* out) {
+    if (rows == 0 || cols == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        return 0;
+    }
+    if (rows != cols) {
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return 0;
+    }
+    if (rows > 30) return set_err(3, "orc_glynn_simple: too many rows");
+    if (prec == 0) put_d(simple_d(A, rows, ld), out);
+    else put_q(simple_q(A, rows, ld), out);
+    return 0;
+}
+
+/* ------------------------------------------------- submatrix extraction */
+/* adaptInterferometer, BatchedPermanentCalculator.cpp:412-451: keep the rows
+ * of nonzero output occupation and the columns of nonzero input occupation. */
+int orc_adapt_interferometer(const double* U, int64_t m, int64_t ld, const int64_t* input_state,
+                             const int64_t* output_state, double* out, int64_t* out_rows,
+                             int64_t* out_cols) {
+    int64_t nr = 0, nc = 0;
+    for (int64_t i = 0; i < m; ++i) nr += output_state[i] > 0;
+    for (int64_t j = 0; j < m; ++j) nc += input_state[j] > 0;
+    *out_rows = nr;
+    *out_cols = nc;
+    if (!out) return 0;
+    int64_t r = 0;
+    for (int64_t i = 0; i < m; ++i) {
+        if (output_state[i] <= 0) continue;
+        int64_t c = 0;
+        for (int64_t j = 0; j < m; ++j) {
+            if (input_state[j] <= 0) continue;
+            out[2 * (r * nc + c)] = U[2 * (i * ld + j)];
+            out[2 * (r * nc + c) + 1] = U[2 * (i * ld + j) + 1];
+            ++c;
+        }
+        ++r;
+    }
+    return 0;
+}
+
+/* adaptInterferometerGlynnMultiplied, BatchedPermanentCalculator.cpp:367-399:
+ * row i repeated output_state[i] times, column j input_state[j] times. */
+int orc_adapt_interferometer_multiplied(const double* U, int64_t m, int64_t ld,
+                                        const int64_t* input_state, const int64_t* output_state,
+                                        double* out, int64_t* out_n) {
+    int64_t n = 0;
+    for (int64_t j = 0; j < m; ++j) n += input_state[j];
+    *out_n = n;
+    if (!out) return 0;
+    int64_t r = 0;
+    for (int64_t i = 0; i < m; ++i)
+        for (int64_t rr = 0; rr < output_state[i]; ++rr) {
+            int64_t c = 0;
+            for (int64_t j = 0; j < m; ++j)
+                for (int64_t cc = 0; cc < input_state[j]; ++cc) {
+                    out[2 * (r * n + c)] = U[2 * (i * ld + j)];
+                    out[2 * (r * n + c) + 1] = U[2 * (i * ld + j) + 1];
+                    ++c;
+                }
+            ++r;
+        }
+    return 0;
+}

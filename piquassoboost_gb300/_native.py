@@ -1,0 +1,149 @@
+"""ctypes binding of libgbperm.so (the C ABI declared in include/gbperm.h).
+
+The library is loaded from the package's own ``_lib`` folder (built in-tree by
+``piquassoboost_gb300.build``).  There is no CPU fallback: if the library is
+missing or no CUDA device is visible, every compute call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from .build import LIB_PATH
+
+GBPERM_OK = 0
+GBPERM_ERR_ARG = 1
+GBPERM_ERR_STATE_SUM = 2
+GBPERM_ERR_TOO_LARGE = 3
+GBPERM_ERR_CUDA = 4
+GBPERM_ERR_LIB = 5
+GBPERM_ERR_NO_DEVICE = 6
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+
+
+class Stats(ctypes.Structure):
+    """Mirror of gbperm_stats."""
+
+    _fields_ = [
+        ("kernel_ms", ctypes.c_double),
+        ("steps", ctypes.c_double),
+        ("flops", ctypes.c_double),
+        ("launches", ctypes.c_int32),
+        ("grid", ctypes.c_int32),
+        ("seg_log2", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class GBPermError(Exception):
+    """Raised when a libgbperm call returns a non-zero status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+# (name, restype, argtypes) of every exported entry point
+_SIGNATURES = [
+    ("gbperm_version", ctypes.c_int, []),
+    ("gbperm_last_error", ctypes.c_char_p, []),
+    ("gbperm_device_count", ctypes.c_int, []),
+    ("gbperm_set_option", ctypes.c_int, [ctypes.c_char_p, _I64]),
+    ("gbperm_get_option", _I64, [ctypes.c_char_p]),
+    ("gbperm_perm", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P, _P]),
+    ("gbperm_perm_workspace_size", ctypes.c_size_t, [_I64, _I64]),
+    ("gbperm_perm_dev", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P, _P, ctypes.c_size_t, _P]),
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Load libgbperm.so once; raise RuntimeError if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            if build_if_missing:
+                from .build import build_native
+
+                build_native()
+            else:
+                raise RuntimeError(
+                    f"libgbperm.so not found at {LIB_PATH}; build it with "
+                    "`python -m piquassoboost_gb300.build` (the GPU path has no CPU fallback)")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, res, args in _SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def exported_symbols() -> list[str]:
+    return [name for name, _, _ in _SIGNATURES]
+
+
+def check(rc: int) -> None:
+    if rc != GBPERM_OK:
+        msg = load().gbperm_last_error().decode("utf-8", "replace")
+        raise GBPermError(rc, msg)
+
+
+def require_device() -> None:
+    if load().gbperm_device_count() <= 0:
+        raise GBPermError(GBPERM_ERR_NO_DEVICE,
+                          "no CUDA device visible: the GB300 permanent library needs a GPU")
+
+
+def set_option(key: str, value: int) -> None:
+    check(load().gbperm_set_option(key.encode(), int(value)))
+
+
+def get_option(key: str) -> int:
+    return int(load().gbperm_get_option(key.encode()))
+
+
+def as_matrix(matrix) -> np.ndarray:
+    """complex128, C-contiguous, 2-D (a 1-D array of length n is n x 1, as the
+    reference's numpy2matrix does, common/numpy_interface.cpp:145-151)."""
+    a = np.asarray(matrix)
+    if a.ndim == 1:
+        a = a.reshape(-1, 1)
+    if a.ndim != 2:
+        raise ValueError("numpy2matrix: Wrong matrix dimension was given")
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def perm(matrix, return_dd: bool = False, stats: Stats | None = None):
+    """Plain permanent on the GPU through gbperm_perm (host buffers)."""
+    lib = load()
+    a = as_matrix(matrix)
+    rows, cols = a.shape
+    out = np.zeros(2)
+    dd = np.zeros(4)
+    if rows > 0 and cols > 0 and rows < cols + 2:
+        require_device()
+    rc = lib.gbperm_perm(a.ctypes.data_as(_P), rows, cols, cols, out.ctypes.data_as(_P),
+                         dd.ctypes.data_as(_P),
+                         ctypes.byref(stats) if stats is not None else None)
+    check(rc)
+    if return_dd:
+        return complex(out[0], out[1]), dd
+    return complex(out[0], out[1])

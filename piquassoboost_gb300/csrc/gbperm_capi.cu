@@ -1,0 +1,296 @@
+// C ABI (include/gbperm.h): validation, workspace management and dispatch.
+//
+// The reference's wrappers throw std::string from C++ and turn it into a
+// Python exception (GlynnPermanentCalculator_Wrapper.hpp:234-237); here every
+// failure is a status code plus a per-thread message.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+
+#include "gbperm.h"
+#include "gbperm_capi_internal.h"
+
+namespace gbperm {
+
+thread_local std::string t_err;
+
+int fail(int code, const std::string& msg) {
+    t_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fail(GBPERM_ERR_CUDA, m);
+}
+
+Options g_opt;
+
+int device_sms(int dev) {
+    static std::mutex mu;
+    static std::unordered_map<int, int> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    cache[dev] = sms;
+    return sms;
+}
+
+ThreadCtx& thread_ctx() {
+    thread_local ThreadCtx c;
+    return c;
+}
+
+int ThreadCtx::ensure(size_t bytes) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (device != dev) {
+        // a new device for this thread: drop the old resources (they belong
+        // to the old device's context)
+        stream = nullptr;
+        dbuf = nullptr;
+        dcap = 0;
+        device = dev;
+        e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+        e = cudaEventCreate(&ev0);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+        e = cudaEventCreate(&ev1);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    }
+    if (bytes > dcap) {
+        if (dbuf) cudaFree(dbuf);
+        dbuf = nullptr;
+        dcap = 0;
+        size_t want = align_up(bytes, 1 << 20);
+        e = cudaMalloc(&dbuf, want);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(workspace)");
+        dcap = want;
+    }
+    return GBPERM_OK;
+}
+
+bool all_finite(const double* A, int64_t rows, int64_t cols, int64_t ld) {
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < 2 * cols; ++j)
+            if (!std::isfinite(A[2 * i * ld + j])) return false;
+    return true;
+}
+
+int ceil_log2_u64(unsigned long long x) {
+    int l = 0;
+    while ((1ull << l) < x && l < 63) ++l;
+    return l;
+}
+
+// ------------------------------------------------------------------ plain
+
+PlainPlan plan_plain(int rows, int cols) {
+    PlainPlan p;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = device_sms(dev);
+    int bps = plain_blocks_per_sm(rows, cols);
+    int grid_full = sms * bps;
+    int slog = rows - 1;
+    // aim at >= 64 segments per thread (load balance within ~1.5%) while
+    // keeping segments >= 16 steps when the problem allows it
+    unsigned long long T = (unsigned long long)grid_full * 128ull;
+    int l = slog - ceil_log2_u64(64ull * T);
+    if (l < 4) l = slog < 4 ? slog : 4;
+    if (l > slog) l = slog;
+    if (l < 0) l = 0;
+    int64_t force = g_opt.plain_seg_log2.load();
+    if (force >= 0) l = (int)(force > slog ? slog : force);
+    unsigned long long nseg = 1ull << (slog - l);
+    unsigned long long need = (nseg + 127ull) / 128ull;
+    int grid = (int)(need < (unsigned long long)grid_full ? need : (unsigned long long)grid_full);
+    int64_t fg = g_opt.plain_grid.load();
+    if (fg > 0) grid = (int)fg;
+    if (grid < 1) grid = 1;
+    p.grid = grid;
+    p.seg_log2 = l;
+    return p;
+}
+
+size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w) {
+    size_t off = 0;
+    size_t mat = align_up((size_t)rows * cols * sizeof(longlong2), 256);
+    if (w) w->a1 = off;
+    off += mat;
+    if (w) w->a2 = off;
+    off += mat;
+    if (w) w->exp = off;
+    off += 256;
+    if (w) w->kern = off;
+    off += plain_workspace_bytes(grid);
+    return off;
+}
+
+int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, size_t ws_bytes,
+                  double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan) {
+    PlainWs w;
+    size_t need = plain_ws_layout(rows, cols, plan.grid, &w);
+    if (ws_bytes < need) return fail(GBPERM_ERR_ARG, "gbperm: workspace too small");
+    char* base = static_cast<char*>(ws);
+    PrepArgs pa;
+    pa.A = dA;
+    pa.ld = ld;
+    pa.rows = rows;
+    pa.cols = cols;
+    pa.row_w = nullptr;
+    pa.col_w = nullptr;
+    pa.norm_shift = rows - 1;
+    pa.a1 = reinterpret_cast<longlong2*>(base + w.a1);
+    pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
+    pa.exp_out = reinterpret_cast<int*>(base + w.exp);
+    cudaError_t e = launch_prepare(pa, st);
+    if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
+    e = launch_plain(pa.a1, pa.a2, pa.exp_out, rows, cols, plan.grid, plan.seg_log2, base + w.kern,
+                     d_out2, d_out4, st);
+    if (e != cudaSuccess) return cuda_fail(e, "plain launch");
+    return GBPERM_OK;
+}
+
+// Trivial shapes shared by the plain entry points; returns true when `out`
+// has been filled without any GPU work.
+bool plain_trivial(int64_t rows, int64_t cols, double* out, double* out_dd) {
+    double v = -1.0;
+    if (rows == 0 || cols == 0) v = 1.0;
+    else if (rows >= cols + 2) v = 0.0;
+    if (v < 0.0) return false;
+    out[0] = v;
+    out[1] = 0.0;
+    if (out_dd) {
+        out_dd[0] = v;
+        out_dd[1] = out_dd[2] = out_dd[3] = 0.0;
+    }
+    return true;
+}
+
+}  // namespace gbperm
+
+using namespace gbperm;
+
+extern "C" {
+
+int gbperm_version(void) { return 100; }
+
+const char* gbperm_last_error(void) { return t_err.c_str(); }
+
+int gbperm_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int gbperm_set_option(const char* key, int64_t value) {
+    if (!key) return fail(GBPERM_ERR_ARG, "gbperm_set_option: null key");
+    std::atomic<int64_t>* slot = g_opt.find(key);
+    if (!slot) return fail(GBPERM_ERR_ARG, std::string("gbperm_set_option: unknown key ") + key);
+    slot->store(value);
+    return GBPERM_OK;
+}
+
+int64_t gbperm_get_option(const char* key) {
+    if (!key) return 0;
+    std::atomic<int64_t>* slot = g_opt.find(key);
+    return slot ? slot->load() : 0;
+}
+
+size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols) {
+    if (rows <= 0 || cols <= 0 || rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM) return 256;
+    PlainPlan plan = plan_plain((int)rows, (int)cols);
+    return plain_ws_layout((int)rows, (int)cols, plan.grid, nullptr);
+}
+
+int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, void* d_out,
+                    void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream) {
+    if (rows < 0 || cols < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: negative shape");
+    if (!d_out) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: null output");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double hv[4];
+    if (plain_trivial(rows, cols, hv, hv)) {
+        hv[1] = 0.0;
+        hv[2] = hv[3] = 0.0;
+        double h2[2] = {hv[0], 0.0};
+        cudaError_t e = cudaMemcpyAsync(d_out, h2, sizeof(h2), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && d_out_dd) e = cudaMemcpyAsync(d_out_dd, hv, sizeof(hv), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        return e == cudaSuccess ? GBPERM_OK : cuda_fail(e, "gbperm_perm_dev");
+    }
+    if (!dA || !workspace) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: null pointer");
+    if (ld < cols) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: ld < cols");
+    if (rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM)
+        return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_dev: matrix larger than 64 x 64");
+    if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+        return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: workspace must be 256-byte aligned");
+    PlainPlan plan = plan_plain((int)rows, (int)cols);
+    return run_plain_dev(static_cast<const double2*>(dA), ld, (int)rows, (int)cols, workspace,
+                         workspace_bytes, static_cast<double*>(d_out), static_cast<double*>(d_out_dd), st,
+                         plan);
+}
+
+int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, double* out, double* out_dd,
+                gbperm_stats* stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (!out) return fail(GBPERM_ERR_ARG, "gbperm_perm: null output");
+    if (rows < 0 || cols < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm: negative shape");
+    if (plain_trivial(rows, cols, out, out_dd)) return GBPERM_OK;
+    if (!A) return fail(GBPERM_ERR_ARG, "gbperm_perm: null matrix");
+    if (ld < cols) return fail(GBPERM_ERR_ARG, "gbperm_perm: ld < cols");
+    if (rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM)
+        return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm: matrix larger than 64 x 64");
+    if (!all_finite(A, rows, cols, ld)) {
+        out[0] = out[1] = NAN;
+        if (out_dd) out_dd[0] = out_dd[1] = out_dd[2] = out_dd[3] = NAN;
+        return GBPERM_OK;
+    }
+    PlainPlan plan = plan_plain((int)rows, (int)cols);
+    size_t mat_bytes = align_up((size_t)rows * cols * sizeof(double2), 256);
+    size_t ws = plain_ws_layout((int)rows, (int)cols, plan.grid, nullptr);
+    ThreadCtx& c = thread_ctx();
+    int rc = c.ensure(mat_bytes + 256 + ws);
+    if (rc) return rc;
+    char* base = static_cast<char*>(c.dbuf);
+    double2* dA = reinterpret_cast<double2*>(base);
+    double* dout = reinterpret_cast<double*>(base + mat_bytes);  // 6 doubles: out2, out4
+    void* dws = base + mat_bytes + 256;
+    cudaError_t e = cudaMemcpy2DAsync(dA, cols * sizeof(double2), A, ld * sizeof(double2),
+                                      cols * sizeof(double2), rows, cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm: upload");
+    if (stats) cudaEventRecord(c.ev0, c.stream);
+    rc = run_plain_dev(dA, cols, (int)rows, (int)cols, dws, ws, dout, dout + 2, c.stream, plan);
+    if (rc) return rc;
+    if (stats) cudaEventRecord(c.ev1, c.stream);
+    double h[6];
+    e = cudaMemcpyAsync(h, dout, sizeof(h), cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm: download");
+    e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm: kernel");
+    out[0] = h[0];
+    out[1] = h[1];
+    if (out_dd) std::memcpy(out_dd, h + 2, 4 * sizeof(double));
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        stats->kernel_ms = ms;
+        stats->steps = std::ldexp(1.0, (int)rows - 1);
+        stats->flops = 8.0 * (double)cols * stats->steps;
+        stats->launches = 2;
+        stats->grid = plan.grid;
+        stats->seg_log2 = plan.seg_log2;
+    }
+    return GBPERM_OK;
+}
+
+}  // extern "C"

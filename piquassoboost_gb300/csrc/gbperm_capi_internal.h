@@ -1,0 +1,79 @@
+// Host-side internals of the C ABI: options, per-thread context, plans.
+#pragma once
+#include <atomic>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbperm_internal.h"
+
+namespace gbperm {
+
+extern thread_local std::string t_err;
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+
+struct Options {
+    std::atomic<int64_t> plain_seg_log2{-1};
+    std::atomic<int64_t> plain_grid{0};
+    std::atomic<int64_t> repeated_low_digits{-1};
+    std::atomic<int64_t> batched_threads{0};
+    std::atomic<int64_t>* find(const char* key) {
+        if (!std::strcmp(key, "plain.seg_log2")) return &plain_seg_log2;
+        if (!std::strcmp(key, "plain.grid")) return &plain_grid;
+        if (!std::strcmp(key, "repeated.low_digits")) return &repeated_low_digits;
+        if (!std::strcmp(key, "batched.threads")) return &batched_threads;
+        return nullptr;
+    }
+};
+extern Options g_opt;
+
+int device_sms(int dev);
+bool all_finite(const double* A, int64_t rows, int64_t cols, int64_t ld);
+int ceil_log2_u64(unsigned long long x);
+
+// Per-thread stream, timing events and a growable device buffer used by the
+// host-pointer entry points.  Resources are kept until the process exits.
+struct ThreadCtx {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void* dbuf = nullptr;
+    size_t dcap = 0;
+    int ensure(size_t bytes);
+};
+ThreadCtx& thread_ctx();
+
+struct PlainPlan {
+    int grid = 1;
+    int seg_log2 = 0;
+};
+struct PlainWs {
+    size_t a1 = 0, a2 = 0, exp = 0, kern = 0;
+};
+PlainPlan plan_plain(int rows, int cols);
+size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w);
+int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, size_t ws_bytes,
+                  double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan);
+bool plain_trivial(int64_t rows, int64_t cols, double* out, double* out_dd);
+
+// Repeated-multiplicity plan built on the host (host_repeated.cu).
+struct RepHost {
+    bool transpose = false;
+    int R = 0, C = 0, nd = 0, q = 0, photons = 0;
+    unsigned long long P = 1, nseg = 1;
+    double steps = 0.0, flops = 0.0;
+    std::vector<double> M;        // R x C complex128 (interleaved), digit rows first
+    std::vector<int> rcoef, D, cpow;
+    std::vector<double> wlow;
+    std::vector<unsigned char> seq;
+};
+struct RepWs {
+    size_t M = 0, a1 = 0, a2 = 0, ints = 0, wlow = 0, seq = 0, binom = 0, exp = 0, out = 0, kern = 0;
+};
+int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
+                  int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
+                  bool* is_trivial);
+size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w);
+
+}  // namespace gbperm

@@ -1,0 +1,349 @@
+// Host side of the repeated-multiplicity permanent: validation with the
+// reference's semantics, compaction, orientation, digit plan and launch.
+//
+// Reference semantics (BBFGPermanentCalculatorRepeated.cpp:75-141, .hpp
+// :74-141; ChinHuhPermanentCalculator_Wrapper.hpp:367-375):
+//   * col_mult is the input state, row_mult the output state;
+//   * rows == 0 -> 1; sum(col_mult) != sum(row_mult) -> error;
+//     sum == 0 -> 1;
+//   * only the first len(row_mult) rows / len(col_mult) columns are used.
+// Rows and columns of zero multiplicity do not change the value and are
+// dropped; the permanent is invariant under transposition (with the roles of
+// the multiplicities swapped), so the orientation with the shorter Gray code
+// is used.  The fixed delta = +1 copy goes to the row of smallest
+// multiplicity, as in the reference (which prepends that row, .hpp:78-94).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "gbperm.h"
+#include "gbperm_capi_internal.h"
+
+namespace gbperm {
+
+namespace {
+
+const std::vector<double>& binom_table() {
+    static std::vector<double> t;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        t.assign(kBinomStride * kBinomStride, 0.0);
+        unsigned long long C[kBinomStride][kBinomStride];  // exact: C(64, 32) < 2^64
+        std::memset(C, 0, sizeof(C));
+        for (int n = 0; n < kBinomStride; ++n) {
+            C[n][0] = 1;
+            for (int k = 1; k <= n; ++k) C[n][k] = C[n - 1][k - 1] + (k <= n - 1 ? C[n - 1][k] : 0);
+        }
+        for (int n = 0; n < kBinomStride; ++n)
+            for (int k = 0; k <= n; ++k) t[n * kBinomStride + k] = (double)C[n][k];
+    });
+    return t;
+}
+
+}  // namespace
+
+int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
+                  int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
+                  bool* is_trivial) {
+    *is_trivial = false;
+    if (rows == 0) {
+        trivial[0] = 1.0;
+        trivial[1] = 0.0;
+        *is_trivial = true;
+        return GBPERM_OK;
+    }
+    if (nrow > rows) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: output state longer than the matrix rows");
+    if (ncol > cols) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: input state longer than the matrix columns");
+    if (nrow > 0 && !row_mult) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: null output state");
+    if (ncol > 0 && !col_mult) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: null input state");
+    int64_t sr = 0, sc = 0;
+    for (int64_t i = 0; i < nrow; ++i) {
+        if (row_mult[i] < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: negative occupation");
+        sr += row_mult[i];
+    }
+    for (int64_t j = 0; j < ncol; ++j) {
+        if (col_mult[j] < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: negative occupation");
+        sc += col_mult[j];
+    }
+    if (sr != sc)
+        return fail(GBPERM_ERR_STATE_SUM,
+                    "BBFGPermanentCalculatorRepeated_Tasks::calculate:  Number of input and output states should be equal");
+    if (sr == 0 || cols == 0) {
+        trivial[0] = 1.0;
+        trivial[1] = 0.0;
+        *is_trivial = true;
+        return GBPERM_OK;
+    }
+    if (sr > 64) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_repeated: more than 64 photons");
+    if (!A) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: null matrix");
+    if (ld < cols) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: ld < cols");
+
+    std::vector<int> ri, ci;  // occupied row / column indices
+    for (int64_t i = 0; i < nrow; ++i)
+        if (row_mult[i] > 0) ri.push_back((int)i);
+    for (int64_t j = 0; j < ncol; ++j)
+        if (col_mult[j] > 0) ci.push_back((int)j);
+    if (ri.size() > (size_t)kMaxRows || ci.size() > (size_t)GBPERM_MAX_DIM)
+        return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_repeated: more than 64 occupied modes");
+
+    // Gray length of one orientation: prod (D_i + 1) with the fixed copy on
+    // the smallest multiplicity
+    auto gray_len = [](const std::vector<int>& idx, const int64_t* mult) {
+        int64_t mn = INT64_MAX;
+        for (int i : idx) mn = std::min(mn, mult[i]);
+        long double t = 1.0L;
+        for (int i : idx) t *= (long double)(mult[i] + 1);
+        return t * (long double)mn / (long double)(mn + 1);
+    };
+    long double t_rows = gray_len(ri, row_mult), t_cols = gray_len(ci, col_mult);
+    bool transpose = t_cols < t_rows;
+    h->transpose = transpose;
+    const std::vector<int>& gi = transpose ? ci : ri;   // Gray-code side (rows of M)
+    const std::vector<int>& pj = transpose ? ri : ci;   // product side (columns of M)
+    const int64_t* gm = transpose ? col_mult : row_mult;
+    const int64_t* pm = transpose ? row_mult : col_mult;
+    int R = (int)gi.size(), C = (int)pj.size();
+    if (C > GBPERM_MAX_DIM) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_repeated: more than 64 occupied modes");
+
+    // fixed copy: first occurrence of the smallest multiplicity
+    int fixed = 0;
+    for (int i = 1; i < R; ++i)
+        if (gm[gi[i]] < gm[gi[fixed]]) fixed = i;
+
+    struct RowInfo {
+        int src;   // index into gi
+        int r;     // multiplicity
+        int D;     // digit range
+    };
+    std::vector<RowInfo> digits, consts;
+    for (int i = 0; i < R; ++i) {
+        int r = (int)gm[gi[i]];
+        int D = (i == fixed) ? r - 1 : r;
+        if (D >= 1) digits.push_back({i, r, D});
+        else consts.push_back({i, r, D});
+    }
+    // small ranges first: they can be low digits (4-bit packed, D <= 15)
+    std::stable_sort(digits.begin(), digits.end(),
+                     [](const RowInfo& a, const RowInfo& b) { return (a.D <= 15) > (b.D <= 15); });
+    long double total = 1.0L;
+    for (auto& d : digits) total *= (long double)(d.D + 1);
+    if (total > 9.0e18L) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_repeated: Gray range beyond 2^63");
+    unsigned long long T = 1ull;
+    for (auto& d : digits) T *= (unsigned long long)(d.D + 1);
+
+    // low digits: grow P while segments stay plentiful (>= 64 per thread of
+    // a full grid) and the weight table small (<= 4096 entries)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned long long threads = (unsigned long long)device_sms(dev) * 2ull * 128ull;
+    int64_t force_q = g_opt.repeated_low_digits.load();
+    int q = 0;
+    unsigned long long P = 1ull;
+    for (size_t i = 0; i < digits.size() && i < 16; ++i) {
+        if (digits[i].D > 15) break;
+        unsigned long long L = (unsigned long long)(digits[i].D + 1);
+        if (force_q >= 0) {
+            if ((int64_t)q >= force_q) break;
+        } else {
+            if (P * L > 4096ull) break;
+            if (T / (P * L) < 64ull * threads && P >= 16ull) break;
+        }
+        P *= L;
+        ++q;
+    }
+
+    h->R = R;
+    h->C = C;
+    h->nd = (int)digits.size();
+    h->q = q;
+    h->P = P;
+    h->nseg = T / P;
+    h->steps = (double)T;
+    h->photons = (int)sr;
+    // matrix M (rows: digits then constants) as complex128, dense
+    h->M.assign((size_t)R * C * 2, 0.0);
+    h->rcoef.clear();
+    h->D.clear();
+    std::vector<RowInfo> order = digits;
+    order.insert(order.end(), consts.begin(), consts.end());
+    for (int r = 0; r < R; ++r) {
+        int src = gi[order[r].src];
+        for (int c = 0; c < C; ++c) {
+            int dst = pj[c];
+            int64_t ii = transpose ? dst : src, jj = transpose ? src : dst;
+            h->M[2 * ((size_t)r * C + c)] = A[2 * (ii * ld + jj)];
+            h->M[2 * ((size_t)r * C + c) + 1] = A[2 * (ii * ld + jj) + 1];
+        }
+        h->rcoef.push_back(order[r].r);
+        if (r < h->nd) h->D.push_back(order[r].D);
+    }
+    h->cpow.clear();
+    for (int c = 0; c < C; ++c) h->cpow.push_back((int)pm[pj[c]]);
+    // low-digit tables
+    h->wlow.assign(P, 1.0);
+    h->seq.assign(P, 0);
+    const std::vector<double>& bt = binom_table();
+    for (unsigned long long k = 0; k < P; ++k) {
+        unsigned long long rem = k;
+        double w = 1.0;
+        for (int i = 0; i < q; ++i) {
+            unsigned long long L = (unsigned long long)(h->D[i] + 1);
+            int g = (int)(rem % L);
+            rem /= L;
+            w *= bt[h->D[i] * kBinomStride + g];
+        }
+        h->wlow[k] = w;
+        if (k > 0) {
+            unsigned long long kk = k;
+            int d = 0;
+            while (d < q && kk % (unsigned long long)(h->D[d] + 1) == 0) {
+                kk /= (unsigned long long)(h->D[d] + 1);
+                ++d;
+            }
+            h->seq[k] = (unsigned char)d;
+        }
+    }
+    double fl = 0.0;  // algorithmic flops: colsum updates + product + accumulate
+    int mults = 0;
+    for (int c = 0; c < C; ++c) mults += h->cpow[c];
+    mults -= 1;
+    fl = (2.0 * C + 6.0 * mults + 2.0) * (double)T;
+    h->flops = fl;
+    return GBPERM_OK;
+}
+
+size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += align_up(bytes, 256);
+        return o;
+    };
+    RepWs l;
+    l.M = take(h.M.size() * sizeof(double));
+    l.a1 = take((size_t)h.R * h.C * sizeof(longlong2));
+    l.a2 = take((size_t)h.R * h.C * sizeof(longlong2));
+    l.ints = take((size_t)(h.R + h.nd + h.C + 64) * sizeof(int));
+    l.wlow = take(h.wlow.size() * sizeof(double));
+    l.seq = take(h.seq.size());
+    l.binom = take((size_t)kBinomStride * kBinomStride * sizeof(double));
+    l.exp = take(16);
+    l.out = take(8 * sizeof(double));
+    l.kern = take(repeated_workspace_bytes(grid));
+    if (w) *w = l;
+    return off;
+}
+
+}  // namespace gbperm
+
+using namespace gbperm;
+
+extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
+                                    const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
+                                    int64_t nrow, double* out, double* out_dd, gbperm_stats* stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (!out) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: null output");
+    if (rows < 0 || cols < 0 || nrow < 0 || ncol < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: negative size");
+    RepHost h;
+    double triv[2];
+    bool is_triv = false;
+    int rc = repeated_plan(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, &h, triv, &is_triv);
+    if (rc) return rc;
+    if (is_triv) {
+        out[0] = triv[0];
+        out[1] = triv[1];
+        if (out_dd) {
+            out_dd[0] = triv[0];
+            out_dd[1] = triv[1];
+            out_dd[2] = out_dd[3] = 0.0;
+        }
+        return GBPERM_OK;
+    }
+    if (!all_finite(h.M.data(), h.R, h.C, h.C)) {
+        out[0] = out[1] = NAN;
+        if (out_dd) out_dd[0] = out_dd[1] = out_dd[2] = out_dd[3] = NAN;
+        return GBPERM_OK;
+    }
+    // launch geometry
+    RepArgs a{};
+    a.R = h.R;
+    a.C = h.C;
+    a.nd = h.nd;
+    a.q = h.q;
+    a.P = h.P;
+    a.nseg = h.nseg;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int bps = repeated_blocks_per_sm(a);
+    unsigned long long grid_full = (unsigned long long)device_sms(dev) * bps;
+    unsigned long long need = (h.nseg + 127ull) / 128ull;
+    int grid = (int)std::max(1ull, std::min(grid_full, need));
+    RepWs w;
+    size_t bytes = repeated_ws_layout(h, grid, &w);
+    ThreadCtx& c = thread_ctx();
+    rc = c.ensure(bytes);
+    if (rc) return rc;
+    char* base = static_cast<char*>(c.dbuf);
+    cudaStream_t st = c.stream;
+    std::vector<int> ints;
+    ints.insert(ints.end(), h.rcoef.begin(), h.rcoef.end());
+    ints.insert(ints.end(), h.D.begin(), h.D.end());
+    ints.insert(ints.end(), h.cpow.begin(), h.cpow.end());
+    cudaError_t e = cudaMemcpyAsync(base + w.M, h.M.data(), h.M.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + w.ints, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + w.wlow, h.wlow.data(), h.wlow.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + w.seq, h.seq.data(), h.seq.size(), cudaMemcpyHostToDevice, st);
+    const std::vector<double>& bt = binom_table();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + w.binom, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: upload");
+    const int* d_ints = reinterpret_cast<const int*>(base + w.ints);
+    PrepArgs pa;
+    pa.A = reinterpret_cast<const double2*>(base + w.M);
+    pa.ld = h.C;
+    pa.rows = h.R;
+    pa.cols = h.C;
+    pa.row_w = d_ints;
+    pa.col_w = d_ints + h.R + h.nd;
+    pa.norm_shift = h.photons - 1;
+    pa.a1 = reinterpret_cast<longlong2*>(base + w.a1);
+    pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
+    pa.exp_out = reinterpret_cast<int*>(base + w.exp);
+    if (stats) cudaEventRecord(c.ev0, st);
+    e = launch_prepare(pa, st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: prepare");
+    a.a1 = pa.a1;
+    a.a2 = pa.a2;
+    a.rcoef = d_ints;
+    a.D = d_ints + h.R;
+    a.cpow = d_ints + h.R + h.nd;
+    a.wlow = reinterpret_cast<const double*>(base + w.wlow);
+    a.seq = reinterpret_cast<const unsigned char*>(base + w.seq);
+    a.binom = reinterpret_cast<const double*>(base + w.binom);
+    a.exp_in = pa.exp_out;
+    double* dout = reinterpret_cast<double*>(base + w.out);
+    a.out2 = dout;
+    a.out4 = dout + 2;
+    e = launch_repeated(a, grid, base + w.kern, st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: launch");
+    if (stats) cudaEventRecord(c.ev1, st);
+    double hres[6];
+    e = cudaMemcpyAsync(hres, dout, sizeof(hres), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: kernel");
+    out[0] = hres[0];
+    out[1] = hres[1];
+    if (out_dd) std::memcpy(out_dd, hres + 2, 4 * sizeof(double));
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        stats->kernel_ms = ms;
+        stats->steps = h.steps;
+        stats->flops = h.flops;
+        stats->launches = 2;
+        stats->grid = grid;
+        stats->seg_log2 = h.q;
+    }
+    return GBPERM_OK;
+}

@@ -1,0 +1,239 @@
+// Plain Glynn / BBFG permanent of one rows x cols complex matrix (GB300).
+//
+// Replaces BBFGPermanentCalculator_Tasks::calculate
+// (piquassoboost/sampling/source/BBFGPermanentCalculator.hpp:87-235) and the
+// recursive GlynnPermanentCalculator (GlynnPermanentCalculator.hpp:47-201):
+//   perm = 2^-(rows-1) * sum_{delta in {+-1}^rows, delta_0 = +1}
+//          (prod_i delta_i) * prod_j (sum_i delta_i a_ij)
+// over the binary-reflected Gray code of rows 1..rows-1 (bit b of the Gray
+// code <-> row rows-1-b, as in the reference).
+//
+// Work split: the 2^(rows-1) Gray indices are cut into aligned segments of
+// L = 2^l steps.  Inside an aligned segment the changed row at local step k is
+// rows-1-ctz(k) for every segment, so all lanes of a warp touch the same row
+// at the same time (a shared-memory broadcast); only the add/subtract
+// direction is per lane.  Each thread walks segments t, t+T, t+2T, ...
+// Column sums are exact 64-bit fixed point (no drift); the product runs in
+// FP64; terms are summed in double per 256 steps and folded into a
+// double-double accumulator; the grid reduction is double-double and its
+// order is fixed, so results are bitwise reproducible.
+#include "gbperm_internal.h"
+
+namespace gbperm {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+struct PlainArgs {
+    const longlong2* a1;   // rows x cols fixed-point a_ij (unit 2^-62 after column scaling)
+    const longlong2* a2;   // rows x cols fixed-point 2 a_ij
+    int rows, cols;
+    int seg_log2;          // L = 2^seg_log2
+    unsigned long long nseg;
+    cdd* block_part;       // gridDim.x partial sums
+    unsigned int* done;    // completion counter (zero before the launch)
+    const int* exp_in;     // final scale exponent (from the prepare kernel)
+    double* out2;          // complex128 result
+    double* out4;          // optional: {re_hi, im_hi, re_lo, im_lo} of the scaled result
+};
+
+template <int NMAX>
+__global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);
+    longlong2* s_a2 = s_a1 + p.rows * NMAX;
+    const int rows = p.rows, cols = p.cols;
+    for (int e = threadIdx.x; e < rows * NMAX; e += blockDim.x) {
+        int r = e / NMAX, j = e % NMAX;
+        longlong2 z = make_longlong2(0, 0);
+        s_a1[e] = j < cols ? p.a1[r * cols + j] : z;
+        s_a2[e] = j < cols ? p.a2[r * cols + j] : z;
+    }
+    __syncthreads();
+
+    cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    const unsigned long long L = 1ull << p.seg_log2;
+    const unsigned long long T = (unsigned long long)gridDim.x * blockDim.x;
+    long long cre[NMAX], cim[NMAX];
+
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < p.nseg;
+         s += T) {
+        const unsigned long long i0 = s << p.seg_log2;
+        // exact segment-start sums: row 0 plus/minus rows 1..rows-1 by the Gray bits
+        const unsigned long long g0 = i0 ^ (i0 >> 1);
+#pragma unroll
+        for (int j = 0; j < NMAX; ++j) {
+            cre[j] = s_a1[j].x;
+            cim[j] = s_a1[j].y;
+        }
+        for (int r = 1; r < rows; ++r) {
+            const long long m = -(long long)((g0 >> (rows - 1 - r)) & 1ull);  // 0 (+) or -1 (-)
+            const longlong2* a = s_a1 + r * NMAX;
+#pragma unroll
+            for (int j = 0; j < NMAX; ++j) {
+                longlong2 v = a[j];
+                cre[j] += (v.x ^ m) - m;
+                cim[j] += (v.y ^ m) - m;
+            }
+        }
+        unsigned long long neg = (unsigned long long)(__popcll(g0) & 1) << 63;
+        double bre = 0.0, bim = 0.0;
+        for (unsigned long long k = 0; k < L; ++k) {
+            if (k != 0) {
+                const int b = __ffsll((long long)k) - 1;  // warp-uniform
+                const unsigned long long idx = i0 + k;
+                const long long m = -(long long)(((idx >> b) ^ (idx >> (b + 1))) & 1ull);
+                const longlong2* a = s_a2 + (rows - 1 - b) * NMAX;
+#pragma unroll
+                for (int j = 0; j < NMAX; ++j) {
+                    if (j < cols) {
+                        longlong2 v = a[j];
+                        cre[j] += (v.x ^ m) - m;
+                        cim[j] += (v.y ^ m) - m;
+                    }
+                }
+                neg ^= 0x8000000000000000ull;
+                if ((k & 255ull) == 0) {
+                    acc.re = dd_add_d(acc.re, bre);
+                    acc.im = dd_add_d(acc.im, bim);
+                    bre = 0.0;
+                    bim = 0.0;
+                }
+            }
+            // product of the column sums, two interleaved chains for ILP;
+            // the term sign goes into the first factor's sign bit (integer op)
+            cd pa, pb;
+            pa.re = __longlong_as_double(__double_as_longlong(fix_to_double(cre[0])) ^ (long long)neg);
+            pa.im = __longlong_as_double(__double_as_longlong(fix_to_double(cim[0])) ^ (long long)neg);
+            pb.re = 1.0;
+            pb.im = 0.0;
+            if (cols > 1) {
+                pb.re = fix_to_double(cre[1]);
+                pb.im = fix_to_double(cim[1]);
+            }
+#pragma unroll
+            for (int j = 2; j < NMAX; j += 2) {
+                if (j < cols) pa = cmul(pa, cd{fix_to_double(cre[j]), fix_to_double(cim[j])});
+                if (j + 1 < cols) pb = cmul(pb, cd{fix_to_double(cre[j + 1]), fix_to_double(cim[j + 1])});
+            }
+            if (cols > 1) pa = cmul(pa, pb);
+            bre += pa.re;
+            bim += pa.im;
+        }
+        acc.re = dd_add_d(acc.re, bre);
+        acc.im = dd_add_d(acc.im, bim);
+    }
+
+    // block reduction (double-double, fixed order)
+    __shared__ cdd s_warp[kThreads / 32];
+    __shared__ bool s_last;
+    acc = warp_sum_cdd(acc);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd b = s_warp[0];
+        for (int w = 1; w < kThreads / 32; ++w) b = cdd_add(b, s_warp[w]);
+        p.block_part[blockIdx.x] = b;
+        __threadfence();
+        unsigned int t = atomicAdd(p.done, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        for (unsigned int bk = 0; bk < gridDim.x; ++bk) {
+            const volatile double* q = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
+            cdd v{{q[0], q[1]}, {q[2], q[3]}};
+            tot = cdd_add(tot, v);
+        }
+        write_result(tot, *p.exp_in, p.out2, p.out4);
+        *p.done = 0u;
+    }
+}
+
+template <int NMAX>
+cudaError_t launch_plain_t(const PlainArgs& a, int grid, cudaStream_t st) {
+    size_t smem = 2ull * a.rows * NMAX * sizeof(longlong2);
+    cudaError_t e = cudaFuncSetAttribute(plain_kernel<NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    plain_kernel<NMAX><<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int NMAX>
+int blocks_per_sm_t(int rows) {
+    int nb = 0;
+    size_t smem = 2ull * rows * NMAX * sizeof(longlong2);
+    cudaFuncSetAttribute(plain_kernel<NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, plain_kernel<NMAX>, kThreads, smem);
+    return nb > 0 ? nb : 1;
+}
+
+}  // namespace
+
+int plain_bucket(int cols) {
+    if (cols <= 8) return 8;
+    if (cols <= 16) return 16;
+    if (cols <= 24) return 24;
+    if (cols <= 32) return 32;
+    if (cols <= 40) return 40;
+    if (cols <= 48) return 48;
+    if (cols <= 56) return 56;
+    return 64;
+}
+
+int plain_blocks_per_sm(int rows, int cols) {
+    switch (plain_bucket(cols)) {
+        case 8: return blocks_per_sm_t<8>(rows);
+        case 16: return blocks_per_sm_t<16>(rows);
+        case 24: return blocks_per_sm_t<24>(rows);
+        case 32: return blocks_per_sm_t<32>(rows);
+        case 40: return blocks_per_sm_t<40>(rows);
+        case 48: return blocks_per_sm_t<48>(rows);
+        case 56: return blocks_per_sm_t<56>(rows);
+        default: return blocks_per_sm_t<64>(rows);
+    }
+}
+
+size_t plain_workspace_bytes(int grid) {
+    // block partials + completion counter
+    return align_up((size_t)grid * sizeof(cdd), 256) + 256;
+}
+
+// Launch the plain kernel on device data that is already in fixed point
+// (launch_prepare).  ws must hold plain_workspace_bytes(grid).
+cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* exp_in, int rows,
+                         int cols, int grid, int seg_log2, void* ws, double* out2, double* out4,
+                         cudaStream_t st) {
+    PlainArgs a;
+    a.a1 = a1;
+    a.a2 = a2;
+    a.rows = rows;
+    a.cols = cols;
+    a.seg_log2 = seg_log2;
+    a.nseg = 1ull << (rows - 1 - seg_log2);
+    char* w = static_cast<char*>(ws);
+    a.block_part = reinterpret_cast<cdd*>(w);
+    a.done = reinterpret_cast<unsigned int*>(w + align_up((size_t)grid * sizeof(cdd), 256));
+    a.exp_in = exp_in;
+    a.out2 = out2;
+    a.out4 = out4;
+    cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    switch (plain_bucket(cols)) {
+        case 8: return launch_plain_t<8>(a, grid, st);
+        case 16: return launch_plain_t<16>(a, grid, st);
+        case 24: return launch_plain_t<24>(a, grid, st);
+        case 32: return launch_plain_t<32>(a, grid, st);
+        case 40: return launch_plain_t<40>(a, grid, st);
+        case 48: return launch_plain_t<48>(a, grid, st);
+        case 56: return launch_plain_t<56>(a, grid, st);
+        default: return launch_plain_t<64>(a, grid, st);
+    }
+}
+
+}  // namespace gbperm

@@ -1,0 +1,52 @@
+"""Seeded synthetic inputs with the shapes of the reference's permanent workloads.
+
+All generators are deterministic in their seed (numpy default_rng).  Haar
+unitaries are drawn as the QR factor of a complex Gaussian matrix with the
+phases of R's diagonal divided out of Q's columns.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def haar_unitary(m: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    z = (rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))) / np.sqrt(2.0)
+    q, r = np.linalg.qr(z)
+    d = np.diag(r)
+    return q * (d / np.abs(d))[None, :]
+
+
+def haar_block(n: int, seed: int, m: int | None = None) -> np.ndarray:
+    """Top-left n x n block of a seeded Haar m x m unitary (m = 2n by default)."""
+    u = haar_unitary(m if m is not None else 2 * n, seed)
+    return np.ascontiguousarray(u[:n, :n])
+
+
+def repeated_instance(seed: int, modes: int = 60, photons: int = 30, max_mult: int = 4):
+    """Haar `modes`-mode unitary, one photon in each of modes 0..photons-1,
+    output occupation from a seeded multinomial over all modes with every
+    multiplicity <= max_mult (redrawn otherwise)."""
+    u = haar_unitary(modes, seed)
+    rng = np.random.default_rng(seed + 7919)
+    inp = np.zeros(modes, dtype=np.int64)
+    inp[:photons] = 1
+    while True:
+        out = rng.multinomial(photons, np.ones(modes) / modes).astype(np.int64)
+        if out.max() <= max_mult:
+            break
+    return u, inp, out
+
+
+def batched_instances(count: int, seed: int, modes: int = 100, kmin: int = 8, kmax: int = 28):
+    """`count` square k x k submatrices (k uniform in kmin..kmax) of one seeded
+    Haar `modes`-mode unitary, rows and columns drawn with repetition."""
+    u = haar_unitary(modes, seed)
+    rng = np.random.default_rng(seed + 104729)
+    ks = rng.integers(kmin, kmax + 1, size=count)
+    mats = []
+    for k in ks:
+        r = rng.integers(0, modes, size=k)
+        c = rng.integers(0, modes, size=k)
+        mats.append(np.ascontiguousarray(u[np.ix_(r, c)]))
+    return mats
