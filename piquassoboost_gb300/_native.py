@@ -62,6 +62,7 @@ _SIGNATURES = [
     ("gbperm_perm", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P, _P]),
     ("gbperm_perm_workspace_size", ctypes.c_size_t, [_I64, _I64]),
     ("gbperm_perm_dev", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P, _P, ctypes.c_size_t, _P]),
+    ("gbperm_perm_repeated", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _P, _P]),
 ]
 
 _lib = None
@@ -143,6 +144,37 @@ def perm(matrix, return_dd: bool = False, stats: Stats | None = None):
     rc = lib.gbperm_perm(a.ctypes.data_as(_P), rows, cols, cols, out.ctypes.data_as(_P),
                          dd.ctypes.data_as(_P),
                          ctypes.byref(stats) if stats is not None else None)
+    check(rc)
+    if return_dd:
+        return complex(out[0], out[1]), dd
+    return complex(out[0], out[1])
+
+
+def as_state(state) -> np.ndarray:
+    s = np.asarray(state)
+    if s.ndim != 1:
+        s = s.reshape(-1)
+    return np.ascontiguousarray(s, dtype=np.int64)
+
+
+def perm_repeated(matrix, input_state, output_state, return_dd: bool = False,
+                  stats: Stats | None = None):
+    """Repeated-multiplicity permanent on the GPU (gbperm_perm_repeated).
+
+    input_state gives the column multiplicities, output_state the row
+    multiplicities (the reference's convention)."""
+    lib = load()
+    a = as_matrix(matrix)
+    cm = as_state(input_state)
+    rm = as_state(output_state)
+    rows, cols = a.shape
+    out = np.zeros(2)
+    dd = np.zeros(4)
+    if rows > 0 and cm.sum() > 0 and cm.sum() == rm.sum():
+        require_device()
+    rc = lib.gbperm_perm_repeated(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), len(cm),
+                                  rm.ctypes.data_as(_P), len(rm), out.ctypes.data_as(_P),
+                                  dd.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None)
     check(rc)
     if return_dd:
         return complex(out[0], out[1]), dd
