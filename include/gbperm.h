@@ -39,6 +39,13 @@ extern "C" {
 #define GBPERM_ERR_LIB 5         /* unknown calculator library id */
 #define GBPERM_ERR_NO_DEVICE 6   /* no CUDA device visible */
 
+/* Arithmetic of the n-term product (column sums are exact 64-bit fixed
+ * point in both; the cross-thread reduction is double-double in both). */
+#define GBPERM_ARITH_FP64 0  /* IEEE double product on the FP64 pipe */
+#define GBPERM_ARITH_DF32 1  /* double-float product on the FP32 pipe (~2^-46 per
+                                complex multiply); used for up to 48 columns when
+                                the matrix's dynamic range allows, else FP64 */
+
 /* Largest supported matrix side (columns of the product, rows of the Gray code). */
 #define GBPERM_MAX_DIM 64
 
@@ -49,7 +56,7 @@ typedef struct gbperm_stats {
     int32_t launches;      /* kernels launched by the call */
     int32_t grid;          /* blocks of the main launch */
     int32_t seg_log2;      /* log2 of the Gray segment length (plain / grad) */
-    int32_t reserved;
+    int32_t arith;         /* arithmetic actually used (GBPERM_ARITH_*) */
 } gbperm_stats;
 
 /* ------------------------------------------------------------- library */
@@ -72,14 +79,16 @@ int64_t gbperm_get_option(const char* key);
  * BBFGPermanentCalculator.cpp:89-126) and GlynnPermanentCalculator::calculate
  * (GlynnPermanentCalculator.hpp:47-57); semantics: rows == 0 or cols == 0 -> 1,
  * rows >= cols + 2 -> 0. */
-int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, double* out,
+int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int arith, double* out,
                 double* out_dd, gbperm_stats* stats);
 
-/* Device-pointer form.  dA: device complex128 matrix; d_out: 2 doubles on the
- * device; d_out_dd: NULL or 4 doubles on the device.  The workspace must hold
- * gbperm_perm_workspace_size(rows, cols) bytes, 256-byte aligned. */
+/* Device-pointer form.  dA: device complex128 matrix; d_out: 2 doubles on
+ * the device; d_out_dd: NULL or 4 doubles on the device.  The workspace must
+ * hold gbperm_perm_workspace_size(rows, cols) bytes, 256-byte aligned.  With
+ * GBPERM_ARITH_DF32 the range check runs on the device and the kernel falls
+ * back to the FP64 product when it fails. */
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols);
-int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, void* d_out,
+int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
                     void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream);
 
 /* --------------------------------------------------- repeated permanent */
@@ -95,7 +104,13 @@ int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, void
  * sum(col_mult) != sum(row_mult) -> GBPERM_ERR_STATE_SUM. */
 int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
                          const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
-                         int64_t nrow, double* out, double* out_dd, gbperm_stats* stats);
+                         int64_t nrow, int arith, double* out, double* out_dd,
+                         gbperm_stats* stats);
+
+/* ------------------------------------------------------------- probes */
+/* Measured pipe peak of the current device in TFLOP/s (FMA = 2 flops):
+ * kind 0 = FP64 FMA, kind 1 = FP32 FMA.  Runs ~0.1 s of probe kernels. */
+int gbperm_probe_peak(int kind, double* tflops);
 
 #ifdef __cplusplus
 }

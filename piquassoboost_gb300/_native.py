@@ -22,6 +22,19 @@ GBPERM_ERR_CUDA = 4
 GBPERM_ERR_LIB = 5
 GBPERM_ERR_NO_DEVICE = 6
 
+ARITH_FP64 = 0
+ARITH_DF32 = 1
+_MODES = {"fp64": ARITH_FP64, "fast": ARITH_DF32, "df32": ARITH_DF32}
+
+
+def arith_of(mode) -> int:
+    if isinstance(mode, int):
+        return mode
+    try:
+        return _MODES[mode]
+    except KeyError:
+        raise ValueError(f"unknown arithmetic mode {mode!r}") from None
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
@@ -37,11 +50,11 @@ class Stats(ctypes.Structure):
         ("launches", ctypes.c_int32),
         ("grid", ctypes.c_int32),
         ("seg_log2", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("arith", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class GBPermError(Exception):
@@ -59,10 +72,12 @@ _SIGNATURES = [
     ("gbperm_device_count", ctypes.c_int, []),
     ("gbperm_set_option", ctypes.c_int, [ctypes.c_char_p, _I64]),
     ("gbperm_get_option", _I64, [ctypes.c_char_p]),
-    ("gbperm_perm", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P, _P]),
+    ("gbperm_perm", ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P]),
     ("gbperm_perm_workspace_size", ctypes.c_size_t, [_I64, _I64]),
-    ("gbperm_perm_dev", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P, _P, ctypes.c_size_t, _P]),
-    ("gbperm_perm_repeated", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _P, _P, _P]),
+    ("gbperm_perm_dev", ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_size_t, _P]),
+    ("gbperm_probe_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbperm_perm_repeated", ctypes.c_int,
+     [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
 ]
 
 _lib = None
@@ -132,7 +147,7 @@ def as_matrix(matrix) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.complex128)
 
 
-def perm(matrix, return_dd: bool = False, stats: Stats | None = None):
+def perm(matrix, mode="fp64", return_dd: bool = False, stats: Stats | None = None):
     """Plain permanent on the GPU through gbperm_perm (host buffers)."""
     lib = load()
     a = as_matrix(matrix)
@@ -141,7 +156,7 @@ def perm(matrix, return_dd: bool = False, stats: Stats | None = None):
     dd = np.zeros(4)
     if rows > 0 and cols > 0 and rows < cols + 2:
         require_device()
-    rc = lib.gbperm_perm(a.ctypes.data_as(_P), rows, cols, cols, out.ctypes.data_as(_P),
+    rc = lib.gbperm_perm(a.ctypes.data_as(_P), rows, cols, cols, arith_of(mode), out.ctypes.data_as(_P),
                          dd.ctypes.data_as(_P),
                          ctypes.byref(stats) if stats is not None else None)
     check(rc)
@@ -157,7 +172,7 @@ def as_state(state) -> np.ndarray:
     return np.ascontiguousarray(s, dtype=np.int64)
 
 
-def perm_repeated(matrix, input_state, output_state, return_dd: bool = False,
+def perm_repeated(matrix, input_state, output_state, mode="fp64", return_dd: bool = False,
                   stats: Stats | None = None):
     """Repeated-multiplicity permanent on the GPU (gbperm_perm_repeated).
 
@@ -173,9 +188,27 @@ def perm_repeated(matrix, input_state, output_state, return_dd: bool = False,
     if rows > 0 and cm.sum() > 0 and cm.sum() == rm.sum():
         require_device()
     rc = lib.gbperm_perm_repeated(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), len(cm),
-                                  rm.ctypes.data_as(_P), len(rm), out.ctypes.data_as(_P),
+                                  rm.ctypes.data_as(_P), len(rm), arith_of(mode), out.ctypes.data_as(_P),
                                   dd.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None)
     check(rc)
     if return_dd:
         return complex(out[0], out[1]), dd
     return complex(out[0], out[1])
+
+
+def perm_repeated_many(matrix, pairs, mode="fp64"):
+    """Repeated permanents of one matrix for a list of (input, output) state
+    pairs, in order."""
+    return [perm_repeated(matrix, i, o, mode=mode) for i, o in pairs]
+
+
+def perm_batched(matrices, mode="fp64"):
+    """Plain permanents of a list of matrices, in order."""
+    return [perm(m, mode=mode) for m in matrices]
+
+
+def probe_peak(kind: str) -> float:
+    """Measured FP64 ("fp64") or FP32 ("fp32") FMA peak in TFLOP/s."""
+    v = ctypes.c_double()
+    check(load().gbperm_probe_peak({"fp64": 0, "fp32": 1}[kind], ctypes.byref(v)))
+    return v.value

@@ -91,12 +91,13 @@ int ceil_log2_u64(unsigned long long x) {
 
 // ------------------------------------------------------------------ plain
 
-PlainPlan plan_plain(int rows, int cols) {
+PlainPlan plan_plain(int rows, int cols, bool df) {
     PlainPlan p;
+    p.df = df;
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = device_sms(dev);
-    int bps = plain_blocks_per_sm(rows, cols);
+    int bps = plain_blocks_per_sm(rows, cols, df);
     int grid_full = sms * bps;
     int slog = rows - 1;
     // aim at >= 64 segments per thread (load balance within ~1.5%) while
@@ -128,6 +129,8 @@ size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w) {
     off += mat;
     if (w) w->exp = off;
     off += 256;
+    if (w) w->scale = off;
+    off += 256;
     if (w) w->kern = off;
     off += plain_workspace_bytes(grid);
     return off;
@@ -150,10 +153,12 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     pa.a1 = reinterpret_cast<longlong2*>(base + w.a1);
     pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
+    pa.df = plan.df ? 1 : 0;
+    pa.df_scale = reinterpret_cast<float*>(base + w.scale);
     cudaError_t e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
-    e = launch_plain(pa.a1, pa.a2, pa.exp_out, rows, cols, plan.grid, plan.seg_log2, base + w.kern,
-                     d_out2, d_out4, st);
+    e = launch_plain(pa.a1, pa.a2, pa.exp_out, plan.df ? pa.df_scale : nullptr, rows, cols, plan.grid,
+                     plan.seg_log2, base + w.kern, d_out2, d_out4, st);
     if (e != cudaSuccess) return cuda_fail(e, "plain launch");
     return GBPERM_OK;
 }
@@ -209,12 +214,17 @@ int64_t gbperm_get_option(const char* key) {
 
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols) {
     if (rows <= 0 || cols <= 0 || rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM) return 256;
-    PlainPlan plan = plan_plain((int)rows, (int)cols);
+    // the larger of the two arithmetics' needs (grids may differ)
+    PlainPlan p0 = plan_plain((int)rows, (int)cols, false);
+    PlainPlan p1 = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols);
+    PlainPlan plan = p0.grid >= p1.grid ? p0 : p1;
     return plain_ws_layout((int)rows, (int)cols, plan.grid, nullptr);
 }
 
-int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, void* d_out,
+int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
                     void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream) {
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+        return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: unknown arithmetic");
     if (rows < 0 || cols < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: negative shape");
     if (!d_out) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: null output");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -234,14 +244,14 @@ int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, void
         return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_dev: matrix larger than 64 x 64");
     if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: workspace must be 256-byte aligned");
-    PlainPlan plan = plan_plain((int)rows, (int)cols);
+    PlainPlan plan = plan_plain((int)rows, (int)cols, arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols);
     return run_plain_dev(static_cast<const double2*>(dA), ld, (int)rows, (int)cols, workspace,
                          workspace_bytes, static_cast<double*>(d_out), static_cast<double*>(d_out_dd), st,
                          plan);
 }
 
-int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, double* out, double* out_dd,
-                gbperm_stats* stats) {
+int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int arith, double* out,
+                double* out_dd, gbperm_stats* stats) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
     if (!out) return fail(GBPERM_ERR_ARG, "gbperm_perm: null output");
     if (rows < 0 || cols < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm: negative shape");
@@ -255,7 +265,13 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, double*
         if (out_dd) out_dd[0] = out_dd[1] = out_dd[2] = out_dd[3] = NAN;
         return GBPERM_OK;
     }
-    PlainPlan plan = plan_plain((int)rows, (int)cols);
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+        return fail(GBPERM_ERR_ARG, "gbperm_perm: unknown arithmetic");
+    bool df = false;
+    int boost = 0;
+    if (arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols)
+        df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost);
+    PlainPlan plan = plan_plain((int)rows, (int)cols, df);
     size_t mat_bytes = align_up((size_t)rows * cols * sizeof(double2), 256);
     size_t ws = plain_ws_layout((int)rows, (int)cols, plan.grid, nullptr);
     ThreadCtx& c = thread_ctx();
@@ -289,6 +305,7 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, double*
         stats->launches = 2;
         stats->grid = plan.grid;
         stats->seg_log2 = plan.seg_log2;
+        stats->arith = df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
     }
     return GBPERM_OK;
 }

@@ -47,11 +47,12 @@ ThreadCtx& thread_ctx();
 struct PlainPlan {
     int grid = 1;
     int seg_log2 = 0;
+    bool df = false;
 };
 struct PlainWs {
-    size_t a1 = 0, a2 = 0, exp = 0, kern = 0;
+    size_t a1 = 0, a2 = 0, exp = 0, scale = 0, kern = 0;
 };
-PlainPlan plan_plain(int rows, int cols);
+PlainPlan plan_plain(int rows, int cols, bool df);
 size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w);
 int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, size_t ws_bytes,
                   double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan);

@@ -94,4 +94,78 @@ __device__ __forceinline__ cd cmul(cd a, cd b) {
     return r;
 }
 
+// ---------------------------------------------------------- double-float
+// Unevaluated float pairs h + l on the FP32 pipe ("df").  Products keep the
+// exact error of the leading product (FMA) and the first-order cross terms;
+// the pair is not renormalised after a multiply (|l| stays below ~2^-22 |z|),
+// which keeps the error of a complex product near 2^-46 |z|.
+struct cf {  // complex double-float
+    float rh, rl, ih, il;
+};
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ cf cf_mul(const cf& x, const cf& y) {
+    cf z;
+    // real part: xr*yr - xi*yi
+    float p1 = x.rh * y.rh;
+    float e1 = fmaf(x.rh, y.rh, -p1);
+    float p2 = x.ih * y.ih;
+    float e2 = fmaf(x.ih, y.ih, -p2);
+    float s, t;
+    two_sum_f(p1, -p2, s, t);
+    float u = (e1 - e2) + t;
+    u = fmaf(x.rh, y.rl, u);
+    u = fmaf(x.rl, y.rh, u);
+    u = fmaf(-x.ih, y.il, u);
+    u = fmaf(-x.il, y.ih, u);
+    z.rh = s;
+    z.rl = u;
+    // imaginary part: xr*yi + xi*yr
+    float q1 = x.rh * y.ih;
+    float f1 = fmaf(x.rh, y.ih, -q1);
+    float q2 = x.ih * y.rh;
+    float f2 = fmaf(x.ih, y.rh, -q2);
+    float s2, t2;
+    two_sum_f(q1, q2, s2, t2);
+    float v = (f1 + f2) + t2;
+    v = fmaf(x.rh, y.il, v);
+    v = fmaf(x.rl, y.ih, v);
+    v = fmaf(x.ih, y.rl, v);
+    v = fmaf(x.il, y.rh, v);
+    z.ih = s2;
+    z.il = v;
+    return z;
+}
+
+// int64 fixed point -> float pair with three exact 21-bit chunks:
+// x = c2 2^42 + c1 2^21 + c0 (c2 signed, c1, c0 in [0, 2^21)).  s2, s1, s0
+// are the powers of two 2^(o-20), 2^(o-41), 2^(o-62) (o: the matrix's range
+// boost).  The leading pair is combined with Fast2Sum, valid because
+// |f2| >= 2^(o-20) > f1 whenever c2 != 0.
+__device__ __forceinline__ void fix_to_df(long long x, float s2, float s1, float s0, float& h, float& l) {
+    const int c2 = (int)(x >> 42);
+    const int c1 = (int)((x >> 21) & 0x1FFFFFll);
+    const int c0 = (int)(x & 0x1FFFFFll);
+    const float f2 = __int2float_rn(c2) * s2;
+    const float f1 = __int2float_rn(c1) * s1;
+    const float f0 = __int2float_rn(c0) * s0;
+    h = f2 + f1;
+    const float e = f1 - (h - f2);
+    l = e + f0;
+}
+
+// df accumulator: a += (h, l), renormalised
+__device__ __forceinline__ void df_acc(float& ah, float& al, float h, float l) {
+    float s, e;
+    two_sum_f(ah, h, s, e);
+    e += al + l;
+    ah = s + e;
+    al = e - (ah - s);
+}
+
 }  // namespace gbperm

@@ -27,16 +27,28 @@ struct PrepArgs {
     longlong2* a1;           // rows x cols
     longlong2* a2;           // rows x cols
     int* exp_out;            // 1 int
+    int df;                  // 1: also write double-float conversion constants
+    float* df_scale;         // 4 floats: 2^(o-20), 2^(o-41), 2^(o-62), ok (1/0);
+                             // ok = 0 when the range check fails (FP64 then)
 };
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st);
 
 // ------------------------------------------------------------------ plain
 int plain_bucket(int cols);
-int plain_blocks_per_sm(int rows, int cols);
+int plain_blocks_per_sm(int rows, int cols, bool df);
 size_t plain_workspace_bytes(int grid);
-cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* exp_in, int rows,
-                         int cols, int grid, int seg_log2, void* ws, double* out2, double* out4,
-                         cudaStream_t st);
+cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* exp_in,
+                         const float* df_scale, int rows, int cols, int grid, int seg_log2, void* ws,
+                         double* out2, double* out4, cudaStream_t st);
+
+// Range boost o for the double-float product (host): columns are first
+// scaled to their L1 bound (< 1); o then centres the typical term
+// (prod of column 2-norms) near 2^-40 while keeping the largest possible
+// term (every |colsum| at its bound, times sqrt 2) below 2^118.  Returns
+// false when no o satisfies both (then the FP64 kernel must be used).
+bool df_boost(const double* A, int64_t rows, int64_t cols, int64_t ld, const int* row_w,
+              const int* col_w, int* boost);
+constexpr int kDfMaxCols = 48;
 
 // --------------------------------------------------------------- repeated
 constexpr int kMaxDigits = 64;

@@ -242,8 +242,11 @@ using namespace gbperm;
 
 extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
                                     const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
-                                    int64_t nrow, double* out, double* out_dd, gbperm_stats* stats) {
+                                    int64_t nrow, int arith, double* out, double* out_dd,
+                                    gbperm_stats* stats) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+        return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: unknown arithmetic");
     if (!out) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: null output");
     if (rows < 0 || cols < 0 || nrow < 0 || ncol < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: negative size");
     RepHost h;
@@ -310,6 +313,8 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     pa.a1 = reinterpret_cast<longlong2*>(base + w.a1);
     pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
+    pa.df = 0;
+    pa.df_scale = nullptr;
     if (stats) cudaEventRecord(c.ev0, st);
     e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: prepare");

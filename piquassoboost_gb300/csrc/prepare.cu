@@ -1,4 +1,6 @@
 // Fixed-point preparation of one matrix on the device (see gbperm_internal.h).
+#include <cmath>
+
 #include "gbperm_internal.h"
 
 namespace gbperm {
@@ -7,13 +9,15 @@ namespace {
 
 __global__ void prepare_kernel(PrepArgs p) {
     __shared__ int s_e[64];
+    __shared__ double s_typ[64];
     for (int j = threadIdx.x; j < p.cols; j += blockDim.x) {
-        double br = 0.0, bi = 0.0;
+        double br = 0.0, bi = 0.0, l2 = 0.0;
         for (int i = 0; i < p.rows; ++i) {
             double2 a = p.A[(long long)i * p.ld + j];
             double w = p.row_w ? (double)p.row_w[i] : 1.0;
             br += w * fabs(a.x);
             bi += w * fabs(a.y);
+            l2 += w * (a.x * a.x + a.y * a.y);
         }
         // a little headroom so that rounding in the bound never lets a sum
         // reach 2^62 in fixed point
@@ -21,6 +25,7 @@ __global__ void prepare_kernel(PrepArgs p) {
         int e = 0;
         if (b > 0.0) frexp(b, &e);
         s_e[j] = e;
+        s_typ[j] = b > 0.0 ? log2(sqrt(l2) / ldexp(1.0, e)) : -1e300;
         for (int i = 0; i < p.rows; ++i) {
             double2 a = p.A[(long long)i * p.ld + j];
             long long xr = __double2ll_rn(ldexp(a.x, GBPERM_FIX_BITS - e));
@@ -32,12 +37,67 @@ __global__ void prepare_kernel(PrepArgs p) {
     __syncthreads();
     if (threadIdx.x == 0) {
         long long tot = 0;
-        for (int j = 0; j < p.cols; ++j) tot += (long long)s_e[j] * (p.col_w ? p.col_w[j] : 1);
+        long long pw = 0;
+        double typ = 0.0;
+        for (int j = 0; j < p.cols; ++j) {
+            long long w = p.col_w ? p.col_w[j] : 1;
+            tot += (long long)s_e[j] * w;
+            pw += w;
+            if (w) typ += (double)w * s_typ[j];
+        }
+        if (p.df) {
+            // range boost o of the double-float product: centre the typical
+            // term near 2^-40, keep the largest possible one below 2^118
+            int o = 0, ok = 0;
+            if (pw > 0 && typ > -1e290) {
+                o = (int)floor((-40.0 - typ) / (double)pw);
+                int omax = (int)floor(118.0 / (double)pw - 0.5);
+                if (o > omax) o = omax;
+                ok = (typ + (double)o * (double)pw >= -100.0) ? 1 : 0;
+            }
+            if (!ok) o = 0;
+            tot -= (long long)o * pw;
+            p.df_scale[0] = ldexpf(1.0f, o - 20);
+            p.df_scale[1] = ldexpf(1.0f, o - 41);
+            p.df_scale[2] = ldexpf(1.0f, o - 62);
+            p.df_scale[3] = ok ? 1.0f : 0.0f;
+        }
         p.exp_out[0] = (int)(tot - p.norm_shift);
     }
 }
 
 }  // namespace
+
+bool df_boost(const double* A, int64_t rows, int64_t cols, int64_t ld, const int* row_w,
+              const int* col_w, int* boost) {
+    double typ = 0.0;   // log2 of the typical |term| before the boost
+    double pw = 0.0;    // number of factors
+    for (int64_t j = 0; j < cols; ++j) {
+        double br = 0.0, bi = 0.0, l2 = 0.0;
+        for (int64_t i = 0; i < rows; ++i) {
+            double w = row_w ? (double)row_w[i] : 1.0;
+            double re = A[2 * (i * ld + j)], im = A[2 * (i * ld + j) + 1];
+            br += w * std::fabs(re);
+            bi += w * std::fabs(im);
+            l2 += w * (re * re + im * im);
+        }
+        double b = std::fmax(br, bi) * (1.0 + 1e-12);
+        double w = col_w ? (double)col_w[j] : 1.0;
+        if (w == 0.0) continue;
+        if (b == 0.0) return false;  // a zero column: permanent 0, no range issue but no scale either
+        int e = 0;
+        std::frexp(b, &e);
+        typ += w * std::log2(std::sqrt(l2) / std::ldexp(1.0, e));
+        pw += w;
+    }
+    if (pw == 0.0) return false;
+    int o = (int)std::floor((-40.0 - typ) / pw);
+    int omax = (int)std::floor(118.0 / pw - 0.5);
+    if (o > omax) o = omax;
+    if (typ + o * pw < -100.0) return false;
+    *boost = o;
+    return true;
+}
 
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st) {
     prepare_kernel<<<1, 64, 0, st>>>(a);
