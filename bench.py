@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 permanent path; prints ONE JSON line (rank 0).
+
+Workload (default): the plain Glynn/BBFG permanent of the top-left n x n block
+of a seeded Haar-random 2n x 2n unitary, n = 36, complex128 (the single large
+permanent configuration, n in {30, 34, 36, 40}).  One step = one permanent.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--n 36] [--mode fast|fp64]
+  python bench.py --impl reference ...   # the reference algorithm on host cores
+
+value   permanents/s with the matrix already resident in HBM (device-pointer
+        entry point, CUDA events on the launching stream; L2 flushed between
+        steps by writing a 256 MiB buffer);
+e2e     the same metric through the public host-buffer entry point
+        (gbperm_perm): pinned host matrix -> device copy, compute, result copied
+        back, every step;
+roofline  the permanent kernel: algorithmic FP64-equivalent flops
+        (8 n 2^(n-1) per permanent) / kernel time against the FP64 FMA peak
+        measured live by the library's probe, and for the double-float path
+        the FP32 pipe peak too;
+cpu_baseline  the C oracle (a restatement of the reference's BBFG double
+        calculator with its 4 x threads segmentation) on all host cores, on a
+        bounded sample of the same permanent's Gray range, scaled to perm/s.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "complex perm/s at n=30/36/40 & batched k=8-28 vs plain GPU, rel err <=1e-10"
+UNIT = "perm/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=36)
+    ap.add_argument("--mode", default="fast", choices=["fast", "fp64"])
+    ap.add_argument("--seed", type=int, default=36)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def flops_plain(n: int) -> float:
+    return 8.0 * n * 2.0 ** (n - 1)
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample_rate(A: np.ndarray, seconds: float, threads: int = 0):
+    """Gray steps/s of the oracle on all host cores, on a bounded contiguous
+    sample of the permanent's Gray range (calibrated to ~`seconds`)."""
+    from tests import oracle_bind as orc
+
+    lib = orc.lib()
+    P = ctypes.c_void_p
+    lib.orc_bbfg_range.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                   ctypes.c_uint64, ctypes.c_uint64, P]
+    a = np.ascontiguousarray(A, dtype=np.complex128)
+    n = a.shape[0]
+    total = 1 << (n - 1)
+    out = np.zeros(4)
+    # calibrate on a small sample, then run the measured sample
+    span = min(total, 1 << 22)
+    t0 = time.perf_counter()
+    lib.orc_bbfg_range(a.ctypes.data_as(P), n, n, n, threads, 0, span, out.ctypes.data_as(P))
+    dt = time.perf_counter() - t0
+    rate = span / max(dt, 1e-9)
+    span = int(min(total, max(1 << 20, rate * seconds)))
+    start = (total - span) // 2
+    t0 = time.perf_counter()
+    lib.orc_bbfg_range(a.ctypes.data_as(P), n, n, n, threads, start, start + span, out.ctypes.data_as(P))
+    dt = time.perf_counter() - t0
+    return span / dt, span, dt
+
+
+def host_threads() -> int:
+    return os.cpu_count() or 1
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from piquassoboost_gb300.workloads import haar_block
+
+    n = args.n
+    A = haar_block(n, seed=args.seed)
+    thr = host_threads()
+    per_step = max(2.0, args.cpu_seconds / 3.0)
+    for _ in range(args.warmup):
+        cpu_sample_rate(A, min(1.0, per_step / 4), thr)
+    rates, spans, times = [], [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, span, dt = cpu_sample_rate(A, per_step, thr)
+        rates.append(r)
+        spans.append(span)
+        times.append(dt)
+    wall = time.perf_counter() - t0
+    steps_per_s = sum(spans) / sum(times)
+    perm_s = steps_per_s / 2.0 ** (n - 1)
+    line = {
+        "impl": "reference",
+        "metric": METRIC, "value": perm_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"plain permanent, top-left {n}x{n} block of a seeded Haar {2 * n}x{2 * n} unitary",
+                   "n": n, "seed": args.seed},
+        "cpu_baseline": {"value": perm_s, "unit": UNIT, "cores": thr, "kind": "port",
+                         "sample": f"per step a contiguous sample of ~{int(statistics.mean(spans))} of the "
+                                   f"2^{n - 1} Gray steps (reference BBFG double algorithm, C restatement, "
+                                   f"{thr} threads, 4 x threads segments); perm/s = steps/s / 2^{n - 1}"},
+        "e2e": {"value": perm_s, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local):
+    import torch
+
+    from piquassoboost_gb300 import _native as nat
+    from piquassoboost_gb300.workloads import haar_block
+
+    if not torch.cuda.is_available():
+        print(json.dumps({"error": "no CUDA device"}))
+        return 1
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = nat.load()
+    n = args.n
+    arith = nat.arith_of(args.mode)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    # per-rank, per-step seeded inputs (weak scaling: every rank does its own permanents)
+    nsteps = args.warmup + args.steps
+    mats = [haar_block(n, seed=args.seed + 1000 * rank + s) for s in range(nsteps)]
+    d_mats = [torch.from_numpy(m).to(dev) for m in mats]
+    ws_bytes = int(lib.gbperm_perm_workspace_size(n, n))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    d_out = torch.zeros(2, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    launches_per_step = 2  # prepare + permanent kernel
+
+    def step(i):
+        rc = lib.gbperm_perm_dev(ctypes.c_void_p(d_mats[i].data_ptr()), n, n, n, arith,
+                                 ctypes.c_void_p(d_out.data_ptr()), None, ctypes.c_void_p(ws.data_ptr()),
+                                 ws_bytes, sptr)
+        nat.check(rc)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    peaks = {"fp64_tflops": nat.probe_peak("fp64"), "fp32_tflops": nat.probe_peak("fp32")}
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    results = []
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step(args.warmup + k)
+        ev[k][1].record(stream)
+        results.append(d_out.clone())
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    kern_ms = [a.elapsed_time(b) for a, b in ev]
+    t_max = wall
+    if world > 1:
+        tt = torch.tensor([wall], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * args.steps / t_max
+
+    # correctness spot check of the timed results against the FP64 kernel
+    # (cheap at small n; skipped at n > 34 where one FP64 permanent costs minutes)
+    check = None
+    if n <= 34 and args.mode == "fast":
+        ref = nat.perm(mats[args.warmup], mode="fp64")
+        got = complex(results[0][0].item(), results[0][1].item())
+        check = abs(got - ref) / abs(ref)
+
+    # e2e through the public host-buffer entry point, pinned input, every step
+    pinned = [torch.from_numpy(m).pin_memory() for m in mats[args.warmup:]]
+    out = np.zeros(2)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for k in range(args.steps):
+        rc = lib.gbperm_perm(ctypes.c_void_p(pinned[k].data_ptr()), n, n, n, arith,
+                             out.ctypes.data_as(ctypes.c_void_p), None, None)
+        nat.check(rc)
+    torch.cuda.synchronize()
+    e2e_wall = time.perf_counter() - t1
+    if world > 1:
+        tt = torch.tensor([e2e_wall], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_wall = float(tt.item())
+    e2e = world * args.steps / e2e_wall
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+
+    avg_ms = statistics.mean(kern_ms)
+    achieved = flops_plain(n) / (avg_ms * 1e-3) / 1e12
+    roof = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / peaks["fp64_tflops"], "traffic": None,
+            "kernel": ("plain_df_kernel" if args.mode == "fast" else "plain_kernel"),
+            "work_per_launch": f"8 n 2^(n-1) = {flops_plain(n):.4g} algorithmic FP64-equivalent flops",
+            "peak_source": "measured live by gbperm_probe_peak (DFMA probe), this run"}
+    if args.mode == "fast":
+        roof["note"] = ("double-float product on the FP32 pipe: frac is against the FP64 FMA peak "
+                        "(the north-star denominator); the FP32 FMA peak measured in the same run is "
+                        f"{peaks['fp32_tflops']:.1f} TFLOP/s")
+        roof["fp32_peak_tflops"] = peaks["fp32_tflops"]
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        thr = host_threads()
+        rate, span, dt = cpu_sample_rate(mats[args.warmup], args.cpu_seconds, thr)
+        cpu = {"value": rate / 2.0 ** (n - 1), "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{span} contiguous Gray steps of the same {n}x{n} permanent ({dt:.1f} s, "
+                         f"{thr} threads, reference BBFG double algorithm as the C oracle); "
+                         f"perm/s = steps/s / 2^{n - 1}"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"plain permanent, top-left {n}x{n} block of a seeded Haar {2 * n}x{2 * n} unitary",
+                   "n": n, "arith": args.mode, "seed": args.seed, "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * n * 16, "d2h_bytes_per_step": 16},
+        "clocks": clk,
+        "gpu_launches": launches_per_step * args.steps,
+        "kernel_ms": kern_ms,
+        "rel_err_vs_fp64_kernel": check,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -69,6 +69,8 @@ int gbperm_device_count(void);
  *   "plain.grid"          force the plain grid size (0 = auto)
  *   "repeated.low_digits" force the digits handled inside a repeated segment (-1 = auto)
  *   "batched.threads"     force threads per instance of the batched kernel (0 = autotuned)
+ *   "plain.df_group"      lanes sharing one Gray segment in the double-float kernel
+ *                         (1, 2, 4 or 8; 0 = by column count)
  */
 int gbperm_set_option(const char* key, int64_t value);
 int64_t gbperm_get_option(const char* key);
@@ -106,6 +108,21 @@ int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld
                          const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
                          int64_t nrow, int arith, double* out, double* out_dd,
                          gbperm_stats* stats);
+
+/* ----------------------------------------------- permanent + gradient */
+/* Permanent of an n x n matrix and its full gradient G[k][l] = dperm/da_kl
+ * (= perm of A without row k and column l) in one Gray-code sweep, for
+ * n <= 32, with the double-float product.  No reference counterpart: this is
+ * the adjoint of BBFGPermanentCalculator::calculate
+ * (BBFGPermanentCalculator.hpp:87-235).  grad receives n x n complex128,
+ * row-major.  GBPERM_ERR_TOO_LARGE when n > 32 or when the matrix's dynamic
+ * range does not fit the double-float product. */
+int gbperm_perm_grad(const double* A, int64_t n, int64_t ld, double* perm, double* perm_dd, double* grad,
+                     gbperm_stats* stats);
+size_t gbperm_perm_grad_workspace_size(int64_t n);
+/* Device-pointer form; on a range-check failure perm and grad are NaN. */
+int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, void* d_perm_dd, void* d_grad,
+                         void* workspace, size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------- probes */
 /* Measured pipe peak of the current device in TFLOP/s (FMA = 2 flops):

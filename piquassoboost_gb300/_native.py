@@ -76,6 +76,16 @@ _SIGNATURES = [
     ("gbperm_perm_workspace_size", ctypes.c_size_t, [_I64, _I64]),
     ("gbperm_perm_dev", ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_size_t, _P]),
     ("gbperm_probe_peak", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbperm_batch_plan_create", ctypes.c_int, [_P, _P, _I64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbperm_batch_plan_destroy", None, [_P]),
+    ("gbperm_batch_plan_run", ctypes.c_int, [_P, _P, _P, _P]),
+    ("gbperm_batch_plan_run_dev", ctypes.c_int, [_P, _P, _P, _P]),
+    ("gbperm_batch_plan_set_item_log2", ctypes.c_int, [_P, _I64]),
+    ("gbperm_batch_plan_get_item_log2", _I64, [_P]),
+    ("gbperm_perm_batched", ctypes.c_int, [_P, _P, _P, _I64, ctypes.c_int, _P, _P]),
+    ("gbperm_perm_grad", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P]),
+    ("gbperm_perm_grad_workspace_size", ctypes.c_size_t, [_I64]),
+    ("gbperm_perm_grad_dev", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P, ctypes.c_size_t, _P]),
     ("gbperm_perm_repeated", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
 ]
@@ -202,9 +212,67 @@ def perm_repeated_many(matrix, pairs, mode="fp64"):
     return [perm_repeated(matrix, i, o, mode=mode) for i, o in pairs]
 
 
-def perm_batched(matrices, mode="fp64"):
-    """Plain permanents of a list of matrices, in order."""
-    return [perm(m, mode=mode) for m in matrices]
+class BatchPlan:
+    """A reusable batched plan (gbperm_batch_plan_*): fixed shapes, a CUDA
+    graph captured at creation, one persistent launch per run."""
+
+    def __init__(self, shapes, mode="fp64"):
+        lib = load()
+        self.shapes = [(int(r), int(c)) for r, c in shapes]
+        self.rows = np.ascontiguousarray([r for r, _ in self.shapes], dtype=np.int64)
+        self.cols = np.ascontiguousarray([c for _, c in self.shapes], dtype=np.int64)
+        self.count = len(self.shapes)
+        self.total = int(np.sum(self.rows * self.cols))
+        self._h = ctypes.c_void_p()
+        if any(r > 0 and c > 0 and r < c + 2 for r, c in self.shapes):
+            require_device()
+        check(lib.gbperm_batch_plan_create(self.rows.ctypes.data_as(_P), self.cols.ctypes.data_as(_P),
+                                           self.count, arith_of(mode), ctypes.byref(self._h)))
+
+    def pack(self, matrices) -> np.ndarray:
+        buf = np.empty(max(self.total, 1), dtype=np.complex128)
+        k = 0
+        for m, (r, c) in zip(matrices, self.shapes):
+            buf[k:k + r * c] = np.asarray(m, dtype=np.complex128).reshape(-1)
+            k += r * c
+        return buf
+
+    def run(self, matrices=None, packed=None, stats: Stats | None = None):
+        if packed is None:
+            packed = self.pack(matrices)
+        out = np.zeros(2 * max(self.count, 1))
+        check(load().gbperm_batch_plan_run(self._h, packed.ctypes.data_as(_P), out.ctypes.data_as(_P),
+                                           ctypes.byref(stats) if stats is not None else None))
+        return [complex(out[2 * i], out[2 * i + 1]) for i in range(self.count)]
+
+    def set_item_log2(self, v: int) -> None:
+        check(load().gbperm_batch_plan_set_item_log2(self._h, int(v)))
+
+    def item_log2(self) -> int:
+        return int(load().gbperm_batch_plan_get_item_log2(self._h))
+
+    def close(self):
+        if self._h:
+            load().gbperm_batch_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def perm_batched(matrices, mode="fp64", stats: Stats | None = None):
+    """Plain permanents of a list of matrices in one persistent launch."""
+    mats = [as_matrix(m) for m in matrices]
+    if not mats:
+        return []
+    plan = BatchPlan([m.shape for m in mats], mode=mode)
+    try:
+        return plan.run(mats, stats=stats)
+    finally:
+        plan.close()
 
 
 def probe_peak(kind: str) -> float:
@@ -212,3 +280,18 @@ def probe_peak(kind: str) -> float:
     v = ctypes.c_double()
     check(load().gbperm_probe_peak({"fp64": 0, "fp32": 1}[kind], ctypes.byref(v)))
     return v.value
+
+
+def perm_grad(matrix, stats: Stats | None = None):
+    """Permanent and full gradient G[k, l] = dperm/da_kl (host buffers)."""
+    lib = load()
+    a = as_matrix(matrix)
+    n = a.shape[0]
+    if a.shape[0] != a.shape[1]:
+        raise ValueError("perm_grad: square matrix required")
+    require_device()
+    perm = np.zeros(2)
+    g = np.zeros((n, n), dtype=np.complex128)
+    check(lib.gbperm_perm_grad(a.ctypes.data_as(_P), n, n, perm.ctypes.data_as(_P), None,
+                               g.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
+    return complex(perm[0], perm[1]), g

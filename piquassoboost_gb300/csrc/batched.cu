@@ -1,0 +1,811 @@
+// Batched plain permanents of many small matrices in one persistent launch.
+//
+// Replaces the sequential list branch of the reference's plain wrapper
+// (GlynnPermanentCalculator_Wrapper.hpp:204-294) and the one-permanent-at-a-
+// time loop of BatchednPermanentCalculator::calculate
+// (BatchedPermanentCalculator.cpp:109-296), where each instance spins up its
+// own TBB parallel region.
+//
+// Work list: every instance's Gray range is cut into aligned segments of
+// 2^l_i steps; a work item is the SPI = 32 / GROUP consecutive segments one
+// warp handles (one segment per lane group).  Items are ordered by instance
+// cost, largest first (longest-processing-time order), and warps take them
+// from an atomic counter until the list is empty, so small instances fill
+// the tail behind the large ones.  Each item's double-double partial sum
+// lands in its own slot; a finalize kernel adds an instance's slots in a
+// fixed order (bitwise-reproducible results) and applies the scale.
+//
+// Arithmetic per instance as in the single-permanent kernels: exact int64
+// column sums; FP64 product (GROUP = 1) or the double-float product with
+// lane groups (GROUP = 2/4), with the FP64 product as the per-instance
+// fallback when the range check fails.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <vector>
+
+#include "gbperm.h"
+#include "gbperm_capi_internal.h"
+
+namespace gbperm {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+struct BInst {              // device instance descriptor
+    int rows, cols;
+    long long a_off;        // offset (complex elements) of the instance in the packed input / fixed arrays
+    int seg_log2;
+    int item0, nitems;
+    unsigned long long nseg;
+};
+
+struct BInstOut {           // written by the batched prepare kernel
+    int exp;
+    int boost;
+    int ok;                 // double-float range check
+    int finite;             // input finite
+};
+
+struct BItem {
+    int inst;
+    int pad;
+    unsigned long long seg0;
+};
+
+struct BArgs {
+    const double2* A;       // packed inputs (dense rows x cols each)
+    longlong2* a1;
+    longlong2* a2;
+    const BInst* inst;
+    BInstOut* iout;
+    const BItem* items;
+    int nitems;
+    int ninst;
+    unsigned int* counter;
+    cdd* item_part;
+    double* out;            // 2 doubles per instance (device)
+    int df;
+};
+
+// One block per instance (grid-stride): fixed point, exponent and
+// double-float boost, as launch_prepare does for one matrix.
+__global__ void batched_prepare_kernel(BArgs p) {
+    __shared__ int s_e[64];
+    __shared__ double s_typ[64];
+    __shared__ int s_bad;
+    for (int i = blockIdx.x; i < p.ninst; i += gridDim.x) {
+        const BInst in = p.inst[i];
+        if (threadIdx.x == 0) s_bad = 0;
+        __syncthreads();
+        const double2* A = p.A + in.a_off;
+        for (int j = threadIdx.x; j < in.cols; j += blockDim.x) {
+            double br = 0.0, bi = 0.0, l2 = 0.0;
+            bool fin = true;
+            for (int r = 0; r < in.rows; ++r) {
+                double2 a = A[r * in.cols + j];
+                fin = fin && isfinite(a.x) && isfinite(a.y);
+                br += fabs(a.x);
+                bi += fabs(a.y);
+                l2 += a.x * a.x + a.y * a.y;
+            }
+            if (!fin) atomicOr(&s_bad, 1);
+            double b = fmax(br, bi) * (1.0 + 1e-12);
+            int e = 0;
+            if (b > 0.0 && fin) frexp(b, &e);
+            s_e[j] = e;
+            s_typ[j] = (b > 0.0 && fin) ? log2(sqrt(l2) / ldexp(1.0, e)) : -1e300;
+            for (int r = 0; r < in.rows; ++r) {
+                double2 a = A[r * in.cols + j];
+                long long xr = fin ? __double2ll_rn(ldexp(a.x, GBPERM_FIX_BITS - e)) : 0;
+                long long xi = fin ? __double2ll_rn(ldexp(a.y, GBPERM_FIX_BITS - e)) : 0;
+                p.a1[in.a_off + r * in.cols + j] = make_longlong2(xr, xi);
+                p.a2[in.a_off + r * in.cols + j] = make_longlong2(2 * xr, 2 * xi);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long tot = 0;
+            double typ = 0.0;
+            for (int j = 0; j < in.cols; ++j) {
+                tot += s_e[j];
+                typ += s_typ[j];
+            }
+            int o = 0, ok = 0;
+            if (p.df && typ > -1e290) {
+                o = (int)floor((-40.0 - typ) / (double)in.cols);
+                int omax = (int)floor(118.0 / (double)in.cols - 0.5);
+                if (o > omax) o = omax;
+                ok = (typ + (double)o * (double)in.cols >= -100.0) ? 1 : 0;
+                if (!ok) o = 0;
+            }
+            BInstOut r;
+            r.exp = (int)(tot - (long long)o * in.cols - (in.rows - 1));
+            r.boost = o;
+            r.ok = ok;
+            r.finite = s_bad ? 0 : 1;
+            p.iout[i] = r;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
+    return cf{__shfl_xor_sync(0xffffffffu, v.rh, m), __shfl_xor_sync(0xffffffffu, v.rl, m),
+              __shfl_xor_sync(0xffffffffu, v.ih, m), __shfl_xor_sync(0xffffffffu, v.il, m)};
+}
+
+// Persistent worker: each warp takes items from the counter.  GROUP lanes
+// share a segment; lane g owns columns [g*CPL, (g+1)*CPL).  DF selects the
+// double-float product (GROUP > 1 allowed) or the FP64 product (GROUP == 1).
+template <int CPL, int GROUP, bool DF>
+__global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
+    const int lane = threadIdx.x & 31;
+    const int g = lane % GROUP;
+    const int grp = lane / GROUP;
+    const int j0 = g * CPL;
+    long long cre[CPL], cim[CPL];
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = (int)atomicAdd(p.counter, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= p.nitems) break;
+        const BItem item = p.items[it];
+        const BInst in = p.inst[item.inst];
+        const BInstOut io = p.iout[item.inst];
+        const int rows = in.rows, cols = in.cols;
+        const unsigned long long s = item.seg0 + (unsigned long long)grp;
+        const bool active = s < in.nseg && io.finite;
+        const unsigned long long i0 = (active ? s : 0ull) << in.seg_log2;
+        const unsigned long long L = 1ull << in.seg_log2;
+        const longlong2* __restrict__ a1 = p.a1 + in.a_off;
+        const longlong2* __restrict__ a2 = p.a2 + in.a_off;
+        const unsigned long long g0 = i0 ^ (i0 >> 1);
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            longlong2 v = (j0 + c < cols) ? __ldg(&a1[j0 + c]) : make_longlong2(0, 0);
+            cre[c] = v.x;
+            cim[c] = v.y;
+        }
+        for (int r = 1; r < rows; ++r) {
+            const long long m = -(long long)((g0 >> (rows - 1 - r)) & 1ull);
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (j0 + c < cols) {
+                    longlong2 v = __ldg(&a1[r * cols + j0 + c]);
+                    cre[c] += (v.x ^ m) - m;
+                    cim[c] += (v.y ^ m) - m;
+                }
+            }
+        }
+        cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+        const bool use_df = DF && io.ok;
+        if (use_df) {
+            const DfConv cv = make_dfconv(io.boost);
+            unsigned int sbit = (unsigned int)(__popcll(g0) & 1) << 31;
+            float brh = 0.f, brl = 0.f, bih = 0.f, bil = 0.f;
+            for (unsigned long long k = 0; k < L; ++k) {
+                if (k != 0) {
+                    const int b = __ffsll((long long)k) - 1;
+                    const unsigned long long idx = i0 + k;
+                    const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;
+                    const longlong2* a = a2 + (rows - 1 - b) * cols + j0;
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        if (j0 + c < cols) {
+                            longlong2 v = __ldg(&a[c]);
+                            if (sub) {
+                                cre[c] -= v.x;
+                                cim[c] -= v.y;
+                            } else {
+                                cre[c] += v.x;
+                                cim[c] += v.y;
+                            }
+                        }
+                    }
+                    sbit ^= 0x80000000u;
+                    if ((k & 255ull) == 0) {
+                        acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
+                        acc.im = dd_add(acc.im, dd{(double)bih, (double)bil});
+                        brh = brl = bih = bil = 0.f;
+                    }
+                }
+                cf pa{1.f, 0.f, 0.f, 0.f}, pb{1.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    if (j0 + c < cols) {
+                        cf x;
+                        fix_to_df_magic(cre[c], cv, x.rh, x.rl);
+                        fix_to_df_magic(cim[c], cv, x.ih, x.il);
+                        if (c == 0) pa = x;
+                        else if (c == 1) pb = x;
+                        else if (c & 1) pb = cf_mul(pb, x);
+                        else pa = cf_mul(pa, x);
+                    }
+                }
+                if (CPL > 1) pa = cf_mul(pa, pb);
+#pragma unroll
+                for (int m = 1; m < GROUP; m <<= 1) pa = cf_mul(pa, shfl_xor_cf(pa, m));
+                if (g == 0 && active) {
+                    df_acc(brh, brl, __uint_as_float(__float_as_uint(pa.rh) ^ sbit),
+                           __uint_as_float(__float_as_uint(pa.rl) ^ sbit));
+                    df_acc(bih, bil, __uint_as_float(__float_as_uint(pa.ih) ^ sbit),
+                           __uint_as_float(__float_as_uint(pa.il) ^ sbit));
+                }
+            }
+            acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
+            acc.im = dd_add(acc.im, dd{(double)bih, (double)bil});
+        } else if (GROUP == 1) {
+            // FP64 product (also the double-float fallback)
+            unsigned long long neg = (unsigned long long)(__popcll(g0) & 1) << 63;
+            double bre = 0.0, bim = 0.0;
+            for (unsigned long long k = 0; k < L; ++k) {
+                if (k != 0) {
+                    const int b = __ffsll((long long)k) - 1;
+                    const unsigned long long idx = i0 + k;
+                    const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;
+                    const longlong2* a = a2 + (rows - 1 - b) * cols + j0;
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        if (j0 + c < cols) {
+                            longlong2 v = __ldg(&a[c]);
+                            if (sub) {
+                                cre[c] -= v.x;
+                                cim[c] -= v.y;
+                            } else {
+                                cre[c] += v.x;
+                                cim[c] += v.y;
+                            }
+                        }
+                    }
+                    neg ^= 0x8000000000000000ull;
+                    if ((k & 255ull) == 0) {
+                        acc.re = dd_add_d(acc.re, bre);
+                        acc.im = dd_add_d(acc.im, bim);
+                        bre = 0.0;
+                        bim = 0.0;
+                    }
+                }
+                cd pa{1.0, 0.0}, pb{1.0, 0.0};
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    if (c < cols) {
+                        cd x{fix_to_double(cre[c]), fix_to_double(cim[c])};
+                        if (c == 0) pa = x;
+                        else if (c == 1) pb = x;
+                        else if (c & 1) pb = cmul(pb, x);
+                        else pa = cmul(pa, x);
+                    }
+                }
+                if (CPL > 1 && cols > 1) pa = cmul(pa, pb);
+                if (active) {
+                    bre += __longlong_as_double(__double_as_longlong(pa.re) ^ (long long)neg);
+                    bim += __longlong_as_double(__double_as_longlong(pa.im) ^ (long long)neg);
+                }
+            }
+            acc.re = dd_add_d(acc.re, bre);
+            acc.im = dd_add_d(acc.im, bim);
+        } else {
+            // GROUP > 1 and the range check failed: FP64 product of the lane's
+            // columns, then the butterfly in FP64
+            unsigned long long neg = (unsigned long long)(__popcll(g0) & 1) << 63;
+            double bre = 0.0, bim = 0.0;
+            for (unsigned long long k = 0; k < L; ++k) {
+                if (k != 0) {
+                    const int b = __ffsll((long long)k) - 1;
+                    const unsigned long long idx = i0 + k;
+                    const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;
+                    const longlong2* a = a2 + (rows - 1 - b) * cols + j0;
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        if (j0 + c < cols) {
+                            longlong2 v = __ldg(&a[c]);
+                            if (sub) {
+                                cre[c] -= v.x;
+                                cim[c] -= v.y;
+                            } else {
+                                cre[c] += v.x;
+                                cim[c] += v.y;
+                            }
+                        }
+                    }
+                    neg ^= 0x8000000000000000ull;
+                    if ((k & 255ull) == 0) {
+                        acc.re = dd_add_d(acc.re, bre);
+                        acc.im = dd_add_d(acc.im, bim);
+                        bre = 0.0;
+                        bim = 0.0;
+                    }
+                }
+                cd pa{1.0, 0.0};
+#pragma unroll
+                for (int c = 0; c < CPL; ++c)
+                    if (j0 + c < cols) pa = cmul(pa, cd{fix_to_double(cre[c]), fix_to_double(cim[c])});
+#pragma unroll
+                for (int m = 1; m < GROUP; m <<= 1) {
+                    cd o{__shfl_xor_sync(0xffffffffu, pa.re, m), __shfl_xor_sync(0xffffffffu, pa.im, m)};
+                    pa = cmul(pa, o);
+                }
+                if (g == 0 && active) {
+                    bre += __longlong_as_double(__double_as_longlong(pa.re) ^ (long long)neg);
+                    bim += __longlong_as_double(__double_as_longlong(pa.im) ^ (long long)neg);
+                }
+            }
+            acc.re = dd_add_d(acc.re, bre);
+            acc.im = dd_add_d(acc.im, bim);
+        }
+        acc = warp_sum_cdd(acc);
+        if (lane == 0) p.item_part[it] = acc;
+    }
+}
+
+__global__ void batched_finalize_kernel(BArgs p) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.ninst; i += gridDim.x * blockDim.x) {
+        const BInst in = p.inst[i];
+        const BInstOut io = p.iout[i];
+        if (!io.finite) {
+            p.out[2 * i] = nan("");
+            p.out[2 * i + 1] = nan("");
+            continue;
+        }
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        for (int k = 0; k < in.nitems; ++k) tot = cdd_add(tot, p.item_part[in.item0 + k]);
+        write_result(tot, io.exp, p.out + 2 * i, nullptr);
+    }
+}
+
+template <int CPL, int GROUP, bool DF>
+int bps_t() {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_kernel<CPL, GROUP, DF>, kThreads, 0);
+    return nb > 0 ? nb : 1;
+}
+
+template <int CPL, int GROUP, bool DF>
+void launch_t(const BArgs& a, int grid, cudaStream_t st) {
+    batched_kernel<CPL, GROUP, DF><<<grid, kThreads, 0, st>>>(a);
+}
+
+// shapes: (CPL, GROUP, DF)
+#define GBPERM_BATCH_SHAPES(X) \
+    X(16, 1, false) X(32, 1, false) X(48, 1, false) X(64, 1, false) \
+    X(8, 2, true) X(12, 2, true) X(16, 2, true) X(4, 4, true) X(6, 4, true) X(8, 4, true) X(10, 4, true) \
+    X(12, 4, true)
+
+int batch_bps(int cpl, int grp, bool df) {
+#define X(C, G, D) \
+    if (cpl == C && grp == G && df == D) return bps_t<C, G, D>();
+    GBPERM_BATCH_SHAPES(X)
+#undef X
+    return 0;
+}
+
+cudaError_t batch_launch(const BArgs& a, int cpl, int grp, bool df, int grid, cudaStream_t st) {
+#define X(C, G, D) \
+    if (cpl == C && grp == G && df == D) {  \
+        launch_t<C, G, D>(a, grid, st);     \
+        return cudaGetLastError();          \
+    }
+    GBPERM_BATCH_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+// smallest compiled shape covering `cols` columns for the arithmetic
+void batch_shape(int cols, bool df, int group, int* cpl, int* grp) {
+    static const int s64[][2] = {{16, 1}, {32, 1}, {48, 1}, {64, 1}};
+    static const int sdf[][2] = {{8, 2}, {12, 2}, {16, 2}, {4, 4}, {6, 4}, {8, 4}, {10, 4}, {12, 4}};
+    if (!df) {
+        for (auto& s : s64)
+            if (s[0] >= cols) {
+                *cpl = s[0];
+                *grp = 1;
+                return;
+            }
+        *cpl = 64;
+        *grp = 1;
+        return;
+    }
+    int want = group > 0 ? group : (cols <= 16 ? 2 : 4);
+    int best = -1;
+    const int n = (int)(sizeof(sdf) / sizeof(sdf[0]));
+    for (int i = 0; i < n; ++i)
+        if (sdf[i][1] == want && sdf[i][0] * sdf[i][1] >= cols && (best < 0 || sdf[i][0] < sdf[best][0])) best = i;
+    if (best < 0)
+        for (int i = 0; i < n; ++i)
+            if (sdf[i][0] * sdf[i][1] >= cols &&
+                (best < 0 || sdf[i][0] * sdf[i][1] < sdf[best][0] * sdf[best][1]))
+                best = i;
+    *cpl = sdf[best][0];
+    *grp = sdf[best][1];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- plan
+
+struct BatchPlan {
+    int device = -1;
+    int64_t count = 0;
+    int arith = GBPERM_ARITH_FP64;
+    bool df = false;
+    int cpl = 16, grp = 1;
+    int grid = 1;
+    int64_t item_target_log2 = 0;
+    std::vector<int> rows, cols;
+    std::vector<long long> off;      // complex offsets of each instance in the packed input
+    std::vector<int> dev_index;      // device instance index or -1 (trivial)
+    std::vector<double> trivial;     // value for trivial instances
+    long long total_elems = 0;       // packed complex elements
+    int ninst = 0, nitems = 0;
+    double steps = 0.0, flops = 0.0;
+    // device buffers
+    char* dbuf = nullptr;
+    size_t dbytes = 0;
+    char* item_buf = nullptr;        // work list + item partial sums
+    size_t item_cap = 0;
+    double2* dA = nullptr;
+    longlong2 *da1 = nullptr, *da2 = nullptr;
+    BInst* dinst = nullptr;
+    BInstOut* diout = nullptr;
+    BItem* ditems = nullptr;
+    unsigned int* dcounter = nullptr;
+    cdd* dpart = nullptr;
+    double* dout = nullptr;
+    // pinned host staging and the captured graph
+    double* hin = nullptr;
+    double* hout = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+static void plan_free(BatchPlan* p) {
+    if (!p) return;
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    if (p->dbuf) cudaFree(p->dbuf);
+    if (p->item_buf) cudaFree(p->item_buf);
+    if (p->hin) cudaFreeHost(p->hin);
+    if (p->hout) cudaFreeHost(p->hout);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+static BArgs plan_args(BatchPlan* p) {
+    BArgs a;
+    a.A = p->dA;
+    a.a1 = p->da1;
+    a.a2 = p->da2;
+    a.inst = p->dinst;
+    a.iout = p->diout;
+    a.items = p->ditems;
+    a.nitems = p->nitems;
+    a.ninst = p->ninst;
+    a.counter = p->dcounter;
+    a.item_part = p->dpart;
+    a.out = p->dout;
+    a.df = p->df ? 1 : 0;
+    return a;
+}
+
+// Enqueue prepare + worker + finalize on the plan's stream (device input
+// already in p->dA).
+static cudaError_t plan_enqueue(BatchPlan* p) {
+    if (p->ninst == 0) return cudaSuccess;
+    BArgs a = plan_args(p);
+    cudaError_t e = cudaMemsetAsync(p->dcounter, 0, sizeof(unsigned int), p->stream);
+    if (e != cudaSuccess) return e;
+    int pg = std::min(p->ninst, 4 * device_sms(p->device));
+    batched_prepare_kernel<<<pg, 64, 0, p->stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = batch_launch(a, p->cpl, p->grp, p->df, p->grid, p->stream);
+    if (e != cudaSuccess) return e;
+    batched_finalize_kernel<<<(p->ninst + 127) / 128, 128, 0, p->stream>>>(a);
+    return cudaGetLastError();
+}
+
+// Build instance descriptors and the LPT-ordered item list for the current
+// item target, upload them.
+static int plan_build_items(BatchPlan* p) {
+    const int spi = 32 / p->grp;
+    std::vector<int> order;
+    for (int64_t i = 0; i < p->count; ++i)
+        if (p->dev_index[i] >= 0) order.push_back((int)i);
+    // largest first
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        double cx = std::ldexp((double)p->cols[x], p->rows[x]);
+        double cy = std::ldexp((double)p->cols[y], p->rows[y]);
+        return cx > cy;
+    });
+    std::vector<BInst> inst(p->ninst);
+    std::vector<BItem> items;
+    for (int i : order) {
+        int d = p->dev_index[i];
+        BInst b;
+        b.rows = p->rows[i];
+        b.cols = p->cols[i];
+        b.a_off = p->off[i];
+        int slog = b.rows - 1;
+        // steps per item ~ 2^target; segment length = that / SPI
+        int l = (int)p->item_target_log2 - ceil_log2_u64((unsigned long long)spi);
+        if (l > slog) l = slog;
+        if (l < 0) l = 0;
+        b.seg_log2 = l;
+        b.nseg = 1ull << (slog - l);
+        b.item0 = (int)items.size();
+        unsigned long long nit = (b.nseg + spi - 1) / spi;
+        for (unsigned long long k = 0; k < nit; ++k) {
+            BItem it;
+            it.inst = d;
+            it.pad = 0;
+            it.seg0 = k * (unsigned long long)spi;
+            items.push_back(it);
+        }
+        b.nitems = (int)nit;
+        inst[d] = b;
+    }
+    p->nitems = (int)items.size();
+    if (items.size() > p->item_cap) {
+        if (p->item_buf) cudaFree(p->item_buf);
+        p->item_buf = nullptr;
+        p->item_cap = 0;
+        size_t want = items.size() + items.size() / 4 + 64;
+        cudaError_t ea = cudaMalloc(&p->item_buf, align_up(want * sizeof(BItem), 256) + want * sizeof(cdd));
+        if (ea != cudaSuccess) return cuda_fail(ea, "batched: work list allocation");
+        p->item_cap = want;
+        p->ditems = reinterpret_cast<BItem*>(p->item_buf);
+        p->dpart = reinterpret_cast<cdd*>(p->item_buf + align_up(want * sizeof(BItem), 256));
+    }
+    cudaError_t e = cudaMemcpy(p->dinst, inst.data(), inst.size() * sizeof(BInst), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !items.empty())
+        e = cudaMemcpy(p->ditems, items.data(), items.size() * sizeof(BItem), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "batched: upload work list");
+    return GBPERM_OK;
+}
+
+static int plan_capture(BatchPlan* p) {
+    if (p->graph) {
+        cudaGraphExecDestroy(p->graph);
+        p->graph = nullptr;
+    }
+    if (p->ninst == 0) return GBPERM_OK;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "batched: begin capture");
+    e = cudaMemcpyAsync(p->dA, p->hin, (size_t)p->total_elems * sizeof(double2), cudaMemcpyHostToDevice, p->stream);
+    cudaError_t e2 = (e == cudaSuccess) ? plan_enqueue(p) : e;
+    cudaError_t e3 = (e2 == cudaSuccess)
+                         ? cudaMemcpyAsync(p->hout, p->dout, (size_t)p->ninst * 2 * sizeof(double),
+                                           cudaMemcpyDeviceToHost, p->stream)
+                         : e2;
+    e = cudaStreamEndCapture(p->stream, &g);
+    if (e3 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e3, "batched: capture");
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "batched: end capture");
+    e = cudaGraphInstantiate(&p->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "batched: instantiate graph");
+    return GBPERM_OK;
+}
+
+}  // namespace gbperm
+
+using namespace gbperm;
+
+struct gbperm_batch_plan {
+    BatchPlan* p;
+};
+
+extern "C" {
+
+int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t count, int arith,
+                             gbperm_batch_plan** out_plan) {
+    if (!out_plan) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_create: null plan pointer");
+    *out_plan = nullptr;
+    if (count < 0 || (count > 0 && (!rows || !cols))) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_create: bad sizes");
+    if (count > (int64_t)1 << 28) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_batch_plan_create: too many instances");
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+        return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_create: unknown arithmetic");
+    BatchPlan* p = new BatchPlan();
+    p->count = count;
+    p->arith = arith;
+    int maxc = 1;
+    double total_steps = 0.0;
+    for (int64_t i = 0; i < count; ++i) {
+        if (rows[i] < 0 || cols[i] < 0) {
+            plan_free(p);
+            return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_create: negative shape");
+        }
+        p->rows.push_back((int)rows[i]);
+        p->cols.push_back((int)cols[i]);
+        p->off.push_back(p->total_elems);
+        p->total_elems += rows[i] * cols[i];
+        double v = -1.0;
+        if (rows[i] == 0 || cols[i] == 0) v = 1.0;
+        else if (rows[i] >= cols[i] + 2) v = 0.0;
+        if (v < 0.0 && (rows[i] > GBPERM_MAX_DIM || cols[i] > GBPERM_MAX_DIM)) {
+            plan_free(p);
+            return fail(GBPERM_ERR_TOO_LARGE, "gbperm_batch_plan_create: matrix larger than 64 x 64");
+        }
+        p->trivial.push_back(v < 0.0 ? 0.0 : v);
+        p->dev_index.push_back(v < 0.0 ? p->ninst++ : -1);
+        if (v < 0.0) {
+            maxc = std::max(maxc, (int)cols[i]);
+            total_steps += std::ldexp(1.0, (int)rows[i] - 1);
+            p->flops += 8.0 * (double)cols[i] * std::ldexp(1.0, (int)rows[i] - 1);
+        }
+    }
+    p->steps = total_steps;
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        return cuda_fail(e, "gbperm_batch_plan_create");
+    }
+    p->df = arith == GBPERM_ARITH_DF32 && maxc <= kDfMaxCols;
+    batch_shape(maxc, p->df, (int)g_opt.batched_threads.load(), &p->cpl, &p->grp);
+    int bps = batch_bps(p->cpl, p->grp, p->df);
+    p->grid = device_sms(p->device) * bps;
+    // item target: ~16 items per resident warp over the whole batch
+    double warps = (double)p->grid * (kThreads / 32);
+    double tgt = total_steps / std::max(1.0, warps * 16.0);
+    int tl = 0;
+    while (std::ldexp(1.0, tl) < tgt && tl < 40) ++tl;
+    p->item_target_log2 = std::max(tl, 8);
+    int64_t force = g_opt.batched_item_log2.load();
+    if (force > 0) p->item_target_log2 = force;
+    // device buffers (the work list is allocated with the items)
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        size_t o = off;
+        off += align_up(b ? b : 1, 256);
+        return o;
+    };
+    size_t oA = take((size_t)p->total_elems * sizeof(double2));
+    size_t o1 = take((size_t)p->total_elems * sizeof(longlong2));
+    size_t o2 = take((size_t)p->total_elems * sizeof(longlong2));
+    size_t oI = take((size_t)std::max(1, p->ninst) * sizeof(BInst));
+    size_t oO = take((size_t)std::max(1, p->ninst) * sizeof(BInstOut));
+    size_t oC = take(sizeof(unsigned int));
+    size_t oR = take((size_t)std::max(1, p->ninst) * 2 * sizeof(double));
+    p->dbytes = off;
+    e = cudaMalloc(&p->dbuf, p->dbytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&p->hin, std::max<size_t>(1, (size_t)p->total_elems) * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMallocHost(&p->hout, (size_t)std::max(1, p->ninst) * 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        return cuda_fail(e, "gbperm_batch_plan_create: allocation");
+    }
+    p->dA = reinterpret_cast<double2*>(p->dbuf + oA);
+    p->da1 = reinterpret_cast<longlong2*>(p->dbuf + o1);
+    p->da2 = reinterpret_cast<longlong2*>(p->dbuf + o2);
+    p->dinst = reinterpret_cast<BInst*>(p->dbuf + oI);
+    p->diout = reinterpret_cast<BInstOut*>(p->dbuf + oO);
+    p->dcounter = reinterpret_cast<unsigned int*>(p->dbuf + oC);
+    p->dout = reinterpret_cast<double*>(p->dbuf + oR);
+    int rc = plan_build_items(p);
+    if (rc == GBPERM_OK) rc = plan_capture(p);
+    if (rc) {
+        plan_free(p);
+        return rc;
+    }
+    gbperm_batch_plan* h = new gbperm_batch_plan{p};
+    *out_plan = h;
+    return GBPERM_OK;
+}
+
+void gbperm_batch_plan_destroy(gbperm_batch_plan* plan) {
+    if (!plan) return;
+    plan_free(plan->p);
+    delete plan;
+}
+
+int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double* out, gbperm_stats* stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (!plan || !plan->p) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run: null plan");
+    BatchPlan* p = plan->p;
+    if (p->count > 0 && !out) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run: null output");
+    if (p->total_elems > 0 && !packed) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run: null input");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != p->device) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run: plan belongs to another device");
+    // gather device instances into the pinned staging buffer (packed order)
+    if (p->ninst > 0) {
+        for (int64_t i = 0; i < p->count; ++i) {
+            if (p->dev_index[i] < 0) continue;
+            std::memcpy(p->hin + 2 * p->off[i], packed + 2 * p->off[i],
+                        (size_t)p->rows[i] * p->cols[i] * sizeof(double2));
+        }
+        if (stats) cudaEventRecord(p->ev0, p->stream);
+        cudaError_t e = cudaGraphLaunch(p->graph, p->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run: graph launch");
+        if (stats) cudaEventRecord(p->ev1, p->stream);
+        e = cudaStreamSynchronize(p->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run: kernels");
+    }
+    for (int64_t i = 0; i < p->count; ++i) {
+        int d = p->dev_index[i];
+        if (d < 0) {
+            out[2 * i] = p->trivial[i];
+            out[2 * i + 1] = 0.0;
+        } else {
+            out[2 * i] = p->hout[2 * d];
+            out[2 * i + 1] = p->hout[2 * d + 1];
+        }
+    }
+    if (stats && p->ninst > 0) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        stats->kernel_ms = ms;
+        stats->steps = p->steps;
+        stats->flops = p->flops;
+        stats->launches = 3;
+        stats->grid = p->grid;
+        stats->seg_log2 = (int)p->item_target_log2;
+        stats->arith = p->df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+    }
+    return GBPERM_OK;
+}
+
+int gbperm_batch_plan_run_dev(gbperm_batch_plan* plan, const void* d_packed, void* d_out, void* stream) {
+    if (!plan || !plan->p) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run_dev: null plan");
+    BatchPlan* p = plan->p;
+    if (p->ninst == 0) return GBPERM_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // device-to-device gather of the non-trivial instances is the identity
+    // on the packed layout; results for trivial instances are left to the caller
+    cudaError_t e = cudaMemcpyAsync(p->dA, d_packed, (size_t)p->total_elems * sizeof(double2),
+                                    cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: copy");
+    cudaStream_t saved = p->stream;
+    p->stream = st;
+    e = plan_enqueue(p);
+    p->stream = saved;
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: launch");
+    // scatter: device instance d -> output slot i
+    for (int64_t i = 0; i < p->count; ++i) {
+        int d = p->dev_index[i];
+        if (d < 0) continue;
+        e = cudaMemcpyAsync(static_cast<double*>(d_out) + 2 * i, p->dout + 2 * d, 2 * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: scatter");
+    }
+    return GBPERM_OK;
+}
+
+int gbperm_batch_plan_set_item_log2(gbperm_batch_plan* plan, int64_t item_log2) {
+    if (!plan || !plan->p) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_set_item_log2: null plan");
+    BatchPlan* p = plan->p;
+    if (item_log2 < 0 || item_log2 > 40) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_set_item_log2: out of range");
+    p->item_target_log2 = item_log2;
+    int rc = plan_build_items(p);
+    if (rc == GBPERM_OK) rc = plan_capture(p);
+    return rc;
+}
+
+int64_t gbperm_batch_plan_get_item_log2(gbperm_batch_plan* plan) {
+    return (plan && plan->p) ? plan->p->item_target_log2 : -1;
+}
+
+int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t* cols, int64_t count, int arith,
+                        double* out, gbperm_stats* stats) {
+    gbperm_batch_plan* plan = nullptr;
+    int rc = gbperm_batch_plan_create(rows, cols, count, arith, &plan);
+    if (rc) return rc;
+    rc = gbperm_batch_plan_run(plan, packed, out, stats);
+    gbperm_batch_plan_destroy(plan);
+    return rc;
+}
+
+}  // extern "C"

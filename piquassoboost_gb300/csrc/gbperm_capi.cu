@@ -91,32 +91,40 @@ int ceil_log2_u64(unsigned long long x) {
 
 // ------------------------------------------------------------------ plain
 
-PlainPlan plan_plain(int rows, int cols, bool df) {
-    PlainPlan p;
-    p.df = df;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int sms = device_sms(dev);
-    int bps = plain_blocks_per_sm(rows, cols, df);
-    int grid_full = sms * bps;
+// Segment length and grid for `seg_threads` threads per segment.
+static void plain_geometry(int rows, int grid_full, int seg_threads, int* grid, int* seg_log2) {
     int slog = rows - 1;
-    // aim at >= 64 segments per thread (load balance within ~1.5%) while
-    // keeping segments >= 16 steps when the problem allows it
-    unsigned long long T = (unsigned long long)grid_full * 128ull;
-    int l = slog - ceil_log2_u64(64ull * T);
+    // aim at >= 64 segments per segment-slot of a full grid (load balance
+    // within ~1.5%) while keeping segments >= 16 steps when possible
+    unsigned long long slots = (unsigned long long)grid_full * (128ull / seg_threads);
+    int l = slog - ceil_log2_u64(64ull * slots);
     if (l < 4) l = slog < 4 ? slog : 4;
     if (l > slog) l = slog;
     if (l < 0) l = 0;
     int64_t force = g_opt.plain_seg_log2.load();
     if (force >= 0) l = (int)(force > slog ? slog : force);
     unsigned long long nseg = 1ull << (slog - l);
-    unsigned long long need = (nseg + 127ull) / 128ull;
-    int grid = (int)(need < (unsigned long long)grid_full ? need : (unsigned long long)grid_full);
+    unsigned long long per_block = 128ull / seg_threads;
+    unsigned long long need = (nseg + per_block - 1) / per_block;
+    int g = (int)(need < (unsigned long long)grid_full ? need : (unsigned long long)grid_full);
     int64_t fg = g_opt.plain_grid.load();
-    if (fg > 0) grid = (int)fg;
-    if (grid < 1) grid = 1;
-    p.grid = grid;
-    p.seg_log2 = l;
+    if (fg > 0) g = (int)fg;
+    if (g < 1) g = 1;
+    *grid = g;
+    *seg_log2 = l;
+}
+
+PlainPlan plan_plain(int rows, int cols, bool df) {
+    PlainPlan p;
+    p.df = df;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = device_sms(dev);
+    plain_geometry(rows, sms * plain_blocks_per_sm(rows, cols), 1, &p.grid, &p.seg_log2);
+    if (df) {
+        df_shape(cols, (int)g_opt.plain_df_group.load(), &p.cpl, &p.grp);
+        plain_geometry(rows, sms * plain_df_blocks_per_sm(rows, p.cpl, p.grp), p.grp, &p.grid_df, &p.seg_log2_df);
+    }
     return p;
 }
 
@@ -139,7 +147,7 @@ size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w) {
 int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, size_t ws_bytes,
                   double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan) {
     PlainWs w;
-    size_t need = plain_ws_layout(rows, cols, plan.grid, &w);
+    size_t need = plain_ws_layout(rows, cols, plan.max_grid(), &w);
     if (ws_bytes < need) return fail(GBPERM_ERR_ARG, "gbperm: workspace too small");
     char* base = static_cast<char*>(ws);
     PrepArgs pa;
@@ -154,10 +162,17 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
     pa.df = plan.df ? 1 : 0;
-    pa.df_scale = reinterpret_cast<float*>(base + w.scale);
+    pa.df_info = reinterpret_cast<int*>(base + w.scale);
     cudaError_t e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
-    e = launch_plain(pa.a1, pa.a2, pa.exp_out, plan.df ? pa.df_scale : nullptr, rows, cols, plan.grid,
+    if (plan.df) {
+        // the double-float kernel returns at once if the device range check
+        // failed; its FP64 twin below returns at once if it passed
+        e = launch_plain_df(pa.a1, pa.a2, pa.exp_out, pa.df_info, rows, cols, plan.cpl, plan.grp, plan.grid_df,
+                            plan.seg_log2_df, base + w.kern, d_out2, d_out4, st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain df launch");
+    }
+    e = launch_plain(pa.a1, pa.a2, pa.exp_out, plan.df ? pa.df_info : nullptr, rows, cols, plan.grid,
                      plan.seg_log2, base + w.kern, d_out2, d_out4, st);
     if (e != cudaSuccess) return cuda_fail(e, "plain launch");
     return GBPERM_OK;
@@ -215,10 +230,8 @@ int64_t gbperm_get_option(const char* key) {
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols) {
     if (rows <= 0 || cols <= 0 || rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM) return 256;
     // the larger of the two arithmetics' needs (grids may differ)
-    PlainPlan p0 = plan_plain((int)rows, (int)cols, false);
-    PlainPlan p1 = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols);
-    PlainPlan plan = p0.grid >= p1.grid ? p0 : p1;
-    return plain_ws_layout((int)rows, (int)cols, plan.grid, nullptr);
+    PlainPlan plan = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols);
+    return plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
 }
 
 int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
@@ -273,7 +286,7 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost);
     PlainPlan plan = plan_plain((int)rows, (int)cols, df);
     size_t mat_bytes = align_up((size_t)rows * cols * sizeof(double2), 256);
-    size_t ws = plain_ws_layout((int)rows, (int)cols, plan.grid, nullptr);
+    size_t ws = plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
     ThreadCtx& c = thread_ctx();
     int rc = c.ensure(mat_bytes + 256 + ws);
     if (rc) return rc;
@@ -302,9 +315,9 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         stats->kernel_ms = ms;
         stats->steps = std::ldexp(1.0, (int)rows - 1);
         stats->flops = 8.0 * (double)cols * stats->steps;
-        stats->launches = 2;
-        stats->grid = plan.grid;
-        stats->seg_log2 = plan.seg_log2;
+        stats->launches = df ? 3 : 2;
+        stats->grid = df ? plan.grid_df : plan.grid;
+        stats->seg_log2 = df ? plan.seg_log2_df : plan.seg_log2;
         stats->arith = df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
     }
     return GBPERM_OK;

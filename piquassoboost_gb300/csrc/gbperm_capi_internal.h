@@ -18,11 +18,15 @@ struct Options {
     std::atomic<int64_t> plain_grid{0};
     std::atomic<int64_t> repeated_low_digits{-1};
     std::atomic<int64_t> batched_threads{0};
+    std::atomic<int64_t> plain_df_group{0};
+    std::atomic<int64_t> batched_item_log2{0};
     std::atomic<int64_t>* find(const char* key) {
         if (!std::strcmp(key, "plain.seg_log2")) return &plain_seg_log2;
         if (!std::strcmp(key, "plain.grid")) return &plain_grid;
         if (!std::strcmp(key, "repeated.low_digits")) return &repeated_low_digits;
         if (!std::strcmp(key, "batched.threads")) return &batched_threads;
+        if (!std::strcmp(key, "plain.df_group")) return &plain_df_group;
+        if (!std::strcmp(key, "batched.item_log2")) return &batched_item_log2;
         return nullptr;
     }
 };
@@ -45,9 +49,13 @@ struct ThreadCtx {
 ThreadCtx& thread_ctx();
 
 struct PlainPlan {
-    int grid = 1;
+    int grid = 1;          // FP64 kernel
     int seg_log2 = 0;
-    bool df = false;
+    bool df = false;       // double-float kernel requested
+    int grid_df = 1;
+    int seg_log2_df = 0;
+    int cpl = 8, grp = 1;  // double-float lane-group shape
+    int max_grid() const { return df && grid_df > grid ? grid_df : grid; }
 };
 struct PlainWs {
     size_t a1 = 0, a2 = 0, exp = 0, scale = 0, kern = 0;

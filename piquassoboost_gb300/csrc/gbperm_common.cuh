@@ -159,6 +159,53 @@ __device__ __forceinline__ void fix_to_df(long long x, float s2, float s1, float
     l = e + f0;
 }
 
+// int64 fixed point -> float pair without conversion instructions.  The three
+// chunks are written straight into float mantissas whose exponents carry the
+// chunk units ("magic number" conversion): for 0 <= c < 2^23,
+//   as_float(bits(2^(23+u)) | c) - 2^(23+u) = c 2^u   exactly,
+// and the signed top chunk is offset by 2^22 first.  m[0..2] are the magic
+// bit patterns for the units 2^(o-20), 2^(o-41), 2^(o-62) of chunks c2, c1,
+// c0; off[0..2] the matching float offsets (off[0] includes the 2^22 shift).
+struct DfConv {
+    unsigned int m2, m1, m0;
+    float o2, o1, o0;
+};
+
+__host__ __device__ inline DfConv make_dfconv(int boost) {
+    DfConv c;
+    // unit exponents of the chunks
+    const int u2 = boost - 20, u1 = boost - 41, u0 = boost - 62;
+    c.m2 = (unsigned int)(127 + 23 + u2) << 23;
+    c.m1 = (unsigned int)(127 + 23 + u1) << 23;
+    c.m0 = (unsigned int)(127 + 23 + u0) << 23;
+    // 2^(23+u) (+ 2^(22+u) for the offset top chunk)
+    union {
+        unsigned int u;
+        float f;
+    } a, b, d;
+    a.u = c.m2;
+    b.u = c.m1;
+    d.u = c.m0;
+    c.o2 = a.f * 1.5f;  // 2^(23+u2) + 2^(22+u2)
+    c.o1 = b.f;
+    c.o0 = d.f;
+    return c;
+}
+
+__device__ __forceinline__ void fix_to_df_magic(long long x, const DfConv& k, float& h, float& l) {
+    const unsigned int lo = (unsigned int)x;
+    const unsigned int hi = (unsigned int)((unsigned long long)x >> 32);
+    const int c2 = ((int)hi >> 10) + (1 << 22);                      // bits 42..63, offset
+    const unsigned int c1 = __funnelshift_r(lo, hi, 21) & 0x1FFFFFu;  // bits 21..41
+    const unsigned int c0 = lo & 0x1FFFFFu;                           // bits 0..20
+    const float f2 = __uint_as_float(k.m2 + (unsigned int)c2) - k.o2;
+    const float f1 = __uint_as_float(k.m1 | c1) - k.o1;
+    const float f0 = __uint_as_float(k.m0 | c0) - k.o0;
+    h = f2 + f1;
+    const float e = f1 - (h - f2);
+    l = e + f0;
+}
+
 // df accumulator: a += (h, l), renormalised
 __device__ __forceinline__ void df_acc(float& ah, float& al, float h, float l) {
     float s, e;

@@ -27,18 +27,37 @@ struct PrepArgs {
     longlong2* a1;           // rows x cols
     longlong2* a2;           // rows x cols
     int* exp_out;            // 1 int
-    int df;                  // 1: also write double-float conversion constants
-    float* df_scale;         // 4 floats: 2^(o-20), 2^(o-41), 2^(o-62), ok (1/0);
-                             // ok = 0 when the range check fails (FP64 then)
+    int df;                  // 1: also decide the double-float range boost
+    int* df_info;            // {o, ok}: boost and range-check result (ok = 0:
+                             // the kernel must use the FP64 product)
 };
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st);
 
 // ------------------------------------------------------------------ plain
+struct PlainArgs {
+    const longlong2* a1;   // rows x cols fixed-point a_ij (unit 2^-62 after column scaling)
+    const longlong2* a2;   // rows x cols fixed-point 2 a_ij
+    int rows, cols;
+    int seg_log2;          // L = 2^seg_log2
+    unsigned long long nseg;
+    cdd* block_part;       // gridDim.x partial sums
+    unsigned int* done;    // completion counter (zero before the launch)
+    const int* exp_in;     // final scale exponent (from the prepare kernel)
+    const int* df_info;    // {boost, ok} from the prepare kernel, or null (FP64 only)
+    double* out2;          // complex128 result
+    double* out4;          // optional: {re_hi, im_hi, re_lo, im_lo} of the scaled result
+};
+
 int plain_bucket(int cols);
-int plain_blocks_per_sm(int rows, int cols, bool df);
+int plain_blocks_per_sm(int rows, int cols);
+void df_shape(int cols, int group, int* cpl, int* grp);
+int plain_df_blocks_per_sm(int rows, int cpl, int grp);
+cudaError_t launch_plain_df(const longlong2* a1, const longlong2* a2, const int* exp_in, const int* df_info,
+                            int rows, int cols, int cpl, int grp, int grid, int seg_log2, void* ws,
+                            double* out2, double* out4, cudaStream_t st);
 size_t plain_workspace_bytes(int grid);
 cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* exp_in,
-                         const float* df_scale, int rows, int cols, int grid, int seg_log2, void* ws,
+                         const int* df_info, int rows, int cols, int grid, int seg_log2, void* ws,
                          double* out2, double* out4, cudaStream_t st);
 
 // Range boost o for the double-float product (host): columns are first
@@ -70,10 +89,14 @@ struct RepArgs {
     cdd* block_part;
     unsigned int* done;
     const int* exp_in;
+    const int* df_info;       // {boost, ok} or null (FP64 only)
     double* out2;
     double* out4;
 };
 int repeated_blocks_per_sm(const RepArgs& a);
+void repeated_df_shape(int cols, int* cpl, int* grp);
+int repeated_df_blocks_per_sm(const RepArgs& a, int cpl, int grp);
+cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, cudaStream_t st);
 size_t repeated_workspace_bytes(int grid);
 cudaError_t launch_repeated(RepArgs a, int grid, void* ws, cudaStream_t st);
 

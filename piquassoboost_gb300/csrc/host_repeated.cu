@@ -229,7 +229,7 @@ size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w) {
     l.wlow = take(h.wlow.size() * sizeof(double));
     l.seq = take(h.seq.size());
     l.binom = take((size_t)kBinomStride * kBinomStride * sizeof(double));
-    l.exp = take(16);
+    l.exp = take(64);  // exponent int at +0, double-float info {boost, ok} at +16
     l.out = take(8 * sizeof(double));
     l.kern = take(repeated_workspace_bytes(grid));
     if (w) *w = l;
@@ -283,8 +283,23 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     unsigned long long grid_full = (unsigned long long)device_sms(dev) * bps;
     unsigned long long need = (h.nseg + 127ull) / 128ull;
     int grid = (int)std::max(1ull, std::min(grid_full, need));
+    // double-float product when requested and the dynamic range allows it
+    bool df = false;
+    int dcpl = 0, dgrp = 0, grid_df = 1;
+    if (arith == GBPERM_ARITH_DF32 && h.C <= kDfMaxCols) {
+        int boost = 0;
+        std::vector<int> cw(h.cpow.begin(), h.cpow.end());
+        df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), cw.data(), &boost);
+    }
+    if (df) {
+        repeated_df_shape(h.C, &dcpl, &dgrp);
+        unsigned long long gfull = (unsigned long long)device_sms(dev) * repeated_df_blocks_per_sm(a, dcpl, dgrp);
+        unsigned long long per_block = 128ull / (unsigned long long)dgrp;
+        unsigned long long need_df = (h.nseg + per_block - 1) / per_block;
+        grid_df = (int)std::max(1ull, std::min(gfull, need_df));
+    }
     RepWs w;
-    size_t bytes = repeated_ws_layout(h, grid, &w);
+    size_t bytes = repeated_ws_layout(h, std::max(grid, grid_df), &w);
     ThreadCtx& c = thread_ctx();
     rc = c.ensure(bytes);
     if (rc) return rc;
@@ -313,8 +328,8 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     pa.a1 = reinterpret_cast<longlong2*>(base + w.a1);
     pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
-    pa.df = 0;
-    pa.df_scale = nullptr;
+    pa.df = df ? 1 : 0;
+    pa.df_info = df ? reinterpret_cast<int*>(base + w.exp + 16) : nullptr;
     if (stats) cudaEventRecord(c.ev0, st);
     e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: prepare");
@@ -327,9 +342,14 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     a.seq = reinterpret_cast<const unsigned char*>(base + w.seq);
     a.binom = reinterpret_cast<const double*>(base + w.binom);
     a.exp_in = pa.exp_out;
+    a.df_info = pa.df_info;
     double* dout = reinterpret_cast<double*>(base + w.out);
     a.out2 = dout;
     a.out4 = dout + 2;
+    if (df) {
+        e = launch_repeated_df(a, dcpl, dgrp, grid_df, base + w.kern, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: df launch");
+    }
     e = launch_repeated(a, grid, base + w.kern, st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: launch");
     if (stats) cudaEventRecord(c.ev1, st);
@@ -346,9 +366,10 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
         stats->kernel_ms = ms;
         stats->steps = h.steps;
         stats->flops = h.flops;
-        stats->launches = 2;
-        stats->grid = grid;
+        stats->launches = df ? 3 : 2;
+        stats->grid = df ? grid_df : grid;
         stats->seg_log2 = h.q;
+        stats->arith = df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
     }
     return GBPERM_OK;
 }

@@ -1,0 +1,295 @@
+// Repeated-multiplicity permanent with the double-float product (GB300).
+//
+// Same sum, digit plan and exact int64 column sums as perm_repeated.cu
+// (BBFGPermanentCalculatorRepeated.hpp:116-307); the product
+// prod_j colsum_j^(c_j) runs as float pairs on the FP32 pipe, with lane groups
+// as in perm_plain_df.cu: GROUP lanes walk one segment, lane g owns columns
+// [g*CPL, (g+1)*CPL) and a shuffle butterfly multiplies the partials.  Every
+// lane of a group tracks the same Gray digits (they are cheap integers), so
+// the weights and signs need no exchange.  Segment loops run over warp-sized
+// blocks of segments so all 32 lanes always reach the shuffles.
+#include "gbperm_internal.h"
+
+namespace gbperm {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
+    return cf{__shfl_xor_sync(0xffffffffu, v.rh, m), __shfl_xor_sync(0xffffffffu, v.rl, m),
+              __shfl_xor_sync(0xffffffffu, v.ih, m), __shfl_xor_sync(0xffffffffu, v.il, m)};
+}
+
+// x^e by squaring (e >= 1)
+__device__ __forceinline__ cf cf_pow(cf x, int e) {
+    cf acc = x;
+    bool have = false;
+    cf y = x;
+    while (e > 0) {
+        if (e & 1) {
+            acc = have ? cf_mul(acc, y) : y;
+            have = true;
+        }
+        e >>= 1;
+        if (e) y = cf_mul(y, y);
+    }
+    return acc;
+}
+
+template <int CPL, int GROUP>
+__global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
+    constexpr int NP = CPL * GROUP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);            // R x NP
+    longlong2* s_a2 = s_a1 + p.R * NP;                                   // nd x NP
+    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);           // P
+    unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);  // P
+    __shared__ int s_cpow[NP];
+    __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
+    __shared__ long long s_stride[kMaxDigits];
+    const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    if (p.df_info[1] == 0) return;  // range check failed: the FP64 kernel runs instead
+    for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
+    }
+    for (int e = threadIdx.x; e < nd * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
+    }
+    for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
+        s_w[e] = p.wlow[e];
+        s_seq[e] = p.seq[e];
+    }
+    for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
+    for (int e = threadIdx.x; e < nd; e += blockDim.x) s_D[e] = p.D[e];
+    for (int e = threadIdx.x; e < R; e += blockDim.x) s_r[e] = p.rcoef[e];
+    if (threadIdx.x == 0) {
+        long long s = 1;
+        for (int i = 0; i < q; ++i) {
+            s_stride[i] = s;
+            s *= (long long)(p.D[i] + 1);
+        }
+    }
+    __syncthreads();
+
+    const DfConv cv = make_dfconv(p.df_info[0]);
+    const int g = threadIdx.x % GROUP;
+    const int j0 = g * CPL;
+    const bool leader = (g == 0);
+    cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
+    const unsigned long long lane_seg = (threadIdx.x & 31) / GROUP;
+    long long cre[CPL], cim[CPL];
+
+    for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / GROUP;
+         hw < p.nseg; hw += T) {
+        const unsigned long long h_raw = hw + lane_seg;
+        const bool active = h_raw < p.nseg;
+        const unsigned long long h = active ? h_raw : 0ull;
+        int gdig[kMaxDigits];
+        {
+            unsigned long long rem = h;
+            int cnt[kMaxDigits];
+            for (int i = q; i < nd; ++i) {
+                unsigned long long L = (unsigned long long)(s_D[i] + 1);
+                cnt[i] = (int)(rem % L);
+                rem /= L;
+            }
+            int par = 0;
+            for (int i = nd - 1; i >= 0; --i) {
+                int c = i >= q ? cnt[i] : 0;
+                int gg = par ? s_D[i] - c : c;
+                gdig[i] = gg;
+                par ^= gg & 1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cre[c] = 0;
+            cim[c] = 0;
+        }
+        int gsum = 0;
+        double whigh = 1.0;
+        unsigned long long Gd = 0ull;
+        unsigned int dir = 0u;
+        long long widx = 0;
+        for (int i = 0; i < R; ++i) {
+            int gi = i < nd ? gdig[i] : 0;
+            long long coef = (long long)(s_r[i] - 2 * gi);
+            const longlong2* a = s_a1 + i * NP + j0;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                longlong2 v = a[c];
+                cre[c] += coef * v.x;
+                cim[c] += coef * v.y;
+            }
+            if (i < nd) {
+                gsum += gi;
+                if (i < q) {
+                    Gd |= (unsigned long long)gi << (4 * i);
+                    if (gi == 0) dir |= 1u << i;
+                    widx += (long long)gi * s_stride[i];
+                } else {
+                    whigh *= p.binom[s_D[i] * kBinomStride + gi];
+                }
+            }
+        }
+        unsigned int sbit = (unsigned int)(gsum & 1) << 31;
+        float brh = 0.f, brl = 0.f, bih = 0.f, bil = 0.f;
+        for (unsigned long long k = 0; k < p.P; ++k) {
+            if (k != 0) {
+                const int d = s_seq[k];  // warp-uniform
+                const bool up = (dir >> d) & 1u;
+                const int sh = 4 * d;
+                int gv = (int)((Gd >> sh) & 15ull);
+                gv += up ? 1 : -1;
+                Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
+                if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
+                widx += up ? s_stride[d] : -s_stride[d];
+                const longlong2* a = s_a2 + d * NP + j0;
+                if (up) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] -= v.x;
+                        cim[c] -= v.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] += v.x;
+                        cim[c] += v.y;
+                    }
+                }
+                sbit ^= 0x80000000u;
+                if ((k & 255ull) == 0) {
+                    acc.re = dd_add(acc.re, dd{(double)brh * whigh, (double)brl * whigh});
+                    acc.im = dd_add(acc.im, dd{(double)bih * whigh, (double)bil * whigh});
+                    brh = brl = bih = bil = 0.f;
+                }
+            }
+            cf pa{1.f, 0.f, 0.f, 0.f};
+            bool first = true;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                const int e = s_cpow[j0 + c];  // 0 for padded columns
+                if (e > 0) {
+                    cf x;
+                    fix_to_df_magic(cre[c], cv, x.rh, x.rl);
+                    fix_to_df_magic(cim[c], cv, x.ih, x.il);
+                    if (e > 1) x = cf_pow(x, e);
+                    pa = first ? x : cf_mul(pa, x);
+                    first = false;
+                }
+            }
+#pragma unroll
+            for (int m = 1; m < GROUP; m <<= 1) pa = cf_mul(pa, shfl_xor_cf(pa, m));
+            if (leader && active) {
+                // weight: exact integer table entry (<= 2^53 here) as a float pair
+                const double w = s_w[widx];
+                const float wh = (float)w;
+                const float wl = (float)(w - (double)wh);
+                cf t = cf_mul(pa, cf{wh, wl, 0.f, 0.f});
+                df_acc(brh, brl, __uint_as_float(__float_as_uint(t.rh) ^ sbit),
+                       __uint_as_float(__float_as_uint(t.rl) ^ sbit));
+                df_acc(bih, bil, __uint_as_float(__float_as_uint(t.ih) ^ sbit),
+                       __uint_as_float(__float_as_uint(t.il) ^ sbit));
+            }
+        }
+        acc.re = dd_add(acc.re, dd{(double)brh * whigh, (double)brl * whigh});
+        acc.im = dd_add(acc.im, dd{(double)bih * whigh, (double)bil * whigh});
+    }
+
+    __shared__ cdd s_warp[kThreads / 32];
+    __shared__ bool s_last;
+    acc = warp_sum_cdd(acc);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd b = s_warp[0];
+        for (int w = 1; w < kThreads / 32; ++w) b = cdd_add(b, s_warp[w]);
+        p.block_part[blockIdx.x] = b;
+        __threadfence();
+        unsigned int t = atomicAdd(p.done, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        for (unsigned int bk = 0; bk < gridDim.x; ++bk) {
+            const volatile double* qv = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
+            cdd v{{qv[0], qv[1]}, {qv[2], qv[3]}};
+            tot = cdd_add(tot, v);
+        }
+        write_result(tot, *p.exp_in, p.out2, p.out4);
+        *p.done = 0u;
+    }
+}
+
+template <int CPL, int GROUP>
+size_t rep_df_smem(const RepArgs& a) {
+    return (size_t)(a.R + a.nd) * CPL * GROUP * sizeof(longlong2) + (size_t)a.P * (sizeof(double) + 1) + 16;
+}
+
+template <int CPL, int GROUP>
+cudaError_t launch_rep_df_t(const RepArgs& a, int grid, cudaStream_t st) {
+    size_t smem = rep_df_smem<CPL, GROUP>(a);
+    cudaError_t e = cudaFuncSetAttribute(repeated_df_kernel<CPL, GROUP>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    repeated_df_kernel<CPL, GROUP><<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int CPL, int GROUP>
+int rep_df_bps_t(const RepArgs& a) {
+    int nb = 0;
+    size_t smem = rep_df_smem<CPL, GROUP>(a);
+    cudaFuncSetAttribute(repeated_df_kernel<CPL, GROUP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, repeated_df_kernel<CPL, GROUP>, kThreads, smem);
+    return nb > 0 ? nb : 1;
+}
+
+#define GBPERM_REP_DF_SHAPES(X) \
+    X(4, 2) X(6, 2) X(8, 2) X(10, 2) X(12, 2) X(14, 2) X(16, 2) X(18, 2) X(20, 2) X(24, 2)
+
+}  // namespace
+
+void repeated_df_shape(int cols, int* cpl, int* grp) {
+    static const int c2[] = {4, 6, 8, 10, 12, 14, 16, 18, 20, 24};
+    *grp = 2;
+    *cpl = 24;
+    for (int c : c2)
+        if (2 * c >= cols) {
+            *cpl = c;
+            return;
+        }
+}
+
+int repeated_df_blocks_per_sm(const RepArgs& a, int cpl, int grp) {
+#define X(C, G) \
+    if (cpl == C && grp == G) return rep_df_bps_t<C, G>(a);
+    GBPERM_REP_DF_SHAPES(X)
+#undef X
+    return 1;
+}
+
+cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, cudaStream_t st) {
+    char* w = static_cast<char*>(ws);
+    a.block_part = reinterpret_cast<cdd*>(w);
+    a.done = reinterpret_cast<unsigned int*>(w + align_up((size_t)grid * sizeof(cdd), 256));
+    cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+#define X(C, G) \
+    if (cpl == C && grp == G) return launch_rep_df_t<C, G>(a, grid, st);
+    GBPERM_REP_DF_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace gbperm

@@ -57,10 +57,8 @@ __global__ void prepare_kernel(PrepArgs p) {
             }
             if (!ok) o = 0;
             tot -= (long long)o * pw;
-            p.df_scale[0] = ldexpf(1.0f, o - 20);
-            p.df_scale[1] = ldexpf(1.0f, o - 41);
-            p.df_scale[2] = ldexpf(1.0f, o - 62);
-            p.df_scale[3] = ok ? 1.0f : 0.0f;
+            p.df_info[0] = o;
+            p.df_info[1] = ok;
         }
         p.exp_out[0] = (int)(tot - p.norm_shift);
     }

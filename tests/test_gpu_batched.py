@@ -1,0 +1,75 @@
+"""GPU parity of the batched persistent kernel."""
+import numpy as np
+import pytest
+
+from piquassoboost_gb300 import _native as nat
+from piquassoboost_gb300.workloads import batched_instances
+from tests import oracle_bind as orc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_batched_uneven_vs_oracle(mode):
+    mats = batched_instances(96, seed=5, modes=40, kmin=1, kmax=16)
+    vals = nat.perm_batched(mats, mode=mode)
+    for m, v in zip(mats, vals):
+        _, q = orc.bbfg(m, prec=1)
+        assert orc.rel_err(v, q) <= TOL
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_batched_matches_single_kernel(mode):
+    mats = batched_instances(24, seed=9, modes=60, kmin=16, kmax=22)
+    vals = nat.perm_batched(mats, mode=mode)
+    for m, v in zip(mats, vals):
+        ref = nat.perm(m, mode="fp64")
+        assert abs(v - ref) <= TOL * abs(ref)
+
+
+def test_batched_trivial_and_rectangular():
+    rng = np.random.default_rng(2)
+    mats = [np.zeros((0, 0)), np.ones((5, 2)), rng.standard_normal((3, 5)) + 1j, rng.standard_normal((4, 3)),
+            rng.standard_normal((1, 1))]
+    vals = nat.perm_batched(mats, mode="fp64")
+    assert vals[0] == 1 and vals[1] == 0
+    for m, v in zip(mats[2:], vals[2:]):
+        ref, q = orc.bbfg(m, prec=1)
+        assert orc.rel_err(v, q) <= TOL
+
+
+def test_batched_nan_instance_isolated():
+    a = np.ones((4, 4)); b = np.ones((4, 4)); b[1, 2] = np.nan
+    vals = nat.perm_batched([a, b, a], mode="fast")
+    assert abs(vals[0] - 24) < 1e-9 and abs(vals[2] - 24) < 1e-9
+    assert np.isnan(vals[1].real)
+
+
+def test_batched_plan_reuse_and_item_sizes():
+    mats = batched_instances(40, seed=21, modes=50, kmin=8, kmax=18)
+    plan = nat.BatchPlan([m.shape for m in mats], mode="fast")
+    first = plan.run(mats)
+    for item_log2 in (6, 10, 14):
+        plan.set_item_log2(item_log2)
+        again = plan.run(mats)
+        for a, b in zip(first, again):
+            assert abs(a - b) <= TOL * abs(b)
+    other = batched_instances(40, seed=22, modes=50, kmin=8, kmax=18)
+    # same shapes are required; rebuild for the other draw
+    plan2 = nat.BatchPlan([m.shape for m in other], mode="fast")
+    vals = plan2.run(other)
+    for m, v in zip(other, vals):
+        ref = nat.perm(m, mode="fp64")
+        assert abs(v - ref) <= TOL * abs(ref)
+    plan.close(); plan2.close()
+
+
+def test_dropin_list_branch_uses_batched():
+    from piquassoboost_gb300.sampling.Boson_Sampling_Utilities import BBFGPermanentDouble
+    mats = batched_instances(10, seed=3, modes=20, kmin=4, kmax=10)
+    vals = BBFGPermanentDouble(mats).calculate()
+    assert isinstance(vals, list) and len(vals) == 10
+    for m, v in zip(mats, vals):
+        _, q = orc.bbfg(m, prec=1)
+        assert orc.rel_err(v, q) <= TOL

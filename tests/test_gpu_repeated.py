@@ -20,10 +20,11 @@ def _random_case(seed):
     return A, cin, rout
 
 
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
 @pytest.mark.parametrize("seed", range(60))
-def test_repeated_random(seed):
+def test_repeated_random(seed, mode):
     A, cin, rout = _random_case(seed)
-    v = nat.perm_repeated(A, cin, rout)
+    v = nat.perm_repeated(A, cin, rout, mode=mode)
     ref, dref = orc.bbfg_repeated(A, cin, rout, prec=1)
     if abs(ref) < 1e-300:
         assert abs(v) < 1e-12
@@ -43,11 +44,24 @@ def test_repeated_matches_expanded_plain():
     assert orc.rel_err(v, dref) <= TOL
 
 
-def test_repeated_config3_small():
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_repeated_config3_small(mode):
     U, inp, out = repeated_instance(seed=11, modes=24, photons=12, max_mult=4)
-    v = nat.perm_repeated(U, inp, out)
+    st = nat.Stats()
+    v = nat.perm_repeated(U, inp, out, mode=mode, stats=st)
     _, dref = orc.bbfg_repeated(U, inp, out, prec=1)
     assert orc.rel_err(v, dref) <= TOL
+    if mode == "fast":
+        assert st.arith == nat.ARITH_DF32
+
+
+def test_repeated_fast_vs_fp64_boson_sampling_shape():
+    # 40 modes, 20 photons (the 60-mode / 30-photon shape at a size the FP64
+    # kernel finishes in well under a second)
+    U, inp, out = repeated_instance(seed=5, modes=40, photons=20, max_mult=4)
+    a = nat.perm_repeated(U, inp, out, mode="fast")
+    b = nat.perm_repeated(U, inp, out, mode="fp64")
+    assert abs(a - b) <= TOL * abs(b)
 
 
 def test_repeated_state_sum_error():
