@@ -164,8 +164,6 @@ def perm(matrix, mode="fp64", return_dd: bool = False, stats: Stats | None = Non
     rows, cols = a.shape
     out = np.zeros(2)
     dd = np.zeros(4)
-    if rows > 0 and cols > 0 and rows < cols + 2:
-        require_device()
     rc = lib.gbperm_perm(a.ctypes.data_as(_P), rows, cols, cols, arith_of(mode), out.ctypes.data_as(_P),
                          dd.ctypes.data_as(_P),
                          ctypes.byref(stats) if stats is not None else None)
@@ -195,8 +193,6 @@ def perm_repeated(matrix, input_state, output_state, mode="fp64", return_dd: boo
     rows, cols = a.shape
     out = np.zeros(2)
     dd = np.zeros(4)
-    if rows > 0 and cm.sum() > 0 and cm.sum() == rm.sum():
-        require_device()
     rc = lib.gbperm_perm_repeated(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), len(cm),
                                   rm.ctypes.data_as(_P), len(rm), arith_of(mode), out.ctypes.data_as(_P),
                                   dd.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None)

@@ -47,6 +47,11 @@ ThreadCtx& thread_ctx() {
 }
 
 int ThreadCtx::ensure(size_t bytes) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return fail(GBPERM_ERR_NO_DEVICE, "no CUDA device visible: the GB300 permanent library needs a GPU");
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");

@@ -81,22 +81,35 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
         for (unsigned long long k = 0; k < L; ++k) {
             if (k != 0) {
                 const int b = __ffsll((long long)k) - 1;  // warp-uniform
-                const unsigned long long idx = i0 + k;
-                const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;  // group-uniform
                 const longlong2* a = s_a2 + (rows - 1 - b) * NP + j0;
-                if (sub) {
+                if (b + 1 < p.seg_log2) {
+                    // the new delta is Gray bit b of i0 + k; below the segment
+                    // boundary bit it depends on k alone: a uniform branch
+                    const bool sub = ((k >> b) ^ (k >> (b + 1))) & 1ull;
+                    if (sub) {
 #pragma unroll
-                    for (int c = 0; c < CPL; ++c) {
-                        longlong2 v = a[c];
-                        cre[c] -= v.x;
-                        cim[c] -= v.y;
+                        for (int c = 0; c < CPL; ++c) {
+                            longlong2 v = a[c];
+                            cre[c] -= v.x;
+                            cim[c] -= v.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < CPL; ++c) {
+                            longlong2 v = a[c];
+                            cre[c] += v.x;
+                            cim[c] += v.y;
+                        }
                     }
                 } else {
+                    // k = L/2: the direction depends on the segment (once per segment)
+                    const unsigned long long idx = i0 + k;
+                    const long long m = -(long long)(((idx >> b) ^ (idx >> (b + 1))) & 1ull);
 #pragma unroll
                     for (int c = 0; c < CPL; ++c) {
                         longlong2 v = a[c];
-                        cre[c] += v.x;
-                        cim[c] += v.y;
+                        cre[c] += (v.x ^ m) - m;
+                        cim[c] += (v.y ^ m) - m;
                     }
                 }
                 sbit ^= 0x80000000u;

@@ -139,14 +139,14 @@ class RepeatedPermanentCalculator(ChinHuhPermanentCalculator_wrapper):
                 input_state = np.array(input_state, dtype=np.int64)
             else:
                 for item in input_state:
-                    if not isinstance(item, np.ndarray) and not isinstance(item, list):
+                    if not isinstance(item, np.ndarray):
                         raise Exception('The input state should be a numpy array, or a list of numpy arrays')
         if not isinstance(output_state, np.ndarray):
             if not isinstance(output_state, list):
                 output_state = np.array(output_state, dtype=np.int64)
             else:
                 for item in output_state:
-                    if not isinstance(item, np.ndarray) and not isinstance(item, list):
+                    if not isinstance(item, np.ndarray):
                         raise Exception('The output state should be a numpy array, or a list of numpy arrays')
         super().__init__(lib=lib, matrix=matrix, input_state=input_state, output_state=output_state)
 
