@@ -124,6 +124,21 @@ size_t gbperm_perm_grad_workspace_size(int64_t n);
 int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, void* d_perm_dd, void* d_grad,
                          void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------- allocation-free plain permanent */
+/* No counterpart in the reference.  The plain permanent for callers that
+ * cannot allocate device memory (their pool belongs to another allocator, or
+ * they must not pay cudaMalloc's device-wide synchronisation): same inputs,
+ * outputs and arithmetics as gbperm_perm_dev, but the scratch lives in one
+ * library-owned device array of gbperm_perm_noalloc_scratch_bytes() bytes
+ * (256 KiB) that every GPU loading the library keeps until exit; sizes whose
+ * scratch would not fit return GBPERM_ERR_TOO_LARGE.  The first call on a
+ * device looks the array's device address up (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race, so serialise them. */
+int gbperm_perm_noalloc(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
+                        void* d_out_dd, void* stream);
+size_t gbperm_perm_noalloc_scratch_bytes(void);
+
 /* ------------------------------------------------------------- probes */
 /* Measured pipe peak of the current device in TFLOP/s (FMA = 2 flops):
  * kind 0 = FP64 FMA, kind 1 = FP32 FMA.  Runs ~0.1 s of probe kernels. */

@@ -86,6 +86,8 @@ _SIGNATURES = [
     ("gbperm_perm_grad", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P]),
     ("gbperm_perm_grad_workspace_size", ctypes.c_size_t, [_I64]),
     ("gbperm_perm_grad_dev", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    ("gbperm_perm_noalloc", ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P]),
+    ("gbperm_perm_noalloc_scratch_bytes", ctypes.c_size_t, []),
     ("gbperm_perm_repeated", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
 ]
