@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "repeated", "batched", "grad"],
+                    help="plain: single n x n Haar block (default); repeated: 60-mode / 30-photon "
+                         "multiplicity permanent; batched: 4096 uneven k=8..28 permanents in one launch; "
+                         "grad: permanent + full gradient")
     ap.add_argument("--n", type=int, default=36)
     ap.add_argument("--mode", default="fast", choices=["fast", "fp64"])
     ap.add_argument("--seed", type=int, default=36)
@@ -98,6 +102,24 @@ def cpu_sample_rate(A: np.ndarray, seconds: float, threads: int = 0):
 
 def host_threads() -> int:
     return os.cpu_count() or 1
+
+
+def traffic_from_profile(n: int, mode: str):
+    """DRAM bytes per launch of the permanent kernel, from the committed ncu
+    summary of this workload (profiles/bench_plain_n36_launches.md), or None."""
+    if n != 36 or mode != "fast":
+        return None
+    path = os.path.join(ROOT, "profiles", "bench_plain_n36_launches.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    import re
+    rd = re.search(r"dram__bytes_read\.sum \| ([0-9,]+) B", text)
+    wr = re.search(r"dram__bytes_write\.sum \| ([0-9,]+) B", text)
+    if not rd or not wr:
+        return None
+    return int(rd.group(1).replace(",", "")) + int(wr.group(1).replace(",", ""))
 
 
 # --------------------------------------------------------------- clocks
@@ -219,13 +241,17 @@ def run_ours(args, rank, world, local):
     sptr = ctypes.c_void_p(stream.cuda_stream)
     # per-rank, per-step seeded inputs (weak scaling: every rank does its own permanents)
     nsteps = args.warmup + args.steps
-    mats = [haar_block(n, seed=args.seed + 1000 * rank + s) for s in range(nsteps)]
+    from piquassoboost_gb300.replicas import shard_seeds
+
+    mats = [haar_block(n, seed=sd) for sd in shard_seeds(args.seed, rank, nsteps)]
     d_mats = [torch.from_numpy(m).to(dev) for m in mats]
     ws_bytes = int(lib.gbperm_perm_workspace_size(n, n))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     d_out = torch.zeros(2, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
-    launches_per_step = 2  # prepare + permanent kernel
+    # prepare + permanent kernel (+ the FP64 twin of the double-float kernel,
+    # which returns at once when the range check passed)
+    launches_per_step = 3 if args.mode == "fast" else 2
 
     def step(i):
         rc = lib.gbperm_perm_dev(ctypes.c_void_p(d_mats[i].data_ptr()), n, n, n, arith,
@@ -259,12 +285,10 @@ def run_ours(args, rank, world, local):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     kern_ms = [a.elapsed_time(b) for a, b in ev]
-    t_max = wall
-    if world > 1:
-        tt = torch.tensor([wall], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * args.steps / t_max
+    from piquassoboost_gb300.replicas import replica_throughput
+
+    # replicas: every rank computed its own `steps` permanents
+    value, t_max = replica_throughput(args.steps, wall, device=dev)
 
     # correctness spot check of the timed results against the FP64 kernel
     # (cheap at small n; skipped at n > 34 where one FP64 permanent costs minutes)
@@ -286,12 +310,7 @@ def run_ours(args, rank, world, local):
                              out.ctypes.data_as(ctypes.c_void_p), None, None)
         nat.check(rc)
     torch.cuda.synchronize()
-    e2e_wall = time.perf_counter() - t1
-    if world > 1:
-        tt = torch.tensor([e2e_wall], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_wall = float(tt.item())
-    e2e = world * args.steps / e2e_wall
+    e2e, _ = replica_throughput(args.steps, time.perf_counter() - t1, device=dev)
 
     if rank != 0:
         if world > 1:
@@ -301,7 +320,7 @@ def run_ours(args, rank, world, local):
     avg_ms = statistics.mean(kern_ms)
     achieved = flops_plain(n) / (avg_ms * 1e-3) / 1e12
     roof = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / peaks["fp64_tflops"], "traffic": None,
+            "frac": achieved / peaks["fp64_tflops"], "traffic": traffic_from_profile(n, args.mode),
             "kernel": ("plain_df_kernel" if args.mode == "fast" else "plain_kernel"),
             "work_per_launch": f"8 n 2^(n-1) = {flops_plain(n):.4g} algorithmic FP64-equivalent flops",
             "peak_source": "measured live by gbperm_probe_peak (DFMA probe), this run"}
@@ -344,6 +363,9 @@ def run_ours(args, rank, world, local):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload != "plain":
+        from piquassoboost_gb300 import bench_workloads
+        return bench_workloads.run(args, rank, world, local)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, world, local)

@@ -21,6 +21,7 @@ SRCS=(
   "$S/BBFGPermanentCalculator.cpp" "$S/BBFGPermanentCalculatorRepeated.cpp"
   "$S/GlynnPermanentCalculators_implementation.cpp" "$S/GlynnPermanentCalculatorSimple.cpp"
   "$S/CChinHuhPermanentCalculator.cpp" "$S/BatchedPermanentCalculator.cpp"
+  "$REF/sampling/simulation_strategies/source/samplingHelperFunctions.cpp"
   "$HERE/ref_capi.cpp"
 )
 OBJS=()
@@ -28,7 +29,8 @@ pids=()
 for s in "${SRCS[@]}"; do
   o="$OUT/$(basename "${s%.cpp}").o"
   OBJS+=("$o")
-  g++ -std=c++17 -O3 -fPIC -DBLAS=3 -w -I "$HERE/tbbshim" -I "$C" -I "$S" -c "$s" -o "$o" &
+  g++ -std=c++17 -O3 -fPIC -DBLAS=3 -w -I "$HERE/tbbshim" -I "$C" -I "$S" \
+      -I "$REF/sampling/simulation_strategies/source" -c "$s" -o "$o" &
   pids+=($!)
 done
 for p in "${pids[@]}"; do wait "$p"; done

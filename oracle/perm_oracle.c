@@ -554,3 +554,61 @@ int orc_adapt_interferometer_multiplied(const double* U, int64_t m, int64_t ld,
         }
     return 0;
 }
+
+/* --------------------------------------------------------- compute_pmf */
+/* compute_pmf, sampling/simulation_strategies/source/samplingHelperFunctions
+ * .cpp:78-342 (its CPU branch): for every occupied input mode idx, the
+ * repeated permanent of the sample (rows) against the input with one photon
+ * removed from idx (columns), then
+ *   pmf[mdx] ~ | sum_idx input[idx] * addend[idx] * U[mdx][idx] |^2,
+ * normalised to sum 1.  addends (2m doubles, may be NULL) receives the
+ * permanents, zero for unoccupied modes. */
+int orc_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample, const int64_t* current_input,
+                    int prec, int nthreads, double* pmf, double* addends) {
+    double* add = (double*)calloc((size_t)(2 * m), sizeof(double));
+    int64_t* inp = (int64_t*)malloc(sizeof(int64_t) * (size_t)m);
+    int64_t* fin = (int64_t*)malloc(sizeof(int64_t) * (size_t)m);
+    int64_t* fout = (int64_t*)malloc(sizeof(int64_t) * (size_t)m);
+    double* sub = (double*)malloc(sizeof(double) * 2 * (size_t)(m * m));
+    int rc = 0;
+    for (int64_t idx = 0; idx < m && rc == 0; ++idx) {
+        if (current_input[idx] <= 0) continue;
+        for (int64_t j = 0; j < m; ++j) inp[j] = current_input[j];
+        inp[idx]--;
+        int64_t nr = 0, nc = 0;
+        orc_adapt_interferometer(U, m, ld, inp, sample, sub, &nr, &nc);
+        int64_t a = 0, b = 0;
+        for (int64_t j = 0; j < m; ++j) {
+            if (inp[j] > 0) fin[a++] = inp[j];
+            if (sample[j] > 0) fout[b++] = sample[j];
+        }
+        double o4[4];
+        rc = orc_bbfg_repeated(sub, nr, nc, nc > 0 ? nc : 1, fin, a, fout, b, prec, nthreads, o4);
+        add[2 * idx] = o4[0];
+        add[2 * idx + 1] = o4[1];
+    }
+    if (rc == 0) {
+        double total = 0.0;
+        for (int64_t mdx = 0; mdx < m; ++mdx) {
+            double re = 0.0, im = 0.0;
+            for (int64_t idx = 0; idx < m; ++idx) {
+                if (current_input[idx] == 0) continue;
+                double ur = U[2 * (mdx * ld + idx)], ui = U[2 * (mdx * ld + idx) + 1];
+                double pr = (double)current_input[idx] * add[2 * idx];
+                double pi = (double)current_input[idx] * add[2 * idx + 1];
+                re += pr * ur - pi * ui;
+                im += pr * ui + pi * ur;
+            }
+            pmf[mdx] = re * re + im * im;
+            total += pmf[mdx];
+        }
+        for (int64_t mdx = 0; mdx < m; ++mdx) pmf[mdx] /= total;
+        if (addends) memcpy(addends, add, sizeof(double) * 2 * (size_t)m);
+    }
+    free(add);
+    free(inp);
+    free(fin);
+    free(fout);
+    free(sub);
+    return rc;
+}

@@ -24,6 +24,7 @@
 #include "GlynnPermanentCalculator.h"
 #include "GlynnPermanentCalculatorRepeated.h"
 #include "GlynnPermanentCalculatorSimple.h"
+#include "samplingHelperFunctions.h"
 
 static thread_local std::string g_err;
 
@@ -109,6 +110,27 @@ int ref_adapt_interferometer_multiplied(const double* U, int64_t m, const int64_
     pic::matrix r = pic::adaptInterferometerGlynnMultiplied(u, &in, &outs);
     std::memcpy(out, r.get_data(), r.rows * r.cols * sizeof(pic::Complex16));
     return 0;
+}
+
+// compute_pmf (sampling/simulation_strategies/source/samplingHelperFunctions
+// .cpp:78-342): the probability of the next output mode given the sample so
+// far and the current input.  pmf must hold m doubles.
+int ref_compute_pmf(const double* U, int64_t m, const int64_t* sample, const int64_t* current_input, double* pmf) {
+    try {
+        pic::matrix u((pic::Complex16*)U, (size_t)m, (size_t)m);
+        pic::PicState_int64 smp((int64_t*)sample, (size_t)m);
+        pic::PicState_int64 inp((int64_t*)current_input, (size_t)m);
+        int64_t ns = 0, ni = 0;
+        for (int64_t i = 0; i < m; ++i) { ns += sample[i]; ni += current_input[i]; }
+        smp.number_of_photons = ns;
+        inp.number_of_photons = ni;
+        pic::matrix_real r = pic::compute_pmf(u, smp, inp);
+        std::memcpy(pmf, r.get_data(), (size_t)m * sizeof(double));
+        return 0;
+    } catch (std::string& e) {
+        g_err = e;
+        return 2;
+    }
 }
 
 }  // extern "C"

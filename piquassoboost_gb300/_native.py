@@ -97,7 +97,9 @@ _lock = threading.Lock()
 
 
 def library_path() -> str:
-    return LIB_PATH
+    """libgbperm.so in the package, or the file named by GBPERM_LIB (a
+    differently configured build of the same sources)."""
+    return os.environ.get("GBPERM_LIB", LIB_PATH)
 
 
 def load(build_if_missing: bool = False):
@@ -106,16 +108,17 @@ def load(build_if_missing: bool = False):
     with _lock:
         if _lib is not None:
             return _lib
-        if not os.path.exists(LIB_PATH):
-            if build_if_missing:
+        path = library_path()
+        if not os.path.exists(path):
+            if build_if_missing and path == LIB_PATH:
                 from .build import build_native
 
                 build_native()
             else:
                 raise RuntimeError(
-                    f"libgbperm.so not found at {LIB_PATH}; build it with "
+                    f"libgbperm.so not found at {path}; build it with "
                     "`python -m piquassoboost_gb300.build` (the GPU path has no CPU fallback)")
-        lib = ctypes.CDLL(LIB_PATH)
+        lib = ctypes.CDLL(path)
         for name, res, args in _SIGNATURES:
             fn = getattr(lib, name)
             fn.restype = res

@@ -371,9 +371,9 @@ void launch_t(const BArgs& a, int grid, cudaStream_t st) {
 }
 
 // shapes: (CPL, GROUP, DF)
-#define GBPERM_BATCH_SHAPES(X) \
-    X(16, 1, false) X(32, 1, false) X(48, 1, false) X(64, 1, false) \
-    X(8, 2, true) X(12, 2, true) X(16, 2, true) X(4, 4, true) X(6, 4, true) X(8, 4, true) X(10, 4, true) \
+#define GBPERM_BATCH_SHAPES(X)                                                                          \
+    X(16, 1, false) X(32, 1, false) X(48, 1, false) X(64, 1, false) X(4, 2, true) X(6, 2, true) X(8, 2, true) \
+    X(10, 2, true) X(12, 2, true) X(14, 2, true) X(16, 2, true) X(20, 2, true) X(24, 2, true) X(8, 4, true)  \
     X(12, 4, true)
 
 int batch_bps(int cpl, int grp, bool df) {
@@ -398,7 +398,8 @@ cudaError_t batch_launch(const BArgs& a, int cpl, int grp, bool df, int grid, cu
 // smallest compiled shape covering `cols` columns for the arithmetic
 void batch_shape(int cols, bool df, int group, int* cpl, int* grp) {
     static const int s64[][2] = {{16, 1}, {32, 1}, {48, 1}, {64, 1}};
-    static const int sdf[][2] = {{8, 2}, {12, 2}, {16, 2}, {4, 4}, {6, 4}, {8, 4}, {10, 4}, {12, 4}};
+    static const int sdf[][2] = {{4, 2},  {6, 2},  {8, 2},  {10, 2}, {12, 2},
+                                 {14, 2}, {16, 2}, {20, 2}, {24, 2}, {8, 4}, {12, 4}};
     if (!df) {
         for (auto& s : s64)
             if (s[0] >= cols) {
@@ -410,7 +411,9 @@ void batch_shape(int cols, bool df, int group, int* cpl, int* grp) {
         *grp = 1;
         return;
     }
-    int want = group > 0 ? group : (cols <= 16 ? 2 : 4);
+    // lane pairs: the widest instances dominate a batch's work, and GROUP = 2
+    // with an exact column fit is the fastest plain shape measured on GB300
+    int want = group > 0 ? group : 2;
     int best = -1;
     const int n = (int)(sizeof(sdf) / sizeof(sdf[0]));
     for (int i = 0; i < n; ++i)

@@ -19,6 +19,10 @@ namespace gbperm {
 namespace {
 
 constexpr int kThreads = 128;
+#ifndef GBPERM_DF_CHAINS
+#define GBPERM_DF_CHAINS 2
+#endif
+constexpr int kChains = GBPERM_DF_CHAINS;  // independent product chains per lane
 
 __device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
     return cf{__shfl_xor_sync(0xffffffffu, v.rh, m), __shfl_xor_sync(0xffffffffu, v.rl, m),
@@ -119,22 +123,27 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
                     brh = brl = bih = bil = 0.f;
                 }
             }
-            // partial product of this lane's columns (two chains for ILP);
-            // padded columns hold zero sums and are skipped
-            cf pa{1.f, 0.f, 0.f, 0.f}, pb{1.f, 0.f, 0.f, 0.f};
+            // partial product of this lane's columns in kChains independent
+            // chains (ILP); padded columns hold zero sums and are skipped
+            cf ch[kChains];
+#pragma unroll
+            for (int t = 0; t < kChains; ++t) ch[t] = cf{1.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
                 if (j0 + c < cols) {
                     cf x;
                     fix_to_df_magic(cre[c], cv, x.rh, x.rl);
                     fix_to_df_magic(cim[c], cv, x.ih, x.il);
-                    if (c == 0) pa = x;
-                    else if (c == 1) pb = x;
-                    else if (c & 1) pb = cf_mul(pb, x);
-                    else pa = cf_mul(pa, x);
+                    if (c < kChains) ch[c] = x;
+                    else ch[c % kChains] = cf_mul(ch[c % kChains], x);
                 }
             }
-            if (CPL > 1) pa = cf_mul(pa, pb);
+#pragma unroll
+            for (int w = 1; w < kChains; w <<= 1)
+#pragma unroll
+                for (int t = 0; t + w < kChains; t += 2 * w)
+                    if (t + w < CPL) ch[t] = cf_mul(ch[t], ch[t + w]);
+            cf pa = ch[0];
 #pragma unroll
             for (int m = 1; m < GROUP; m <<= 1) pa = cf_mul(pa, shfl_xor_cf(pa, m));
             if (leader && active) {

@@ -153,6 +153,17 @@ class Ref:
             raise RuntimeError(self.lib.ref_last_error())
         return complex(out[0], out[1])
 
+    def compute_pmf(self, U, sample, current_input):
+        U = np.ascontiguousarray(U, dtype=np.complex128)
+        s = np.ascontiguousarray(sample, dtype=np.int64)
+        c = np.ascontiguousarray(current_input, dtype=np.int64)
+        out = np.zeros(U.shape[0])
+        rc = self.lib.ref_compute_pmf(U.ctypes.data_as(_P), _I(U.shape[0]), s.ctypes.data_as(_P),
+                                      c.ctypes.data_as(_P), out.ctypes.data_as(_P))
+        if rc:
+            raise RuntimeError(self.lib.ref_last_error())
+        return out
+
     def adapt(self, U, cin, rout):
         U = np.ascontiguousarray(U, dtype=np.complex128)
         cin = np.ascontiguousarray(cin, dtype=np.int64)
@@ -168,7 +179,7 @@ class Ref:
 
 
 def reference_calculators(ref):
-    cases = {"plain": [], "repeated": [], "adapt": []}
+    cases = {"plain": [], "repeated": [], "adapt": [], "pmf": []}
     rng = np.random.default_rng(20240611)
     # plain: Gaussian and Haar blocks, square and rectangular
     shapes = [(n, n) for n in range(1, 15)] + [(2, 3), (3, 5), (4, 3), (5, 3), (1, 4), (3, 1), (2, 1),
@@ -217,6 +228,15 @@ def reference_calculators(ref):
         cases["adapt"].append({"m": m, "matrix": _cplx_list(U), "input_state": cin.tolist(),
                                "output_state": rout.tolist(), "shape": list(sub.shape),
                                "result": _cplx_list(sub)})
+    # compute_pmf: a Clifford-Clifford layer (k input photons, k-1 sampled)
+    for t in range(12):
+        m = int(rng.integers(4, 16))
+        U = haar_unitary(m, 6000 + t)
+        k = int(rng.integers(1, 9))
+        inp = rng.multinomial(k, np.ones(m) / m).astype(np.int64)
+        smp = rng.multinomial(k - 1, np.ones(m) / m).astype(np.int64)
+        cases["pmf"].append({"m": m, "matrix": _cplx_list(U), "sample": smp.tolist(), "current_input": inp.tolist(),
+                             "pmf": [float(x) for x in ref.compute_pmf(U, smp, inp)]})
     return cases
 
 

@@ -121,3 +121,19 @@ def rel_err(val, ref_dd):
     hi = complex(ref_dd[0], ref_dd[1]); lo = complex(ref_dd[2], ref_dd[3])
     d = (complex(val) - hi) - lo
     return abs(d) / abs(hi)
+
+
+def compute_pmf(U, sample, current_input, prec=0, threads=0):
+    """(pmf, addends) of the reference's compute_pmf restated in the oracle."""
+    u = _mat(U)
+    m = u.shape[0]
+    s = np.ascontiguousarray(sample, dtype=np.int64)
+    c = np.ascontiguousarray(current_input, dtype=np.int64)
+    pmf = np.zeros(m)
+    add = np.zeros(m, dtype=np.complex128)
+    rc = lib().orc_compute_pmf(u.ctypes.data_as(_P), _I(m), _I(m), s.ctypes.data_as(_P), c.ctypes.data_as(_P),
+                               ctypes.c_int(prec), ctypes.c_int(threads), pmf.ctypes.data_as(_P),
+                               add.ctypes.data_as(_P))
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return pmf, add

@@ -125,3 +125,13 @@ def test_oracle_all_ones_factorial():
     for n in range(1, 13):
         v, _ = orc.bbfg(np.ones((n, n)), prec=1)
         assert abs(v - math.factorial(n)) <= 1e-12 * math.factorial(n)
+
+
+@pytest.mark.parametrize("i", range(len(CALC.get("pmf", []))))
+def test_oracle_compute_pmf_vs_reference_build(i):
+    # samplingHelperFunctions.cpp:78-342
+    case = CALC["pmf"][i]
+    m = case["m"]
+    U = np.array([complex(r, im) for r, im in case["matrix"]]).reshape(m, m)
+    pmf, _ = orc.compute_pmf(U, case["sample"], case["current_input"], prec=1)
+    assert np.allclose(pmf, case["pmf"], rtol=1e-10, atol=1e-14)
