@@ -109,6 +109,49 @@ int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld
                          int64_t nrow, int arith, double* out, double* out_dd,
                          gbperm_stats* stats);
 
+/* ------------------------------------------------- batched permanents */
+/* Many plain permanents of uneven sizes in one persistent launch (a CUDA
+ * graph per plan).  Replaces the list branch of the plain wrapper
+ * (piquassoboost/sampling/GlynnPermanentCalculator_Wrapper.hpp:204-294) and
+ * BatchednPermanentCalculator::calculate (BatchedPermanentCalculator.cpp:
+ * 109-296).  Instance i is a rows[i] x cols[i] complex128 matrix, dense
+ * (ld = cols[i]); the instances are packed back to back in index order.
+ * A plan holds the instance sizes, the work list and the device buffers; it
+ * belongs to the device current at creation.  out: 2 * count doubles. */
+typedef struct gbperm_batch_plan gbperm_batch_plan;
+int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t count, int arith,
+                             gbperm_batch_plan** out_plan);
+void gbperm_batch_plan_destroy(gbperm_batch_plan* plan);
+int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double* out, gbperm_stats* stats);
+/* Device-pointer form: d_packed and d_out on the device, enqueued on
+ * stream; slots of trivial instances (an empty side, or rows >= cols + 2)
+ * are not written. */
+int gbperm_batch_plan_run_dev(gbperm_batch_plan* plan, const void* d_packed, void* d_out, void* stream);
+/* log2 of the Gray steps in one work item (the load-balancing grain);
+ * setting it rebuilds the work list and the graph. */
+int gbperm_batch_plan_set_item_log2(gbperm_batch_plan* plan, int64_t item_log2);
+int64_t gbperm_batch_plan_get_item_log2(gbperm_batch_plan* plan);
+/* One-shot: create, run, destroy. */
+int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t* cols, int64_t count, int arith,
+                        double* out, gbperm_stats* stats);
+
+/* ------------------------------------------ boson-sampling pmf layer */
+/* One probability layer of the generalized Clifford & Clifford sampler.
+ * Replaces compute_pmf (piquassoboost/sampling/simulation_strategies/source/
+ * samplingHelperFunctions.cpp:78-342).  U: m x m complex128 interferometer
+ * (leading dimension ld); sample: m output occupations (the photons placed so
+ * far); current_input: m input occupations holding exactly one photon more.
+ * pmf (m doubles) receives, normalised to sum 1,
+ *   pmf[k] ~ | sum_l current_input[l] * perm_l * U[k][l] |^2
+ * with perm_l the repeated permanent of the sample rows against the input
+ * with one photon removed from mode l; addends (NULL or 2 m doubles)
+ * receives the perm_l as complex128 (0 for empty input modes).  All perm_l
+ * come from one Gray-code sweep over the sample.  Up to 64 sample photons
+ * and 64 occupied input modes; a photon-count mismatch ->
+ * GBPERM_ERR_STATE_SUM. */
+int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample, const int64_t* current_input,
+                       double* pmf, double* addends, gbperm_stats* stats);
+
 /* ----------------------------------------------- permanent + gradient */
 /* Permanent of an n x n matrix and its full gradient G[k][l] = dperm/da_kl
  * (= perm of A without row k and column l) in one Gray-code sweep, for

@@ -90,6 +90,7 @@ _SIGNATURES = [
     ("gbperm_perm_noalloc_scratch_bytes", ctypes.c_size_t, []),
     ("gbperm_perm_repeated", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
+    ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P, _P]),
 ]
 
 _lib = None
@@ -274,6 +275,28 @@ def perm_batched(matrices, mode="fp64", stats: Stats | None = None):
         return plan.run(mats, stats=stats)
     finally:
         plan.close()
+
+
+def compute_pmf(interferometer, sample, current_input, stats: Stats | None = None):
+    """One probability layer of the Clifford & Clifford sampler on the GPU
+    (gbperm_compute_pmf): returns (pmf, addends), pmf normalised to sum 1 over
+    the m output modes and addends[l] the permanent with one photon removed
+    from input mode l (0 where the input mode is empty)."""
+    lib = load()
+    u = as_matrix(interferometer)
+    m = u.shape[0]
+    if u.shape[1] != m:
+        raise ValueError("compute_pmf: square interferometer required")
+    s = as_state(sample)
+    c = as_state(current_input)
+    if len(s) != m or len(c) != m:
+        raise ValueError("compute_pmf: states must have one entry per mode")
+    pmf = np.zeros(m)
+    add = np.zeros(m, dtype=np.complex128)
+    check(lib.gbperm_compute_pmf(u.ctypes.data_as(_P), m, m, s.ctypes.data_as(_P), c.ctypes.data_as(_P),
+                                 pmf.ctypes.data_as(_P), add.ctypes.data_as(_P),
+                                 ctypes.byref(stats) if stats is not None else None))
+    return pmf, add
 
 
 def probe_peak(kind: str) -> float:

@@ -156,6 +156,7 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     if (ws_bytes < need) return fail(GBPERM_ERR_ARG, "gbperm: workspace too small");
     char* base = static_cast<char*>(ws);
     PrepArgs pa;
+    pa.col_e_out = nullptr;
     pa.A = dA;
     pa.ld = ld;
     pa.rows = rows;

@@ -74,6 +74,7 @@ struct RepHost {
     double steps = 0.0, flops = 0.0;
     std::vector<double> M;        // R x C complex128 (interleaved), digit rows first
     std::vector<int> rcoef, D, cpow;
+    std::vector<int> col_src;     // original column index of each column of M
     std::vector<double> wlow;
     std::vector<unsigned char> seq;
 };
@@ -82,7 +83,8 @@ struct RepWs {
 };
 int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
                   int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
-                  bool* is_trivial);
+                  bool* is_trivial, bool allow_transpose, int col_surplus);
+const std::vector<double>& binom_table();
 size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w);
 
 }  // namespace gbperm

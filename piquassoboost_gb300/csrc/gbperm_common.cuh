@@ -99,26 +99,34 @@ __device__ __forceinline__ cd cmul(cd a, cd b) {
 // exact error of the leading product (FMA) and the first-order cross terms;
 // the pair is not renormalised after a multiply (|l| stays below ~2^-22 |z|),
 // which keeps the error of a complex product near 2^-46 |z|.
+//
+// The error-free steps below only hold with every add and multiply rounded
+// on its own: a multiply that the compiler fused into a following add (its
+// default FMA contraction) would already carry the product's exact value,
+// which the separately computed error term then adds a second time.  The
+// primitives therefore use __fadd_rn / __fsub_rn / __fmul_rn, which are
+// never contracted; the FMAs they need are written out as fmaf.
 struct cf {  // complex double-float
     float rh, rl, ih, il;
 };
 
+// Knuth's TwoSum: s + e == a + b exactly.
 __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 __device__ __forceinline__ cf cf_mul(const cf& x, const cf& y) {
     cf z;
     // real part: xr*yr - xi*yi
-    float p1 = x.rh * y.rh;
-    float e1 = fmaf(x.rh, y.rh, -p1);
-    float p2 = x.ih * y.ih;
-    float e2 = fmaf(x.ih, y.ih, -p2);
+    const float p1 = __fmul_rn(x.rh, y.rh);
+    const float e1 = fmaf(x.rh, y.rh, -p1);
+    const float p2 = __fmul_rn(x.ih, y.ih);
+    const float e2 = fmaf(x.ih, y.ih, -p2);
     float s, t;
     two_sum_f(p1, -p2, s, t);
-    float u = (e1 - e2) + t;
+    float u = __fadd_rn(__fsub_rn(e1, e2), t);
     u = fmaf(x.rh, y.rl, u);
     u = fmaf(x.rl, y.rh, u);
     u = fmaf(-x.ih, y.il, u);
@@ -126,13 +134,13 @@ __device__ __forceinline__ cf cf_mul(const cf& x, const cf& y) {
     z.rh = s;
     z.rl = u;
     // imaginary part: xr*yi + xi*yr
-    float q1 = x.rh * y.ih;
-    float f1 = fmaf(x.rh, y.ih, -q1);
-    float q2 = x.ih * y.rh;
-    float f2 = fmaf(x.ih, y.rh, -q2);
+    const float q1 = __fmul_rn(x.rh, y.ih);
+    const float f1 = fmaf(x.rh, y.ih, -q1);
+    const float q2 = __fmul_rn(x.ih, y.rh);
+    const float f2 = fmaf(x.ih, y.rh, -q2);
     float s2, t2;
     two_sum_f(q1, q2, s2, t2);
-    float v = (f1 + f2) + t2;
+    float v = __fadd_rn(__fadd_rn(f1, f2), t2);
     v = fmaf(x.rh, y.il, v);
     v = fmaf(x.rl, y.ih, v);
     v = fmaf(x.ih, y.rl, v);
@@ -151,12 +159,12 @@ __device__ __forceinline__ void fix_to_df(long long x, float s2, float s1, float
     const int c2 = (int)(x >> 42);
     const int c1 = (int)((x >> 21) & 0x1FFFFFll);
     const int c0 = (int)(x & 0x1FFFFFll);
-    const float f2 = __int2float_rn(c2) * s2;
-    const float f1 = __int2float_rn(c1) * s1;
-    const float f0 = __int2float_rn(c0) * s0;
-    h = f2 + f1;
-    const float e = f1 - (h - f2);
-    l = e + f0;
+    const float f2 = __fmul_rn(__int2float_rn(c2), s2);
+    const float f1 = __fmul_rn(__int2float_rn(c1), s1);
+    const float f0 = __fmul_rn(__int2float_rn(c0), s0);
+    h = __fadd_rn(f2, f1);
+    const float e = __fsub_rn(f1, __fsub_rn(h, f2));
+    l = __fadd_rn(e, f0);
 }
 
 // int64 fixed point -> float pair without conversion instructions.  The three
@@ -198,21 +206,21 @@ __device__ __forceinline__ void fix_to_df_magic(long long x, const DfConv& k, fl
     const int c2 = ((int)hi >> 10) + (1 << 22);                      // bits 42..63, offset
     const unsigned int c1 = __funnelshift_r(lo, hi, 21) & 0x1FFFFFu;  // bits 21..41
     const unsigned int c0 = lo & 0x1FFFFFu;                           // bits 0..20
-    const float f2 = __uint_as_float(k.m2 + (unsigned int)c2) - k.o2;
-    const float f1 = __uint_as_float(k.m1 | c1) - k.o1;
-    const float f0 = __uint_as_float(k.m0 | c0) - k.o0;
-    h = f2 + f1;
-    const float e = f1 - (h - f2);
-    l = e + f0;
+    const float f2 = __fsub_rn(__uint_as_float(k.m2 + (unsigned int)c2), k.o2);
+    const float f1 = __fsub_rn(__uint_as_float(k.m1 | c1), k.o1);
+    const float f0 = __fsub_rn(__uint_as_float(k.m0 | c0), k.o0);
+    h = __fadd_rn(f2, f1);
+    const float e = __fsub_rn(f1, __fsub_rn(h, f2));
+    l = __fadd_rn(e, f0);
 }
 
 // df accumulator: a += (h, l), renormalised
 __device__ __forceinline__ void df_acc(float& ah, float& al, float h, float l) {
     float s, e;
     two_sum_f(ah, h, s, e);
-    e += al + l;
-    ah = s + e;
-    al = e - (ah - s);
+    e = __fadd_rn(e, __fadd_rn(al, l));
+    ah = __fadd_rn(s, e);
+    al = __fsub_rn(e, __fsub_rn(ah, s));
 }
 
 }  // namespace gbperm

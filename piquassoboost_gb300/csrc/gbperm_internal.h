@@ -27,6 +27,7 @@ struct PrepArgs {
     longlong2* a1;           // rows x cols
     longlong2* a2;           // rows x cols
     int* exp_out;            // 1 int
+    int* col_e_out;          // optional: per-column scaling exponents e_j (cols ints)
     int df;                  // 1: also decide the double-float range boost
     int* df_info;            // {o, ok}: boost and range-check result (ok = 0:
                              // the kernel must use the FP64 product)

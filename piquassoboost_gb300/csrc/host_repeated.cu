@@ -23,8 +23,6 @@
 
 namespace gbperm {
 
-namespace {
-
 const std::vector<double>& binom_table() {
     static std::vector<double> t;
     static std::once_flag once;
@@ -42,11 +40,9 @@ const std::vector<double>& binom_table() {
     return t;
 }
 
-}  // namespace
-
 int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
                   int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
-                  bool* is_trivial) {
+                  bool* is_trivial, bool allow_transpose, int col_surplus) {
     *is_trivial = false;
     if (rows == 0) {
         trivial[0] = 1.0;
@@ -67,7 +63,7 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
         if (col_mult[j] < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: negative occupation");
         sc += col_mult[j];
     }
-    if (sr != sc)
+    if (sr + col_surplus != sc)
         return fail(GBPERM_ERR_STATE_SUM,
                     "BBFGPermanentCalculatorRepeated_Tasks::calculate:  Number of input and output states should be equal");
     if (sr == 0 || cols == 0) {
@@ -98,7 +94,7 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
         return t * (long double)mn / (long double)(mn + 1);
     };
     long double t_rows = gray_len(ri, row_mult), t_cols = gray_len(ci, col_mult);
-    bool transpose = t_cols < t_rows;
+    bool transpose = allow_transpose && t_cols < t_rows;
     h->transpose = transpose;
     const std::vector<int>& gi = transpose ? ci : ri;   // Gray-code side (rows of M)
     const std::vector<int>& pj = transpose ? ri : ci;   // product side (columns of M)
@@ -180,7 +176,11 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
         if (r < h->nd) h->D.push_back(order[r].D);
     }
     h->cpow.clear();
-    for (int c = 0; c < C; ++c) h->cpow.push_back((int)pm[pj[c]]);
+    h->col_src.clear();
+    for (int c = 0; c < C; ++c) {
+        h->cpow.push_back((int)pm[pj[c]]);
+        h->col_src.push_back(pj[c]);
+    }
     // low-digit tables
     h->wlow.assign(P, 1.0);
     h->seq.assign(P, 0);
@@ -252,7 +252,7 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     RepHost h;
     double triv[2];
     bool is_triv = false;
-    int rc = repeated_plan(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, &h, triv, &is_triv);
+    int rc = repeated_plan(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, &h, triv, &is_triv, true, 0);
     if (rc) return rc;
     if (is_triv) {
         out[0] = triv[0];
@@ -318,6 +318,7 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: upload");
     const int* d_ints = reinterpret_cast<const int*>(base + w.ints);
     PrepArgs pa;
+    pa.col_e_out = nullptr;
     pa.A = reinterpret_cast<const double2*>(base + w.M);
     pa.ld = h.C;
     pa.rows = h.R;

@@ -15,12 +15,23 @@
 // instead of all n.  Q is folded into G and restarted every kChunk steps to
 // keep the running sums small (bounded rounding growth).
 //
+// Per step and lane (CPL columns): prefix products of the lane's columns
+// (which also give its partial product), the other three lanes' partials
+// (shuffles), then a suffix chain seeded with the signed exclusive product,
+// so W_c = prefix_c x suffix_c: 3 CPL - 1 double-float complex products for
+// the CPL gradient columns, one more for the permanent term on the group's
+// first lane.  Running sums are added
+// with an exact two-sum of the high parts and renormalised every 8 steps.
+//
 // Layout: GROUP = 4 lanes share a Gray walk, lane g owns columns
 // [g*CPL, (g+1)*CPL); the 8 groups of a warp walk 8 aligned ranges in
 // lockstep.  The per-step row update of G is a reduce-scatter over the 8
 // groups (lane (g, grp) ends with column g*CPL + grp), added into the warp's
-// own n x n double-float G tile in shared memory.  Warp tiles are written to
-// global memory and summed in a fixed order by a finalize kernel.
+// own n x n double-float G tile in shared memory.  The flip sign is the same
+// for all 8 walks except at the middle step of a walk, so it is applied after
+// the reduction.  Warp tiles are written to global memory and summed in a
+// fixed order by two finalize kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -34,7 +45,8 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kGroup = 4;
 constexpr int kGroups = 32 / kGroup;  // walks per warp
-constexpr int kChunk = 256;           // steps between folds of Q into G
+constexpr int kChunk = 1024;          // steps between folds of Q into G
+constexpr int kFinWarps = 64;         // warp tiles per partial of the first finalize stage
 
 __device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
     return cf{__shfl_xor_sync(0xffffffffu, v.rh, m), __shfl_xor_sync(0xffffffffu, v.rl, m),
@@ -46,10 +58,28 @@ __device__ __forceinline__ cf shfl_cf(const cf& v, int src) {
               __shfl_sync(0xffffffffu, v.ih, src), __shfl_sync(0xffffffffu, v.il, src)};
 }
 
-__device__ __forceinline__ cf cf_add(const cf& a, const cf& b) {
+// a += b without renormalisation: exact two-sum of the high parts, the low
+// parts and the rounding error collected in the low word.  Over m such adds
+// the low word stays below ~m 2^-24 of the running magnitude, so a
+// renormalisation every few adds keeps the pair accurate to ~2^-44.
+__device__ __forceinline__ void df_add_lazy(float& ah, float& al, float bh, float bl) {
+    float s, e;
+    two_sum_f(ah, bh, s, e);
+    ah = s;
+    al = __fadd_rn(al, __fadd_rn(bl, e));
+}
+
+__device__ __forceinline__ void df_renorm(float& h, float& l) {
+    float s, e;
+    two_sum_f(h, l, s, e);
+    h = s;
+    l = e;
+}
+
+__device__ __forceinline__ cf cf_add_lazy(const cf& a, const cf& b) {
     cf r = a;
-    df_acc(r.rh, r.rl, b.rh, b.rl);
-    df_acc(r.ih, r.il, b.ih, b.il);
+    df_add_lazy(r.rh, r.rl, b.rh, b.rl);
+    df_add_lazy(r.ih, r.il, b.ih, b.il);
     return r;
 }
 
@@ -63,7 +93,7 @@ struct GradArgs {
     const longlong2* a2;
     int n;
     int seg_log2;              // each walk covers 2^seg_log2 Gray steps
-    unsigned long long nseg;   // walks (multiple of kGroups, or smaller total)
+    unsigned long long nseg;   // walks
     const int* df_info;        // {boost, ok}
     float4* warp_g;            // per warp: n x n complex double-float tiles (re_h, re_l, im_h, im_l)
     float4* warp_p;            // per warp: permanent partial
@@ -73,12 +103,10 @@ struct GradArgs {
 // equal g): afterwards lane (g, grp) holds, in v[0], the sum over groups of
 // column g*CPL + (grp % CPL) (CPL <= kGroups).  The ownership pattern is
 // fixed: at each halving stage with mask m, the lane with (grp & m) keeps
-// the upper half.
+// the upper half.  The sums are lazily normalised pairs.
 template <int CPL>
 __device__ __forceinline__ cf reduce_scatter(cf (&v)[CPL], int grp) {
-    int lanes_per_col = kGroups;  // groups still sharing each column slot
     int width = CPL;
-    int base = 0;                 // first column index this lane still holds
 #pragma unroll
     for (int m = kGroups / 2; m >= 1; m >>= 1) {
         if (width > 1) {
@@ -91,18 +119,15 @@ __device__ __forceinline__ cf reduce_scatter(cf (&v)[CPL], int grp) {
                     cf send = upper ? v[c] : v[c + half];
                     cf recv = shfl_xor_cf(send, m * kGroup);
                     cf keep = upper ? v[c + half] : v[c];
-                    v[c] = cf_add(keep, recv);
+                    v[c] = cf_add_lazy(keep, recv);
                 }
             }
-            if (upper) base += half;
             width = half;
         } else {
             cf recv = shfl_xor_cf(v[0], m * kGroup);
-            v[0] = cf_add(v[0], recv);
+            v[0] = cf_add_lazy(v[0], recv);
         }
-        lanes_per_col >>= 1;
     }
-    (void)base;
     return v[0];
 }
 
@@ -145,30 +170,34 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
     const DfConv cv = make_dfconv(p.df_info[0]);
     const int my_col = scatter_col<CPL>(g, grp);
     // with CPL < kGroups the last stages are all-reduces: one lane per column writes
-    const bool writer = (grp & (kGroups / CPL - 1)) == 0;
-    const unsigned long long L = 1ull << p.seg_log2;
+    const bool writer = (grp & (kGroups / CPL - 1)) == 0 && my_col < n;
+    const int L = p.seg_log2;
+    const unsigned long long Lsteps = 1ull << L;
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (kThreads / 32);
     const unsigned long long gwarp = (unsigned long long)blockIdx.x * (kThreads / 32) + warp;
+    const int lbase = lane - g;
     long long cre[CPL], cim[CPL];
     cf Q[CPL];
     float prh = 0.f, prl = 0.f, pih = 0.f, pil = 0.f;  // permanent partial (group leader)
 
+    auto g_add = [&](int r, const cf& s) {
+        if (writer) {
+            float4 gg = G[r * NP + my_col];
+            df_acc(gg.x, gg.y, s.rh, s.rl);
+            df_acc(gg.z, gg.w, s.ih, s.il);
+            G[r * NP + my_col] = gg;
+        }
+    };
     // fold Q into every row of G: G[r] += delta_r * Q (the end term), then Q = 0
-    auto fold_all = [&](unsigned long long idx, bool active) {
+    auto fold_all = [&](unsigned long long idx) {
         const unsigned long long gray = idx ^ (idx >> 1);
         for (int r = 0; r < n; ++r) {
             // delta_r = -1 when bit (n-1-r) of the Gray code is set (row 0: +1)
             const bool neg = r > 0 && ((gray >> (n - 1 - r)) & 1ull);
             cf v[CPL];
 #pragma unroll
-            for (int c = 0; c < CPL; ++c) v[c] = active ? cf_scale_sign(Q[c], neg ? 0x80000000u : 0u) : cf{0.f, 0.f, 0.f, 0.f};
-            cf s = reduce_scatter<CPL>(v, grp);
-            if (writer && my_col < n) {
-                float4 gg = G[r * NP + my_col];
-                df_acc(gg.x, gg.y, s.rh, s.rl);
-                df_acc(gg.z, gg.w, s.ih, s.il);
-                G[r * NP + my_col] = gg;
-            }
+            for (int c = 0; c < CPL; ++c) v[c] = cf_scale_sign(Q[c], neg ? 0x80000000u : 0u);
+            g_add(r, reduce_scatter<CPL>(v, grp));
         }
 #pragma unroll
         for (int c = 0; c < CPL; ++c) Q[c] = cf{0.f, 0.f, 0.f, 0.f};
@@ -177,7 +206,7 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
     for (unsigned long long wb = gwarp * kGroups; wb < p.nseg; wb += warps_total * kGroups) {
         const unsigned long long s_raw = wb + grp;
         const bool active = s_raw < p.nseg;
-        const unsigned long long i0 = (active ? s_raw : 0ull) << p.seg_log2;
+        const unsigned long long i0 = (active ? s_raw : 0ull) << L;
         const unsigned long long g0 = i0 ^ (i0 >> 1);
 #pragma unroll
         for (int c = 0; c < CPL; ++c) {
@@ -196,35 +225,45 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
             }
         }
         unsigned int sbit = (unsigned int)(__popcll(g0) & 1) << 31;
-        for (unsigned long long k = 0; k < L; ++k) {
+        // inactive walks (past the end of the range) carry weight 0
+        const float wgt = active ? 1.f : 0.f;
+        for (unsigned long long k = 0; k < Lsteps; ++k) {
             const unsigned long long idx = i0 + k;
             if (k != 0) {
-                const int b = __ffsll((long long)k) - 1;          // warp-uniform
-                const int r = n - 1 - b;                            // the row that flips
+                const int b = __ffsll((long long)k) - 1;                  // warp-uniform
+                const int r = n - 1 - b;                                    // the row that flips
                 const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;  // new delta_r = -1
                 if ((k % kChunk) == 0) {
                     // chunk boundary: end term at idx-1 for every row, Q = 0;
                     // the flip term of this step would then add 2 * 0
-                    fold_all(idx - 1, active);
+                    fold_all(idx - 1);
+                } else if (b + 1 < L) {
+                    // flip term G[r] += 2 delta_r(k-1) Q(k-1), delta_r(k-1) = +1
+                    // when the row now turns -1; bits b, b+1 of idx are bits
+                    // of k here, so the sign is the same for all walks
+                    cf v[CPL];
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) v[c] = Q[c];
+                    cf s = reduce_scatter<CPL>(v, grp);
+                    const float f = sub ? 2.f : -2.f;
+                    s.rh = __fmul_rn(s.rh, f);
+                    s.rl = __fmul_rn(s.rl, f);
+                    s.ih = __fmul_rn(s.ih, f);
+                    s.il = __fmul_rn(s.il, f);
+                    g_add(r, s);
                 } else {
-                    // flip term: G[r] += 2 delta_r(k-1) Q(k-1); delta_r(k-1) = +1
-                    // when the row now turns -1
-                    {
+                    // middle step of the walk: the sign depends on the walk
                     cf v[CPL];
 #pragma unroll
                     for (int c = 0; c < CPL; ++c) {
                         cf q = Q[c];
-                        q.rh *= 2.f; q.rl *= 2.f; q.ih *= 2.f; q.il *= 2.f;
-                        v[c] = active ? cf_scale_sign(q, sub ? 0u : 0x80000000u) : cf{0.f, 0.f, 0.f, 0.f};
+                        q.rh = __fmul_rn(q.rh, 2.f);
+                        q.rl = __fmul_rn(q.rl, 2.f);
+                        q.ih = __fmul_rn(q.ih, 2.f);
+                        q.il = __fmul_rn(q.il, 2.f);
+                        v[c] = cf_scale_sign(q, sub ? 0u : 0x80000000u);
                     }
-                    cf s = reduce_scatter<CPL>(v, grp);
-                    if (writer && my_col < n) {
-                        float4 gg = G[r * NP + my_col];
-                        df_acc(gg.x, gg.y, s.rh, s.rl);
-                        df_acc(gg.z, gg.w, s.ih, s.il);
-                        G[r * NP + my_col] = gg;
-                    }
-                }
+                    g_add(r, reduce_scatter<CPL>(v, grp));
                 }
                 const longlong2* a = s_a2 + r * NP + j0;
                 if (sub) {
@@ -255,37 +294,51 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
                     x[c] = cf{1.f, 0.f, 0.f, 0.f};
                 }
             }
-            // partial product of my columns, then the product of the other
-            // three lanes' partials (gathered in the group)
+            // prefix products pre[c] = prod_{c' < c} x_c' (pre[0] = 1 is implicit);
+            // the last one times x[CPL-1] is the lane's partial product
+            cf pre[CPL];
             cf part = x[0];
+            if (CPL > 1) {
+                pre[1] = x[0];
 #pragma unroll
-            for (int c = 1; c < CPL; ++c) part = cf_mul(part, x[c]);
-            const int lbase = lane - g;
+                for (int c = 2; c < CPL; ++c) pre[c] = cf_mul(pre[c - 1], x[c - 1]);
+                part = cf_mul(pre[CPL - 1], x[CPL - 1]);
+            }
+            // product of the other three lanes' partials (gathered in the group)
             cf o1 = shfl_cf(part, lbase + ((g + 1) & 3));
             cf o2 = shfl_cf(part, lbase + ((g + 2) & 3));
             cf o3 = shfl_cf(part, lbase + ((g + 3) & 3));
-            cf excl = cf_mul(cf_mul(o1, o2), o3);
+            cf seed = cf_scale_sign(cf_mul(cf_mul(o1, o2), o3), sbit);  // s(delta) folded in once
+            seed.rh = __fmul_rn(seed.rh, wgt);
+            seed.rl = __fmul_rn(seed.rl, wgt);
+            seed.ih = __fmul_rn(seed.ih, wgt);
+            seed.il = __fmul_rn(seed.il, wgt);
             // permanent term (leader)
-            if (g == 0 && active) {
-                cf tot = cf_scale_sign(cf_mul(excl, part), sbit);
-                df_acc(prh, prl, tot.rh, tot.rl);
-                df_acc(pih, pil, tot.ih, tot.il);
+            if (g == 0) {
+                cf t = cf_mul(seed, part);
+                df_add_lazy(prh, prl, t.rh, t.rl);
+                df_add_lazy(pih, pil, t.ih, t.il);
             }
-            // W_c = excl * prod_{c' < c} x_c' * prod_{c' > c} x_c' (prefix/suffix)
-            cf pre[CPL];
-            pre[0] = cf_scale_sign(excl, sbit);  // fold the sign s(delta) in once
-#pragma unroll
-            for (int c = 1; c < CPL; ++c) pre[c] = cf_mul(pre[c - 1], x[c - 1]);
-            cf suf{1.f, 0.f, 0.f, 0.f};
+            // W_c = seed * prod_{c' > c} x_c' * pre[c]
+            cf suf = seed;
 #pragma unroll
             for (int c = CPL - 1; c >= 0; --c) {
-                cf w = (c == CPL - 1) ? pre[c] : cf_mul(pre[c], suf);
-                Q[c] = cf_add(Q[c], w);
-                if (c > 0) suf = (c == CPL - 1) ? x[c] : cf_mul(suf, x[c]);
+                cf w = (c == 0) ? suf : cf_mul(pre[c], suf);
+                Q[c] = cf_add_lazy(Q[c], w);
+                if (c > 0) suf = cf_mul(suf, x[c]);
+            }
+            if ((k & 7ull) == 7ull) {
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    df_renorm(Q[c].rh, Q[c].rl);
+                    df_renorm(Q[c].ih, Q[c].il);
+                }
+                df_renorm(prh, prl);
+                df_renorm(pih, pil);
             }
         }
         // end term of the walk
-        fold_all(i0 + L - 1, active);
+        fold_all(i0 + Lsteps - 1);
     }
     __syncwarp();
     // write the warp's G tile and permanent partial
@@ -295,68 +348,70 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
         outg[e] = G[r * NP + j];
     }
     // permanent: sum the 8 leaders' partials
+    df_renorm(prh, prl);
+    df_renorm(pih, pil);
     cf pp{prh, prl, pih, pil};
 #pragma unroll
-    for (int m = kGroup; m < 32; m <<= 1) pp = cf_add(pp, shfl_xor_cf(pp, m));
+    for (int m = kGroup; m < 32; m <<= 1) {
+        cf o = shfl_xor_cf(pp, m);
+        df_acc(pp.rh, pp.rl, o.rh, o.rl);
+        df_acc(pp.ih, pp.il, o.ih, o.il);
+    }
     if (lane == 0) p.warp_p[gwarp] = make_float4(pp.rh, pp.rl, pp.ih, pp.il);
 }
 
-// Sum the warp tiles (fixed order) in double-double, scale, write the
-// gradient (complex128, n x n row-major) and the permanent.
-__global__ void grad_finalize_kernel(const float4* warp_g, const float4* warp_p, int nwarps, int n,
-                                     const int* exp_in, const int* col_e, const int* df_info, double* grad,
-                                     double* perm2, double* perm4) {
+// First finalize stage: element e < n*n of the gradient (e == n*n: the
+// permanent) summed over kFinWarps consecutive warp tiles, in double-float,
+// one partial per (chunk, element).  Every SM takes part.
+__global__ void grad_partial_kernel(const float4* warp_g, const float4* warp_p, int nwarps, int n,
+                                    float4* part) {
+    const int ne = n * n + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    const int boost = df_info[0];
+    if (e >= ne) return;
+    const int w0 = blockIdx.y * kFinWarps;
+    const int w1 = min(w0 + kFinWarps, nwarps);
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int w = w0; w < w1; ++w) {
+        const float4 v = e < n * n ? warp_g[(size_t)w * n * n + e] : warp_p[w];
+        df_acc(rh, rl, v.x, v.y);
+        df_acc(ih, il, v.z, v.w);
+    }
+    part[(size_t)blockIdx.y * ne + e] = make_float4(rh, rl, ih, il);
+}
+
+// Second stage: sum the chunk partials in a fixed order in double-double,
+// scale, write the gradient (complex128, n x n row-major) and the permanent.
+__global__ void grad_finalize_kernel(const float4* part, int nchunks, int n, const int* exp_in, const int* col_e,
+                                     const int* df_info, double* grad, double* perm2, double* perm4) {
+    const int ne = n * n + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
     if (df_info[1] == 0) {
-        if (e < n * n) grad[2 * e] = grad[2 * e + 1] = nan("");
-        if (e == 0) {
+        if (e < n * n) {
+            grad[2 * e] = grad[2 * e + 1] = nan("");
+        } else {
             perm2[0] = perm2[1] = nan("");
             if (perm4) perm4[0] = perm4[1] = perm4[2] = perm4[3] = nan("");
         }
         return;
     }
+    cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    for (int c = 0; c < nchunks; ++c) {
+        const float4 v = part[(size_t)c * ne + e];
+        acc.re = dd_add(acc.re, dd{(double)v.x, (double)v.y});
+        acc.im = dd_add(acc.im, dd{(double)v.z, (double)v.w});
+    }
     if (e < n * n) {
-        cdd acc{{0.0, 0.0}, {0.0, 0.0}};
-        for (int w = 0; w < nwarps; ++w) {
-            float4 v = warp_g[(size_t)w * n * n + e];
-            acc.re = dd_add(acc.re, dd{(double)v.x, (double)v.y});
-            acc.im = dd_add(acc.im, dd{(double)v.z, (double)v.w});
-        }
         const int l = e % n;
         // W_l omits column l: remove its factor from the permanent's scale
-        const int ex = *exp_in - (col_e[l] - boost);
+        const int ex = *exp_in - (col_e[l] - df_info[0]);
         double r2[2];
         write_result(acc, ex, r2, nullptr);
         grad[2 * e] = r2[0];
         grad[2 * e + 1] = r2[1];
-    }
-    if (e == 0) {
-        cdd acc{{0.0, 0.0}, {0.0, 0.0}};
-        for (int w = 0; w < nwarps; ++w) {
-            float4 v = warp_p[w];
-            acc.re = dd_add(acc.re, dd{(double)v.x, (double)v.y});
-            acc.im = dd_add(acc.im, dd{(double)v.z, (double)v.w});
-        }
+    } else {
         write_result(acc, *exp_in, perm2, perm4);
     }
-}
-
-// Per-column exponents e_j of the fixed-point scaling (the prepare kernel
-// keeps them internal; recomputed here identically).
-__global__ void col_exp_kernel(const double2* A, long long ld, int n, int* col_e) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    double br = 0.0, bi = 0.0;
-    for (int i = 0; i < n; ++i) {
-        double2 a = A[(long long)i * ld + j];
-        br += fabs(a.x);
-        bi += fabs(a.y);
-    }
-    double b = fmax(br, bi) * (1.0 + 1e-12);
-    int e = 0;
-    if (b > 0.0) frexp(b, &e);
-    col_e[j] = e;
 }
 
 template <int CPL>
@@ -372,6 +427,7 @@ struct GradPlan {
     int seg_log2 = 0;
     unsigned long long nseg = 1;
     int nwarps = 1;
+    int nchunks = 1;  // partials of the first finalize stage
 };
 
 static GradPlan plan_grad(int n) {
@@ -390,27 +446,40 @@ static GradPlan plan_grad(int n) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, grad_kernel<8>, kThreads, smem);
     }
     if (nb < 1) nb = 1;
-    int grid_full = sms * nb;
-    int slog = n - 1;
-    // walks of >= 2 kChunk steps when possible; >= 8 walks per resident group slot
-    unsigned long long slots = (unsigned long long)grid_full * (kThreads / 32) * kGroups;
-    int l = slog - ceil_log2_u64(8ull * slots);
-    if (l < 9) l = 9;
-    if (l > slog) l = slog;
-    gp.seg_log2 = l;
-    gp.nseg = 1ull << (slog - l);
+    const int grid_full = sms * nb;
+    const int slog = n - 1;
+    // walk length 2^l: the walks are dealt to the resident walk slots in
+    // passes, so the time goes as passes x (2^l + per-walk cost), the
+    // per-walk cost (start-up and the final fold of n rows) being about
+    // 0.2 n + 16 steps.  Ties go to the longer walk.
+    const unsigned long long slots = (unsigned long long)grid_full * (kThreads / 32) * kGroups;
+    double best = 1e300;
+    int best_l = slog;
+    for (int l = slog; l >= 0; --l) {
+        const unsigned long long nseg = 1ull << (slog - l);
+        const double passes = (double)((nseg + slots - 1) / slots);
+        const double cost = passes * (std::ldexp(1.0, l) + 0.2 * n + 16.0);
+        if (cost < best * (1.0 - 1e-9)) {
+            best = cost;
+            best_l = l;
+        }
+    }
+    gp.seg_log2 = best_l;
+    gp.nseg = 1ull << (slog - best_l);
     unsigned long long warps_needed = (gp.nseg + kGroups - 1) / kGroups;
     unsigned long long blocks_needed = (warps_needed + 3) / 4;
     gp.grid = (int)(blocks_needed < (unsigned long long)grid_full ? blocks_needed : (unsigned long long)grid_full);
     if (gp.grid < 1) gp.grid = 1;
     gp.nwarps = gp.grid * (kThreads / 32);
+    gp.nchunks = (gp.nwarps + kFinWarps - 1) / kFinWarps;
     return gp;
 }
 
 static size_t grad_ws_bytes(int n, const GradPlan& gp) {
     size_t mat = align_up((size_t)n * n * sizeof(longlong2), 256);
     return 2 * mat + 256 + 256 + align_up((size_t)n * sizeof(int), 256) +
-           align_up((size_t)gp.nwarps * n * n * sizeof(float4), 256) + align_up((size_t)gp.nwarps * sizeof(float4), 256);
+           align_up((size_t)gp.nwarps * n * n * sizeof(float4), 256) + align_up((size_t)gp.nwarps * sizeof(float4), 256) +
+           align_up((size_t)gp.nchunks * (n * n + 1) * sizeof(float4), 256);
 }
 
 // Device-side gradient: dA (n x n complex128, ld), grad out (n x n complex128
@@ -436,7 +505,10 @@ static int run_grad_dev(const double2* dA, long long ld, int n, void* ws, size_t
     float4* warp_g = reinterpret_cast<float4*>(base + off);
     off += align_up((size_t)gp.nwarps * n * n * sizeof(float4), 256);
     float4* warp_p = reinterpret_cast<float4*>(base + off);
+    off += align_up((size_t)gp.nwarps * sizeof(float4), 256);
+    float4* fin_part = reinterpret_cast<float4*>(base + off);
     PrepArgs pa;
+    pa.col_e_out = col_e;
     pa.A = dA;
     pa.ld = ld;
     pa.rows = n;
@@ -451,7 +523,6 @@ static int run_grad_dev(const double2* dA, long long ld, int n, void* ws, size_t
     pa.df_info = df_info;
     cudaError_t e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: prepare");
-    col_exp_kernel<<<1, 64, 0, st>>>(dA, ld, n, col_e);
     GradArgs g;
     g.a1 = a1;
     g.a2 = a2;
@@ -466,8 +537,10 @@ static int run_grad_dev(const double2* dA, long long ld, int n, void* ws, size_t
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: kernel");
     // the boost is read on the device by the finalize kernel via df_info
-    grad_finalize_kernel<<<(n * n + 127) / 128, 128, 0, st>>>(warp_g, warp_p, gp.nwarps, n, exp_out, col_e,
-                                                            df_info, d_grad, d_perm, d_perm4);
+    const int ne = n * n + 1;
+    grad_partial_kernel<<<dim3((ne + 127) / 128, gp.nchunks), 128, 0, st>>>(warp_g, warp_p, gp.nwarps, n, fin_part);
+    grad_finalize_kernel<<<(ne + 127) / 128, 128, 0, st>>>(fin_part, gp.nchunks, n, exp_out, col_e, df_info, d_grad,
+                                                          d_perm, d_perm4);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: finalize");
     return GBPERM_OK;

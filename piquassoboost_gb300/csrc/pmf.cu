@@ -1,0 +1,548 @@
+// One probability layer of the generalized Clifford & Clifford sampler.
+//
+// Replaces compute_pmf (piquassoboost/sampling/simulation_strategies/source/
+// samplingHelperFunctions.cpp:78-342), called once per photon by the
+// simulation strategies (CGeneralizedCliffordsBSimulationStrategy.cpp:298,
+// CGeneralizedCliffordsBUniformLossesSimulationStrategy.cpp:262,
+// CGeneralizedCliffordsBLossySimulationStrategy.cpp:350).  For every occupied
+// input mode l the reference computes the repeated permanent of the sample
+// (rows) against the input with one photon removed from l (columns) -- one
+// task and one full Gray sweep per l on the CPU, or one multi-input batch on
+// its FPGA path (GlynnPermanentCalculatorRepeatedInputBatch_DFE) -- and
+// contracts them with the interferometer:
+//   pmf[m] ~ | sum_l input[l] * perm_l * U[m][l] |^2,  normalised to sum 1.
+//
+// All these permanents share the row side (the sample), hence the Gray walk,
+// the column sums and the binomial weights; they differ only in the product,
+// where column l carries one power less:
+//   perm_l = 2^-(N-1) sum_g sign w(g) x_l^(c_l - 1) prod_{j != l} x_j^(c_j).
+// One sweep evaluates every perm_l with leave-one-out products (prefix and
+// suffix products, no division).  G lanes share a segment; lane g owns
+// columns [g*CPL, (g+1)*CPL), gathers the other lanes' partial products and
+// forms  prefix x x_c^(c_c - 1) x suffix  for its own columns.  Column sums
+// are exact int64 fixed point and the digit walk is the one of
+// perm_repeated.cu; the product runs on the FP64 pipe.  A step costs about
+// 4 C complex multiplies for all C permanents, against C - 1 per permanent
+// (C^2 in all) in the per-mode form.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gbperm.h"
+#include "gbperm_capi_internal.h"
+
+namespace gbperm {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kFinThreads = 256;
+
+__device__ __forceinline__ cd shfl_cd(cd v, int src) {
+    return cd{__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src)};
+}
+
+// x^e for e >= 1 by squaring
+__device__ __forceinline__ cd cpow_pos(cd x, int e) {
+    cd acc = x;
+    bool have = false;
+    cd y = x;
+    while (e > 0) {
+        if (e & 1) {
+            acc = have ? cmul(acc, y) : y;
+            have = true;
+        }
+        e >>= 1;
+        if (e) y = cmul(y, y);
+    }
+    return acc;
+}
+
+template <int CPL, int G>
+__global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part) {
+    constexpr int NP = CPL * G;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cdd* s_acc = reinterpret_cast<cdd*>(smem_raw);                           // CPL x kThreads
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(s_acc + CPL * kThreads);  // R x NP
+    longlong2* s_a2 = s_a1 + p.R * NP;                                       // nd x NP
+    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);               // P
+    unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);      // P
+    __shared__ int s_cpow[NP];
+    __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
+    __shared__ long long s_stride[kMaxDigits];
+    const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
+    }
+    for (int e = threadIdx.x; e < nd * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
+    }
+    for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
+        s_w[e] = p.wlow[e];
+        s_seq[e] = p.seq[e];
+    }
+    for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
+    for (int e = threadIdx.x; e < nd; e += blockDim.x) s_D[e] = p.D[e];
+    for (int e = threadIdx.x; e < R; e += blockDim.x) s_r[e] = p.rcoef[e];
+    for (int e = threadIdx.x; e < CPL * kThreads; e += blockDim.x) s_acc[e] = cdd{{0.0, 0.0}, {0.0, 0.0}};
+    if (threadIdx.x == 0) {
+        long long s = 1;
+        for (int i = 0; i < q; ++i) {
+            s_stride[i] = s;
+            s *= (long long)(p.D[i] + 1);
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int g = lane % G;
+    const int j0 = g * CPL;
+    const int lbase = lane - g;
+    cdd* my_acc = s_acc + threadIdx.x;  // column c at my_acc[c * kThreads]
+    // segments: each warp takes 32/G consecutive ones per pass; the loop
+    // bound is warp-uniform so every shuffle runs with the full warp
+    const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / G;
+    const unsigned long long lane_seg = (unsigned long long)(lane / G);
+    long long cre[CPL], cim[CPL];
+
+    for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / G;
+         hw < p.nseg; hw += T) {
+        const unsigned long long h_raw = hw + lane_seg;
+        const bool active = h_raw < p.nseg;
+        const unsigned long long h = active ? h_raw : 0ull;
+        int gdig[kMaxDigits];
+        {
+            unsigned long long rem = h;
+            int cnt[kMaxDigits];
+            for (int i = q; i < nd; ++i) {
+                unsigned long long L = (unsigned long long)(s_D[i] + 1);
+                cnt[i] = (int)(rem % L);
+                rem /= L;
+            }
+            int par = 0;
+            for (int i = nd - 1; i >= 0; --i) {
+                int c = i >= q ? cnt[i] : 0;
+                int gg = par ? s_D[i] - c : c;
+                gdig[i] = gg;
+                par ^= gg & 1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cre[c] = 0;
+            cim[c] = 0;
+        }
+        int gsum = 0;
+        double whigh = 1.0;
+        unsigned long long Gd = 0ull;  // low Gray digits, 4 bits each
+        unsigned int dir = 0u;         // bit i set: low digit i moves up next
+        long long widx = 0;
+        for (int i = 0; i < R; ++i) {
+            int gi = i < nd ? gdig[i] : 0;
+            long long coef = (long long)(s_r[i] - 2 * gi);
+            const longlong2* a = s_a1 + i * NP + j0;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                longlong2 v = a[c];
+                cre[c] += coef * v.x;
+                cim[c] += coef * v.y;
+            }
+            if (i < nd) {
+                gsum += gi;
+                if (i < q) {
+                    Gd |= (unsigned long long)gi << (4 * i);
+                    if (gi == 0) dir |= 1u << i;
+                    widx += (long long)gi * s_stride[i];
+                } else {
+                    whigh *= p.binom[s_D[i] * kBinomStride + gi];
+                }
+            }
+        }
+        double sgn = (gsum & 1) ? -whigh : whigh;
+        if (!active) sgn = 0.0;
+        cd blk[CPL];
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) blk[c] = cd{0.0, 0.0};
+        for (unsigned long long k = 0; k < p.P; ++k) {
+            if (k != 0) {
+                const int d = s_seq[k];  // warp-uniform
+                const bool up = (dir >> d) & 1u;
+                const int sh = 4 * d;
+                int gv = (int)((Gd >> sh) & 15ull);
+                gv += up ? 1 : -1;
+                Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
+                if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
+                widx += up ? s_stride[d] : -s_stride[d];
+                const long long m = up ? -1ll : 0ll;  // up: one more -1 delta -> subtract 2 a
+                const longlong2* a = s_a2 + d * NP + j0;
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    longlong2 v = a[c];
+                    cre[c] += (v.x ^ m) - m;
+                    cim[c] += (v.y ^ m) - m;
+                }
+                sgn = -sgn;
+                if ((k & 255ull) == 0) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        cdd t = my_acc[c * kThreads];
+                        t.re = dd_add_d(t.re, blk[c].re);
+                        t.im = dd_add_d(t.im, blk[c].im);
+                        my_acc[c * kThreads] = t;
+                        blk[c] = cd{0.0, 0.0};
+                    }
+                }
+            }
+            // P_c = x_c^(c_c) (1 for padding columns)
+            cd Pv[CPL];
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                const int e = s_cpow[j0 + c];
+                cd x{fix_to_double(cre[c]), fix_to_double(cim[c])};
+                Pv[c] = e == 1 ? x : (e == 0 ? cd{1.0, 0.0} : cpow_pos(x, e));
+            }
+            cd part = Pv[0];
+#pragma unroll
+            for (int c = 1; c < CPL; ++c) part = cmul(part, Pv[c]);
+            // weight x product of the other lanes of the group
+            cd run{sgn * s_w[widx], 0.0};
+#pragma unroll
+            for (int t = 1; t < G; ++t) run = cmul(run, shfl_cd(part, lbase + ((g + t) % G)));
+            // suffix products: suf[c] = prod_{c' > c} P_c'
+            cd suf[CPL];
+            suf[CPL - 1] = cd{1.0, 0.0};
+            if (CPL > 1) suf[CPL > 1 ? CPL - 2 : 0] = Pv[CPL - 1];
+#pragma unroll
+            for (int c = CPL - 3; c >= 0; --c) suf[c] = cmul(suf[c + 1], Pv[c + 1]);
+            // leave-one-out: run (weight x other lanes x prefix) x x_c^(c_c - 1) x suffix
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                const int e = s_cpow[j0 + c];
+                cd lo = c == CPL - 1 ? run : cmul(run, suf[c]);
+                if (e > 1) {
+                    cd x{fix_to_double(cre[c]), fix_to_double(cim[c])};
+                    lo = cmul(lo, cpow_pos(x, e - 1));
+                }
+                blk[c].re += lo.re;
+                blk[c].im += lo.im;
+                if (c < CPL - 1) run = cmul(run, Pv[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cdd t = my_acc[c * kThreads];
+            t.re = dd_add_d(t.re, blk[c].re);
+            t.im = dd_add_d(t.im, blk[c].im);
+            my_acc[c * kThreads] = t;
+        }
+    }
+    __syncthreads();
+    // column j = g*CPL + c is held by the threads t with t % G == g: sum them
+    // in a fixed order
+    for (int j = threadIdx.x; j < NP; j += blockDim.x) {
+        const int gj = j / CPL, c = j % CPL;
+        cdd b = s_acc[c * kThreads + gj];
+        for (int t = gj + G; t < kThreads; t += G) b = cdd_add(b, s_acc[c * kThreads + t]);
+        if (j < C) col_part[(size_t)blockIdx.x * C + j] = b;
+    }
+}
+
+// Sum the block partials per column in a fixed order and scale: perm_l =
+// sum * 2^(exp - e_l) (column l lost one factor of its 2^-e_l scaling).
+// Then the contraction with the interferometer and the normalisation, in the
+// reference's order (input modes ascending, total over modes ascending).
+__global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* col_part, int nblocks, int C,
+                                                                   const int* exp_in, const int* col_e,
+                                                                   const int* col_mode, const double* cin_w,
+                                                                   const double2* U, long long ldu, int m,
+                                                                   double* pmf, double2* addends) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2* s_perm = reinterpret_cast<double2*>(smem_raw);  // C
+    __shared__ double s_tot;
+    for (int j = threadIdx.x; j < C; j += blockDim.x) {
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        for (int b = 0; b < nblocks; ++b) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
+        double o[2];
+        write_result(tot, *exp_in - col_e[j], o, nullptr);
+        s_perm[j] = make_double2(o[0], o[1]);
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) addends[i] = make_double2(0.0, 0.0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < C; j += blockDim.x) addends[col_mode[j]] = s_perm[j];
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        double re = 0.0, im = 0.0;
+        for (int j = 0; j < C; ++j) {
+            const double2 u = U[(long long)i * ldu + col_mode[j]];
+            const double pr = cin_w[j] * s_perm[j].x, pi = cin_w[j] * s_perm[j].y;
+            re += pr * u.x - pi * u.y;
+            im += pr * u.y + pi * u.x;
+        }
+        pmf[i] = re * re + im * im;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int i = 0; i < m; ++i) tot += pmf[i];
+        s_tot = tot;
+    }
+    __syncthreads();
+    const double tot = s_tot;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) pmf[i] = pmf[i] / tot;
+}
+
+template <int CPL, int G>
+size_t pmf_smem(const RepArgs& a) {
+    return (size_t)CPL * kThreads * sizeof(cdd) + (size_t)(a.R + a.nd) * CPL * G * sizeof(longlong2) +
+           (size_t)a.P * (sizeof(double) + 1) + 16;
+}
+
+template <int CPL, int G>
+int pmf_bps_t(const RepArgs& a) {
+    int nb = 0;
+    size_t smem = pmf_smem<CPL, G>(a);
+    cudaFuncSetAttribute(pmf_kernel<CPL, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pmf_kernel<CPL, G>, kThreads, smem);
+    return nb > 0 ? nb : 1;
+}
+
+template <int CPL, int G>
+cudaError_t pmf_launch_t(const RepArgs& a, cdd* col_part, int grid, cudaStream_t st) {
+    size_t smem = pmf_smem<CPL, G>(a);
+    cudaError_t e =
+        cudaFuncSetAttribute(pmf_kernel<CPL, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    pmf_kernel<CPL, G><<<grid, kThreads, smem, st>>>(a, col_part);
+    return cudaGetLastError();
+}
+
+// lane-group shape for C product columns: 4 lanes up to 32 columns, 8 above
+void pmf_shape(int C, int* cpl, int* grp) {
+    *grp = 4;
+    if (C <= 4) *cpl = 1;
+    else if (C <= 8) *cpl = 2;
+    else if (C <= 16) *cpl = 4;
+    else if (C <= 32) *cpl = 8;
+    else *cpl = 8, *grp = 8;
+}
+
+int pmf_bps(const RepArgs& a, int cpl, int grp) {
+    if (grp == 8) return pmf_bps_t<8, 8>(a);
+    switch (cpl) {
+        case 1: return pmf_bps_t<1, 4>(a);
+        case 2: return pmf_bps_t<2, 4>(a);
+        case 4: return pmf_bps_t<4, 4>(a);
+        default: return pmf_bps_t<8, 4>(a);
+    }
+}
+
+cudaError_t pmf_launch(const RepArgs& a, int cpl, int grp, cdd* col_part, int grid, cudaStream_t st) {
+    if (grp == 8) return pmf_launch_t<8, 8>(a, col_part, grid, st);
+    switch (cpl) {
+        case 1: return pmf_launch_t<1, 4>(a, col_part, grid, st);
+        case 2: return pmf_launch_t<2, 4>(a, col_part, grid, st);
+        case 4: return pmf_launch_t<4, 4>(a, col_part, grid, st);
+        default: return pmf_launch_t<8, 4>(a, col_part, grid, st);
+    }
+}
+
+// FP64 flops of one Gray step of pmf_kernel: per lane CPL-1 (partial
+// product) + G-1 (gather) + CPL-2 (suffix) + 2 (CPL-1) (leave-one-out)
+// complex products of 6 flops, plus 2 adds per column
+double pmf_step_flops(int C, int cpl, int grp) {
+    double cm = (double)(cpl - 1) + (grp - 1) + std::max(cpl - 2, 0) + 2.0 * (cpl - 1);
+    return 6.0 * cm * grp + 2.0 * C;
+}
+
+}  // namespace
+
+}  // namespace gbperm
+
+using namespace gbperm;
+
+extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample,
+                                  const int64_t* current_input, double* pmf, double* addends,
+                                  gbperm_stats* stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (m <= 0) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: no modes");
+    if (!U || !sample || !current_input || !pmf) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: null argument");
+    if (ld < m) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: ld < m");
+    int64_t ns = 0, ni = 0;
+    std::vector<int> cols;  // occupied input modes, ascending
+    for (int64_t i = 0; i < m; ++i) {
+        if (sample[i] < 0 || current_input[i] < 0)
+            return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: negative occupation");
+        ns += sample[i];
+        ni += current_input[i];
+        if (current_input[i] > 0) cols.push_back((int)i);
+    }
+    if (ni == 0) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: empty input state");
+    if (ns + 1 != ni)
+        return fail(GBPERM_ERR_STATE_SUM,
+                    "gbperm_compute_pmf: the input state must hold one photon more than the sample");
+    if (ns > 64) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_compute_pmf: more than 64 photons in the sample");
+    if (!all_finite(U, m, m, ld)) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: non-finite interferometer");
+
+    RepHost h;
+    const bool first_photon = (ns == 0);
+    if (!first_photon) {
+        double triv[2];
+        bool is_triv = false;
+        int rc = repeated_plan(U, m, m, ld, current_input, m, sample, m, &h, triv, &is_triv, false, 1);
+        if (rc) return rc;
+    } else {
+        h.C = (int)cols.size();
+        h.col_src = cols;
+    }
+    const int C = h.C;
+    if (C > 64) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_compute_pmf: more than 64 occupied input modes");
+    RepArgs a{};
+    int cpl = 1, grp = 4, grid = 1;
+    if (!first_photon) {
+        a.R = h.R;
+        a.C = h.C;
+        a.nd = h.nd;
+        a.q = h.q;
+        a.P = h.P;
+        a.nseg = h.nseg;
+        pmf_shape(C, &cpl, &grp);
+    }
+    ThreadCtx& cx = thread_ctx();
+    int rc = cx.ensure(0);  // device check before any runtime query
+    if (rc) return rc;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!first_photon) {
+        int bps = pmf_bps(a, cpl, grp);
+        unsigned long long full = (unsigned long long)device_sms(dev) * bps;
+        unsigned long long per_block = (unsigned long long)(kThreads / grp);
+        unsigned long long need = (h.nseg + per_block - 1) / per_block;
+        grid = (int)std::max(1ull, std::min(full, need));
+    }
+    // device layout
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += align_up(bytes, 256);
+        return o;
+    };
+    const size_t o_U = take((size_t)m * m * sizeof(double2));
+    const size_t o_M = take(h.M.size() * sizeof(double));
+    const size_t o_a1 = take((size_t)h.R * C * sizeof(longlong2));
+    const size_t o_a2 = take((size_t)h.R * C * sizeof(longlong2));
+    const size_t o_ints = take((size_t)(h.R + h.nd + 3 * C + 64) * sizeof(int));
+    const size_t o_cw = take((size_t)C * sizeof(double));
+    const size_t o_wlow = take(h.wlow.size() * sizeof(double));
+    const size_t o_seq = take(h.seq.size());
+    const size_t o_binom = take((size_t)kBinomStride * kBinomStride * sizeof(double));
+    const size_t o_exp = take(64);
+    const size_t o_pmf = take((size_t)m * sizeof(double));
+    const size_t o_add = take((size_t)m * sizeof(double2));  // 16-byte elements: own aligned region
+    const size_t o_part = take((size_t)grid * C * sizeof(cdd));
+    rc = cx.ensure(off);
+    if (rc) return rc;
+    char* base = static_cast<char*>(cx.dbuf);
+    cudaStream_t st = cx.stream;
+
+    // interferometer, dense (ld = m) complex128
+    std::vector<double> Ud((size_t)m * m * 2);
+    for (int64_t i = 0; i < m; ++i)
+        std::memcpy(&Ud[(size_t)i * m * 2], U + 2 * i * ld, (size_t)m * 2 * sizeof(double));
+    std::vector<int> ints;
+    ints.insert(ints.end(), h.rcoef.begin(), h.rcoef.end());
+    ints.insert(ints.end(), h.D.begin(), h.D.end());
+    ints.insert(ints.end(), h.cpow.begin(), h.cpow.end());
+    const size_t i_cole = ints.size();
+    ints.resize(ints.size() + C, 0);  // per-column exponents (written by the prepare kernel)
+    const size_t i_mode = ints.size();
+    ints.insert(ints.end(), h.col_src.begin(), h.col_src.end());
+    std::vector<double> cw(C);
+    for (int j = 0; j < C; ++j) cw[j] = (double)current_input[h.col_src[j]];
+    cudaError_t e = cudaMemcpyAsync(base + o_U, Ud.data(), Ud.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !h.M.empty())
+        e = cudaMemcpyAsync(base + o_M, h.M.data(), h.M.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + o_ints, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + o_cw, cw.data(), cw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !h.wlow.empty())
+        e = cudaMemcpyAsync(base + o_wlow, h.wlow.data(), h.wlow.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !h.seq.empty())
+        e = cudaMemcpyAsync(base + o_seq, h.seq.data(), h.seq.size(), cudaMemcpyHostToDevice, st);
+    const std::vector<double>& bt = binom_table();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + o_binom, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: upload");
+    int* d_ints = reinterpret_cast<int*>(base + o_ints);
+    int* d_exp = reinterpret_cast<int*>(base + o_exp);
+    cdd* d_part = reinterpret_cast<cdd*>(base + o_part);
+    int nblocks = grid;
+    std::vector<cdd> ones;
+    std::vector<int> zero;
+    if (stats) cudaEventRecord(cx.ev0, st);
+    if (!first_photon) {
+        PrepArgs pa;
+        pa.A = reinterpret_cast<const double2*>(base + o_M);
+        pa.ld = C;
+        pa.rows = h.R;
+        pa.cols = C;
+        pa.row_w = d_ints;
+        pa.col_w = d_ints + h.R + h.nd;
+        pa.norm_shift = h.photons - 1;
+        pa.a1 = reinterpret_cast<longlong2*>(base + o_a1);
+        pa.a2 = reinterpret_cast<longlong2*>(base + o_a2);
+        pa.exp_out = d_exp;
+        pa.col_e_out = d_ints + i_cole;
+        pa.df = 0;
+        pa.df_info = nullptr;
+        e = launch_prepare(pa, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: prepare");
+        a.a1 = pa.a1;
+        a.a2 = pa.a2;
+        a.rcoef = d_ints;
+        a.D = d_ints + h.R;
+        a.cpow = d_ints + h.R + h.nd;
+        a.wlow = reinterpret_cast<const double*>(base + o_wlow);
+        a.seq = reinterpret_cast<const unsigned char*>(base + o_seq);
+        a.binom = reinterpret_cast<const double*>(base + o_binom);
+        e = pmf_launch(a, cpl, grp, d_part, grid, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: launch");
+    } else {
+        // no sample yet: every permanent is of an empty matrix, i.e. 1
+        ones.assign(C, cdd{{1.0, 0.0}, {0.0, 0.0}});
+        zero.assign(1, 0);
+        e = cudaMemcpyAsync(d_part, ones.data(), C * sizeof(cdd), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_exp, zero.data(), sizeof(int), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: upload");
+        nblocks = 1;
+    }
+    double* d_pmf = reinterpret_cast<double*>(base + o_pmf);
+    double2* d_add = reinterpret_cast<double2*>(base + o_add);
+    const size_t fsmem = (size_t)C * sizeof(double2);
+    pmf_finalize_kernel<<<1, kFinThreads, fsmem, st>>>(d_part, nblocks, C, d_exp, d_ints + i_cole, d_ints + i_mode,
+                                                       reinterpret_cast<const double*>(base + o_cw),
+                                                       reinterpret_cast<const double2*>(base + o_U), m, (int)m,
+                                                       d_pmf, d_add);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: finalize");
+    if (stats) cudaEventRecord(cx.ev1, st);
+    e = cudaMemcpyAsync(pmf, d_pmf, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && addends)
+        e = cudaMemcpyAsync(addends, d_add, (size_t)m * sizeof(double2), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: kernel");
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, cx.ev0, cx.ev1);
+        stats->kernel_ms = ms;
+        stats->steps = first_photon ? 0.0 : h.steps;
+        stats->flops = first_photon ? 0.0 : pmf_step_flops(C, cpl, grp) * h.steps;
+        stats->launches = first_photon ? 1 : 3;
+        stats->grid = grid;
+        stats->seg_log2 = h.q;
+        stats->arith = GBPERM_ARITH_FP64;
+    }
+    return GBPERM_OK;
+}

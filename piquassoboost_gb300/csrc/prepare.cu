@@ -25,6 +25,7 @@ __global__ void prepare_kernel(PrepArgs p) {
         int e = 0;
         if (b > 0.0) frexp(b, &e);
         s_e[j] = e;
+        if (p.col_e_out) p.col_e_out[j] = e;
         s_typ[j] = b > 0.0 ? log2(sqrt(l2) / ldexp(1.0, e)) : -1e300;
         for (int i = 0; i < p.rows; ++i) {
             double2 a = p.A[(long long)i * p.ld + j];

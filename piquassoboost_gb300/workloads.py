@@ -50,3 +50,16 @@ def batched_instances(count: int, seed: int, modes: int = 100, kmin: int = 8, km
         c = rng.integers(0, modes, size=k)
         mats.append(np.ascontiguousarray(u[np.ix_(r, c)]))
     return mats
+
+
+def pmf_layer_instance(seed: int, modes: int = 60, photons: int = 30):
+    """The last probability layer of a Clifford & Clifford run: Haar
+    `modes`-mode unitary, one input photon in each of modes 0..photons-1, and
+    a sample of photons - 1 output photons from a seeded uniform multinomial
+    over all modes (a Haar interferometer spreads photons near uniformly)."""
+    u = haar_unitary(modes, seed)
+    rng = np.random.default_rng(seed + 15485863)
+    inp = np.zeros(modes, dtype=np.int64)
+    inp[:photons] = 1
+    sample = rng.multinomial(photons - 1, np.ones(modes) / modes).astype(np.int64)
+    return u, sample, inp
