@@ -7,7 +7,7 @@ permanent configuration, n in {30, 34, 36, 40}).  One step = one permanent.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--n 36] [--mode fast|fp64]
   python bench.py --impl reference ...   # the reference algorithm on host cores
-  python bench.py --workload repeated|batched|grad|pmf   # the other hot-path entry points
+  python bench.py --workload repeated|batched|grad|pmf|mesh   # the other hot-path entry points
 
 value   permanents/s with the matrix already resident in HBM (device-pointer
         entry point, CUDA events on the launching stream; L2 flushed between
@@ -50,11 +50,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "repeated", "batched", "grad", "pmf"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "repeated", "batched", "grad", "pmf", "mesh"],
                     help="plain: single n x n Haar block (default); repeated: 60-mode / 30-photon "
                          "multiplicity permanent; batched: 4096 uneven k=8..28 permanents in one launch; "
                          "grad: permanent + full gradient; pmf: one 60-mode / 30-photon boson-sampling "
-                         "probability layer")
+                         "probability layer; mesh: 512-term Clements-mesh log-likelihood, forward + backward")
     ap.add_argument("--n", type=int, default=36)
     ap.add_argument("--mode", default="fast", choices=["fast", "fp64"])
     ap.add_argument("--seed", type=int, default=36)
@@ -409,7 +409,7 @@ def run_secondary(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    fn = {"repeated": _repeated, "batched": _batched, "grad": _grad, "pmf": _pmf}[args.workload]
+    fn = {"repeated": _repeated, "batched": _batched, "grad": _grad, "pmf": _pmf, "mesh": _mesh}[args.workload]
     rc = fn(args, rank, world, torch)
     if world > 1:
         import torch.distributed as dist
@@ -618,7 +618,7 @@ def _grad(args, rank, world, torch):
                            f"Haar {2 * n}x{2 * n} unitary, one sweep", "n": n, "arith": "fast"},
               _roof(flops, statistics.mean(gms), peak, "grad_kernel (forward flops only)"),
               None, {"value": e2e, "unit": "(perm+grad)/s", "h2d_bytes_per_step": n * n * 16,
-                     "d2h_bytes_per_step": n * n * 16 + 16}, 4 * args.steps,
+                     "d2h_bytes_per_step": n * n * 16 + 16}, 5 * args.steps,
               {"forward_only_ms": statistics.mean(fms), "grad_ms": statistics.mean(gms),
                "grad_over_forward": statistics.mean(gms) / statistics.mean(fms)}, clocks=clocks)
     return 0
@@ -637,14 +637,14 @@ def _pmf(args, rank, world, torch):
     peak = nat.probe_peak("fp64")
     st = nat.Stats()
     for U, smp, cin in layers[:args.warmup]:
-        nat.compute_pmf(U, smp, cin)
+        nat.compute_pmf(U, smp, cin, mode=args.mode)
     kms, flops, nperm = [], 0.0, 0
     clk = ClockSampler(torch.cuda.current_device())
     clk.start()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for U, smp, cin in layers[args.warmup:]:
-        nat.compute_pmf(U, smp, cin, stats=st)
+        nat.compute_pmf(U, smp, cin, mode=args.mode, stats=st)
         kms.append(st.kernel_ms)
         flops += st.flops
         nperm += int(np.count_nonzero(cin))
@@ -670,12 +670,123 @@ def _pmf(args, rank, world, torch):
         _line(args, world, value, "layers/s", 1000 * wall / args.steps,
               {"workload": "boson-sampling pmf layer: 60-mode Haar, one input photon in modes 0-29, a seeded "
                            "uniform-multinomial sample of 29 photons; 30 leave-one-out permanents per layer",
-               "arith": "fp64", "l2": "inputs < 100 KB; compute-bound, no flush"},
-              _roof(flops / args.steps, statistics.mean(kms), peak, "pmf_kernel (executed FP64 flops)"),
+               "arith": args.mode, "l2": "inputs < 100 KB; compute-bound, no flush"},
+              _roof(flops / args.steps, statistics.mean(kms), peak,
+                    "pmf_df_kernel (FP64-equivalent flops of the FP64 form)" if args.mode == "fast"
+                    else "pmf_kernel (executed FP64 flops)"),
               cpu, {"value": e2e, "unit": "layers/s", "h2d_bytes_per_step": 60 * 60 * 16 + 2 * 60 * 8,
-                    "d2h_bytes_per_step": 60 * 8 + 60 * 16}, 3 * args.steps,
+                    "d2h_bytes_per_step": 60 * 8 + 60 * 16}, (4 if args.mode == "fast" else 3) * args.steps,
               {"permanents_per_s": value * nperm / args.steps,
                "kernel_ms": kms}, clocks=clocks)
+    return 0
+
+
+# ------------------------------------------------------------------- mesh
+def _mesh(args, rank, world, torch):
+    """Differentiable permanents in a photonic circuit: 512 terms
+    log|perm(U_S)|^2 of 12 photons in a 40-mode Clements mesh with seeded
+    uniform phases, backpropagated to the 1560 phases.  A step is the whole
+    forward and backward pass: mesh unitary, the 512 12 x 12 submatrices, their
+    permanents and full gradients (one batched sweep), the loss and the phase
+    gradient."""
+    from piquassoboost_gb300.torch_perm import clements_unitary, permanent
+    from piquassoboost_gb300.workloads import mesh_instance
+
+    m, k, terms = 40, 12, 512
+    insts = [mesh_instance(seed=args.seed + 1000 * rank + s, modes=m, photons=k, terms=terms)
+             for s in range(args.warmup + args.steps)]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+
+    def step(ph_dev, ins, outs):
+        ph = ph_dev.detach().requires_grad_(True)
+        U = clements_unitary(ph, m)
+        o = torch.as_tensor(outs, device=dev)
+        i = torch.as_tensor(ins, device=dev)
+        p = permanent(U[o[:, :, None], i[:, None, :]])
+        loss = torch.log((p * p.conj()).real).sum()
+        loss.backward()
+        return loss.detach(), ph.grad
+
+    dev_in = [(torch.tensor(ph, device=dev), ins, outs) for ph, ins, outs in insts]
+    for ph, ins, outs in dev_in[:args.warmup]:
+        step(ph, ins, outs)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    t0 = time.perf_counter()
+    for q in range(args.steps):
+        ph, ins, outs = dev_in[args.warmup + q]
+        ev[q][0].record(stream)
+        step(ph, ins, outs)
+        ev[q][1].record(stream)
+    torch.cuda.synchronize()
+    wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
+    clocks = clk.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    value = world * args.steps / (sum(ms) * 1e-3)
+    # e2e: phases from pinned host memory, loss and phase gradient back to the host
+    pinned = [torch.tensor(ph).pin_memory() for ph, _, _ in insts[args.warmup:]]
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for q in range(args.steps):
+        _, ins, outs = insts[args.warmup + q]
+        loss, g = step(pinned[q].to(dev, non_blocking=True), ins, outs)
+        loss.item()
+        g.cpu()
+    e2e = world * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
+    # the permanent kernels alone on the same 512 submatrices
+    from piquassoboost_gb300.torch_perm import permanents_and_grads
+    ph, ins, outs = dev_in[args.warmup]
+    with torch.no_grad():
+        U = clements_unitary(ph, m)
+        subs = U[torch.as_tensor(outs, device=dev)[:, :, None], torch.as_tensor(ins, device=dev)[:, None, :]]
+    permanents_and_grads(subs)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    permanents_and_grads(subs)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    perm_ms = e0.elapsed_time(e1)
+    flops = terms * 8.0 * k * 2.0 ** (k - 1)
+    from piquassoboost_gb300 import _native as nat
+    peak = nat.probe_peak("fp64")
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from concurrent.futures import ThreadPoolExecutor
+
+        orc = _oracle()
+        Uc = clements_unitary(torch.tensor(insts[args.warmup][0]), m).numpy()
+        _, ins, outs = insts[args.warmup]
+
+        def one_term(q):
+            A = Uc[np.ix_(outs[q], ins[q])]
+            orc.bbfg(A, prec=0, threads=1)
+            for r in range(k):
+                for c in range(k):
+                    orc.bbfg(np.delete(np.delete(A, r, 0), c, 1), prec=0, threads=1)
+
+        sample = 32
+        t = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+            list(ex.map(one_term, range(sample)))
+        dt = time.perf_counter() - t
+        cpu = {"value": 1.0 / (dt * terms / sample), "unit": "(loss+grad)/s", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": f"{sample} of the {terms} terms: each term's 12x12 permanent and its 144 11x11 minors "
+                         f"(the gradient through the reference's BBFG double algorithm, C oracle, one thread per "
+                         f"term on {os.cpu_count()} threads), scaled to the whole batch; the mesh itself not counted"}
+    if rank == 0:
+        _line(args, world, value, "(loss+grad)/s", 1000 * wall / args.steps,
+              {"workload": "512 terms log|perm(U_S)|^2, 12 photons in a 40-mode Clements mesh (seeded uniform "
+                           "phases, seeded mode sets), forward + backward to the 1560 phases", "arith": "fast",
+               "l2": "inputs < 1 MB; launch- and compute-bound, no flush"},
+              _roof(flops, perm_ms, peak, "grad_kernel (batched; forward flops only)"),
+              cpu, {"value": e2e, "unit": "(loss+grad)/s", "h2d_bytes_per_step": 1560 * 8,
+                    "d2h_bytes_per_step": 1560 * 8 + 8}, 5 * args.steps,
+              {"step_ms": ms, "permanent_kernels_ms": perm_ms}, clocks=clocks)
     return 0
 
 
@@ -710,6 +821,34 @@ def _reference_secondary(args, world):
             fl.append(f)
         v = 4096 / (sum(ts) / len(ts) * flops / fl[0])
         unit, sample = "perm/s", "16 size-stratified instances per step, scaled to the 4096-instance batch"
+    elif args.workload == "mesh":
+        from concurrent.futures import ThreadPoolExecutor
+
+        import torch
+
+        from piquassoboost_gb300.torch_perm import clements_unitary
+        from piquassoboost_gb300.workloads import mesh_instance
+
+        ph, ins, outs = mesh_instance(seed=args.seed, modes=40, photons=12, terms=512)
+        Uc = clements_unitary(torch.tensor(ph), 40).numpy()
+
+        def one_term(q):
+            A = Uc[np.ix_(outs[q], ins[q])]
+            orc.bbfg(A, prec=0, threads=1)
+            for r in range(12):
+                for c in range(12):
+                    orc.bbfg(np.delete(np.delete(A, r, 0), c, 1), prec=0, threads=1)
+
+        sample = 32
+        ts = []
+        with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+            for _ in range(args.steps):
+                t = time.perf_counter()
+                list(ex.map(one_term, range(sample)))
+                ts.append((time.perf_counter() - t) * 512 / sample)
+        v = args.steps / sum(ts)
+        unit, sample = "(loss+grad)/s", ("32 of the 512 terms per step (permanent + 144 minors each, one thread per "
+                                         "term), scaled to the batch")
     elif args.workload == "pmf":
         from piquassoboost_gb300.workloads import pmf_layer_instance
 

@@ -52,7 +52,8 @@ extern "C" {
 typedef struct gbperm_stats {
     double kernel_ms;      /* device time of the compute launches (CUDA events) */
     double steps;          /* Gray-code steps evaluated (terms of the sum) */
-    double flops;          /* algorithmic FP64 flops: 8 n per plain step, see DESIGN */
+    double flops;          /* algorithmic FP64 flops: 8 n per plain step (2n column-sum adds,
+                              6(n-1) for the product, 2 for the accumulate) */
     int32_t launches;      /* kernels launched by the call */
     int32_t grid;          /* blocks of the main launch */
     int32_t seg_log2;      /* log2 of the Gray segment length (plain / grad) */
@@ -146,11 +147,13 @@ int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t
  * with perm_l the repeated permanent of the sample rows against the input
  * with one photon removed from mode l; addends (NULL or 2 m doubles)
  * receives the perm_l as complex128 (0 for empty input modes).  All perm_l
- * come from one Gray-code sweep over the sample.  Up to 64 sample photons
- * and 64 occupied input modes; a photon-count mismatch ->
+ * come from one Gray-code sweep over the sample.  arith as for the
+ * permanents (the double-float product serves up to 32 occupied input modes
+ * and falls back to FP64 beyond that or when the range check fails).  Up to
+ * 64 sample photons and 64 occupied input modes; a photon-count mismatch ->
  * GBPERM_ERR_STATE_SUM. */
 int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample, const int64_t* current_input,
-                       double* pmf, double* addends, gbperm_stats* stats);
+                       int arith, double* pmf, double* addends, gbperm_stats* stats);
 
 /* ----------------------------------------------- permanent + gradient */
 /* Permanent of an n x n matrix and its full gradient G[k][l] = dperm/da_kl
@@ -166,6 +169,17 @@ size_t gbperm_perm_grad_workspace_size(int64_t n);
 /* Device-pointer form; on a range-check failure perm and grad are NaN. */
 int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, void* d_perm_dd, void* d_grad,
                          void* workspace, size_t workspace_bytes, void* stream);
+/* Batch of `count` n x n matrices in one set of launches (no reference
+ * counterpart; the per-term gradients of a sampler log-likelihood).  Host
+ * form: A holds the matrices densely, count x n x n complex128; perms
+ * receives count x 2 doubles and grads count x n x n complex128.  A
+ * non-finite matrix gives NaN for its own outputs only.  Device form: matrix
+ * b starts at dA + b * stride complex elements (leading dimension ld). */
+int gbperm_perm_grad_batched(const double* A, int64_t n, int64_t count, double* perms, double* grads,
+                             gbperm_stats* stats);
+size_t gbperm_perm_grad_batched_workspace_size(int64_t n, int64_t count);
+int gbperm_perm_grad_batched_dev(const void* dA, int64_t n, int64_t count, int64_t ld, int64_t stride, void* d_perm,
+                                 void* d_grad, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------- allocation-free plain permanent */
 /* No counterpart in the reference.  The plain permanent for callers that

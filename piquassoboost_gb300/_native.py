@@ -86,11 +86,14 @@ _SIGNATURES = [
     ("gbperm_perm_grad", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P]),
     ("gbperm_perm_grad_workspace_size", ctypes.c_size_t, [_I64]),
     ("gbperm_perm_grad_dev", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    ("gbperm_perm_grad_batched", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P]),
+    ("gbperm_perm_grad_batched_workspace_size", ctypes.c_size_t, [_I64, _I64]),
+    ("gbperm_perm_grad_batched_dev", ctypes.c_int, [_P, _I64, _I64, _I64, _I64, _P, _P, _P, ctypes.c_size_t, _P]),
     ("gbperm_perm_noalloc", ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P]),
     ("gbperm_perm_noalloc_scratch_bytes", ctypes.c_size_t, []),
     ("gbperm_perm_repeated", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
-    ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P, _P]),
+    ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, ctypes.c_int, _P, _P, _P]),
 ]
 
 _lib = None
@@ -277,11 +280,12 @@ def perm_batched(matrices, mode="fp64", stats: Stats | None = None):
         plan.close()
 
 
-def compute_pmf(interferometer, sample, current_input, stats: Stats | None = None):
+def compute_pmf(interferometer, sample, current_input, mode="fp64", stats: Stats | None = None):
     """One probability layer of the Clifford & Clifford sampler on the GPU
     (gbperm_compute_pmf): returns (pmf, addends), pmf normalised to sum 1 over
     the m output modes and addends[l] the permanent with one photon removed
-    from input mode l (0 where the input mode is empty)."""
+    from input mode l (0 where the input mode is empty).  mode "fast" uses the
+    double-float product."""
     lib = load()
     u = as_matrix(interferometer)
     m = u.shape[0]
@@ -294,7 +298,7 @@ def compute_pmf(interferometer, sample, current_input, stats: Stats | None = Non
     pmf = np.zeros(m)
     add = np.zeros(m, dtype=np.complex128)
     check(lib.gbperm_compute_pmf(u.ctypes.data_as(_P), m, m, s.ctypes.data_as(_P), c.ctypes.data_as(_P),
-                                 pmf.ctypes.data_as(_P), add.ctypes.data_as(_P),
+                                 arith_of(mode), pmf.ctypes.data_as(_P), add.ctypes.data_as(_P),
                                  ctypes.byref(stats) if stats is not None else None))
     return pmf, add
 
@@ -319,3 +323,18 @@ def perm_grad(matrix, stats: Stats | None = None):
     check(lib.gbperm_perm_grad(a.ctypes.data_as(_P), n, n, perm.ctypes.data_as(_P), None,
                                g.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
     return complex(perm[0], perm[1]), g
+
+
+def perm_grad_batched(matrices, stats: Stats | None = None):
+    """Permanents and full gradients of a batch of equal-size square matrices
+    (host buffers, one set of launches): returns (perms[count], grads[count, n, n])."""
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(matrices), dtype=np.complex128)
+    if a.ndim != 3 or a.shape[1] != a.shape[2]:
+        raise ValueError("perm_grad_batched: a count x n x n stack of square matrices is required")
+    count, n = a.shape[0], a.shape[1]
+    perms = np.zeros(count, dtype=np.complex128)
+    grads = np.zeros((count, n, n), dtype=np.complex128)
+    check(lib.gbperm_perm_grad_batched(a.ctypes.data_as(_P), n, count, perms.ctypes.data_as(_P),
+                                       grads.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
+    return perms, grads

@@ -31,6 +31,11 @@ struct PrepArgs {
     int df;                  // 1: also decide the double-float range boost
     int* df_info;            // {o, ok}: boost and range-check result (ok = 0:
                              // the kernel must use the FP64 product)
+    // batch of equal-shape matrices, one block each: matrix b starts at
+    // A + b * a_stride and writes a1/a2 + b*rows*cols, exp_out + b,
+    // col_e_out + b*cols, df_info + 2b
+    int count = 1;
+    long long a_stride = 0;
 };
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st);
 

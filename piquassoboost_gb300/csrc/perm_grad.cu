@@ -34,6 +34,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "gbperm.h"
 #include "gbperm_capi_internal.h"
@@ -45,7 +47,8 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kGroup = 4;
 constexpr int kGroups = 32 / kGroup;  // walks per warp
-constexpr int kChunk = 1024;          // steps between folds of Q into G
+constexpr int kChunk = 4096;          // steps between folds of Q into G
+constexpr int kHot = 8;               // rows of G kept in shared memory (the 8 that flip most often)
 constexpr int kFinWarps = 64;         // warp tiles per partial of the first finalize stage
 
 __device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
@@ -88,119 +91,108 @@ __device__ __forceinline__ cf cf_scale_sign(const cf& a, unsigned int sbit) {
               __uint_as_float(__float_as_uint(a.ih) ^ sbit), __uint_as_float(__float_as_uint(a.il) ^ sbit)};
 }
 
+// One launch serves a batch of equal-size matrices: blockIdx.y is the
+// matrix, blockIdx.x the block within it; every per-matrix array is
+// consecutive in the matrix index.
 struct GradArgs {
-    const longlong2* a1;
+    const longlong2* a1;       // per matrix n x n
     const longlong2* a2;
     int n;
     int seg_log2;              // each walk covers 2^seg_log2 Gray steps
-    unsigned long long nseg;   // walks
-    const int* df_info;        // {boost, ok}
-    float4* warp_g;            // per warp: n x n complex double-float tiles (re_h, re_l, im_h, im_l)
-    float4* warp_p;            // per warp: permanent partial
+    unsigned long long nseg;   // walks per matrix
+    const int* df_info;        // per matrix {boost, ok}
+    float4* warp_g;            // per matrix and warp: n x n complex double-float tiles (re_h, re_l, im_h, im_l)
 };
 
-// Reduce-scatter of v[0..CPL) over the kGroups groups of a warp (lanes with
-// equal g): afterwards lane (g, grp) holds, in v[0], the sum over groups of
-// column g*CPL + (grp % CPL) (CPL <= kGroups).  The ownership pattern is
-// fixed: at each halving stage with mask m, the lane with (grp & m) keeps
-// the upper half.  The sums are lazily normalised pairs.
+// Reduce-scatter of v[0..CPL) over the kGroups walks of a warp (lanes with
+// equal g), without selects: every lane keeps the lower half of its
+// positions and receives its partner's upper half at each halving stage.
+// That adds the same column on both sides because lane (g, grp) stores its
+// columns in the order column = position ^ perm_mask<CPL>(grp): the partner
+// across stage bit m has the matching bit of the mask flipped, so its upper
+// positions hold this lane's lower-position columns.  Afterwards lane
+// (g, grp) holds, in v[0], the sum over walks of column g*CPL +
+// perm_mask<CPL>(grp); with CPL < kGroups the last stages are all-reduces.
+// The sums are lazily normalised pairs.
 template <int CPL>
-__device__ __forceinline__ cf reduce_scatter(cf (&v)[CPL], int grp) {
+__device__ __forceinline__ int perm_mask(int grp) {
+    // log2(kGroups / CPL) low bits of grp are all-reduce stages
+    return CPL == 8 ? grp : CPL == 4 ? (grp >> 1) : CPL == 2 ? (grp >> 2) : 0;
+}
+
+template <int CPL>
+__device__ __forceinline__ cf reduce_scatter(cf (&v)[CPL]) {
     int width = CPL;
 #pragma unroll
     for (int m = kGroups / 2; m >= 1; m >>= 1) {
         if (width > 1) {
             const int half = width / 2;
-            const bool upper = (grp & m) != 0;
 #pragma unroll
-            for (int c = 0; c < CPL / 2; ++c) {
-                if (c < half) {
-                    // send the half I drop, receive the matching half I keep
-                    cf send = upper ? v[c] : v[c + half];
-                    cf recv = shfl_xor_cf(send, m * kGroup);
-                    cf keep = upper ? v[c + half] : v[c];
-                    v[c] = cf_add_lazy(keep, recv);
-                }
-            }
+            for (int c = 0; c < CPL / 2; ++c)
+                if (c < half) v[c] = cf_add_lazy(v[c], shfl_xor_cf(v[c + half], m * kGroup));
             width = half;
         } else {
-            cf recv = shfl_xor_cf(v[0], m * kGroup);
-            v[0] = cf_add_lazy(v[0], recv);
+            v[0] = cf_add_lazy(v[0], shfl_xor_cf(v[0], m * kGroup));
         }
     }
     return v[0];
 }
 
-// Column owned by lane (g, grp) after reduce_scatter<CPL>.
 template <int CPL>
-__device__ __forceinline__ int scatter_col(int g, int grp) {
-    int width = CPL, base = 0;
-#pragma unroll
-    for (int m = kGroups / 2; m >= 1; m >>= 1) {
-        if (width > 1) {
-            const int half = width / 2;
-            if (grp & m) base += half;
-            width = half;
-        }
-    }
-    return g * CPL + base;
-}
-
-template <int CPL>
-__global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
+__global__ void __launch_bounds__(kThreads, 3) grad_kernel(GradArgs p) {
     constexpr int NP = CPL * kGroup;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);           // n x NP
-    longlong2* s_a2 = s_a1 + p.n * NP;                                  // n x NP
-    float4* s_g = reinterpret_cast<float4*>(s_a2 + p.n * NP);           // (warps) x n x NP
+    longlong2* s_a2 = reinterpret_cast<longlong2*>(smem_raw);           // n x NP (interleaved)
+    float4* s_g = reinterpret_cast<float4*>(s_a2 + p.n * NP);           // (warps) x kHot x NP
     const int n = p.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane % kGroup, grp = lane / kGroup;
     const int j0 = g * CPL;
-    float4* G = s_g + (size_t)warp * n * NP;
+    const size_t inst = blockIdx.y;
+    const longlong2* A1 = p.a1 + inst * n * n;
+    const longlong2* A2 = p.a2 + inst * n * n;
+    const int* dfi = p.df_info + 2 * inst;
+    // G: the kHot rows that flip most often (rows n-kHot .. n-1) live in a
+    // per-warp shared-memory tile; the other rows, which flip at most once
+    // every 2^kHot steps, accumulate straight into the warp's own tile in
+    // global memory (L2-resident), which is also the kernel's output.
+    const int hot0 = n > kHot ? n - kHot : 0;
+    float4* G = s_g + (size_t)warp * kHot * NP;
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (kThreads / 32);
+    const unsigned long long gwarp = (unsigned long long)blockIdx.x * (kThreads / 32) + warp;
+    const size_t slot = inst * warps_total + gwarp;
+    float4* outg = p.warp_g + slot * n * n;
+    // the step's row table, interleaved by lane: column j = g*CPL + c of row r
+    // sits at r*NP + c*kGroup + g, so the four lanes of a walk read four
+    // adjacent 16-byte words (one wavefront) when they fetch their c-th column
     for (int e = threadIdx.x; e < n * NP; e += blockDim.x) {
-        int r = e / NP, j = e % NP;
-        longlong2 z = make_longlong2(0, 0);
-        s_a1[e] = j < n ? p.a1[r * n + j] : z;
-        s_a2[e] = j < n ? p.a2[r * n + j] : z;
+        const int r = e / NP, q = e % NP;
+        const int j = (q % kGroup) * CPL + q / kGroup;
+        s_a2[e] = j < n ? A2[r * n + j] : make_longlong2(0, 0);
     }
-    for (int e = lane; e < n * NP; e += 32) G[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = lane; e < kHot * NP; e += 32) G[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = lane; e < hot0 * n; e += 32) outg[e] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    if (p.df_info[1] == 0) return;  // range check failed: finalize writes NaN
-    const DfConv cv = make_dfconv(p.df_info[0]);
-    const int my_col = scatter_col<CPL>(g, grp);
+    if (dfi[1] == 0) return;  // range check failed: finalize writes NaN
+    const DfConv cv = make_dfconv(dfi[0]);
+    // register position c of this lane holds column j0 + (c ^ pm)
+    const int pm = perm_mask<CPL>(grp);
+    const int my_col = j0 + pm;
     // with CPL < kGroups the last stages are all-reduces: one lane per column writes
     const bool writer = (grp & (kGroups / CPL - 1)) == 0 && my_col < n;
     const int L = p.seg_log2;
     const unsigned long long Lsteps = 1ull << L;
-    const unsigned long long warps_total = (unsigned long long)gridDim.x * (kThreads / 32);
-    const unsigned long long gwarp = (unsigned long long)blockIdx.x * (kThreads / 32) + warp;
-    const int lbase = lane - g;
     long long cre[CPL], cim[CPL];
     cf Q[CPL];
-    float prh = 0.f, prl = 0.f, pih = 0.f, pil = 0.f;  // permanent partial (group leader)
 
     auto g_add = [&](int r, const cf& s) {
         if (writer) {
-            float4 gg = G[r * NP + my_col];
+            float4* dst = r >= hot0 ? G + (r - hot0) * NP + my_col : outg + r * n + my_col;  // r warp-uniform
+            float4 gg = *dst;
             df_acc(gg.x, gg.y, s.rh, s.rl);
             df_acc(gg.z, gg.w, s.ih, s.il);
-            G[r * NP + my_col] = gg;
+            *dst = gg;
         }
-    };
-    // fold Q into every row of G: G[r] += delta_r * Q (the end term), then Q = 0
-    auto fold_all = [&](unsigned long long idx) {
-        const unsigned long long gray = idx ^ (idx >> 1);
-        for (int r = 0; r < n; ++r) {
-            // delta_r = -1 when bit (n-1-r) of the Gray code is set (row 0: +1)
-            const bool neg = r > 0 && ((gray >> (n - 1 - r)) & 1ull);
-            cf v[CPL];
-#pragma unroll
-            for (int c = 0; c < CPL; ++c) v[c] = cf_scale_sign(Q[c], neg ? 0x80000000u : 0u);
-            g_add(r, reduce_scatter<CPL>(v, grp));
-        }
-#pragma unroll
-        for (int c = 0; c < CPL; ++c) Q[c] = cf{0.f, 0.f, 0.f, 0.f};
     };
 
     for (unsigned long long wb = gwarp * kGroups; wb < p.nseg; wb += warps_total * kGroups) {
@@ -208,18 +200,22 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
         const bool active = s_raw < p.nseg;
         const unsigned long long i0 = (active ? s_raw : 0ull) << L;
         const unsigned long long g0 = i0 ^ (i0 >> 1);
+        // walk-start column sums from the fixed-point matrix in global
+        // memory (once per walk): row 0 plus rows 1.. with their signs
 #pragma unroll
         for (int c = 0; c < CPL; ++c) {
-            cre[c] = s_a1[j0 + c].x;
-            cim[c] = s_a1[j0 + c].y;
+            const int j = j0 + (c ^ pm);
+            const longlong2 v = j < n ? A1[j] : make_longlong2(0, 0);
+            cre[c] = v.x;
+            cim[c] = v.y;
             Q[c] = cf{0.f, 0.f, 0.f, 0.f};
         }
         for (int r = 1; r < n; ++r) {
             const long long m = -(long long)((g0 >> (n - 1 - r)) & 1ull);
-            const longlong2* a = s_a1 + r * NP + j0;
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
-                longlong2 v = a[c];
+                const int j = j0 + (c ^ pm);
+                const longlong2 v = j < n ? A1[r * n + j] : make_longlong2(0, 0);
                 cre[c] += (v.x ^ m) - m;
                 cim[c] += (v.y ^ m) - m;
             }
@@ -227,152 +223,139 @@ __global__ void __launch_bounds__(kThreads) grad_kernel(GradArgs p) {
         unsigned int sbit = (unsigned int)(__popcll(g0) & 1) << 31;
         // inactive walks (past the end of the range) carry weight 0
         const float wgt = active ? 1.f : 0.f;
-        for (unsigned long long k = 0; k < Lsteps; ++k) {
-            const unsigned long long idx = i0 + k;
-            if (k != 0) {
-                const int b = __ffsll((long long)k) - 1;                  // warp-uniform
-                const int r = n - 1 - b;                                    // the row that flips
-                const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;  // new delta_r = -1
-                if ((k % kChunk) == 0) {
-                    // chunk boundary: end term at idx-1 for every row, Q = 0;
-                    // the flip term of this step would then add 2 * 0
-                    fold_all(idx - 1);
-                } else if (b + 1 < L) {
-                    // flip term G[r] += 2 delta_r(k-1) Q(k-1), delta_r(k-1) = +1
-                    // when the row now turns -1; bits b, b+1 of idx are bits
-                    // of k here, so the sign is the same for all walks
+        for (unsigned long long k0 = 0; k0 < Lsteps; k0 += kChunk) {
+            const unsigned long long kend = k0 + kChunk < Lsteps ? k0 + kChunk : Lsteps;
+            for (unsigned long long k = k0; k < kend; ++k) {
+                const unsigned long long idx = i0 + k;
+                if (k != 0) {
+                    const int b = __ffsll((long long)k) - 1;                  // warp-uniform
+                    const int r = n - 1 - b;                                    // the row that flips
+                    const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;  // new delta_r = -1
+                    // flip term G[r] += 2 delta_r(k-1) Q(k-1), delta_r(k-1) = +1 when
+                    // the row now turns -1 (Q is zero right after a fold).  Bits b,
+                    // b+1 of idx are bits of k unless b is the walk's top bit, so the
+                    // sign is the same for all walks and is applied after the
+                    // reduction; at the middle step it is applied per walk before.
+                    const bool mid = b + 1 >= L;
                     cf v[CPL];
 #pragma unroll
                     for (int c = 0; c < CPL; ++c) v[c] = Q[c];
-                    cf s = reduce_scatter<CPL>(v, grp);
-                    const float f = sub ? 2.f : -2.f;
+                    if (mid) {
+#pragma unroll
+                        for (int c = 0; c < CPL; ++c) {
+                            cf q = v[c];
+                            q.rh = __fmul_rn(q.rh, 2.f);
+                            q.rl = __fmul_rn(q.rl, 2.f);
+                            q.ih = __fmul_rn(q.ih, 2.f);
+                            q.il = __fmul_rn(q.il, 2.f);
+                            v[c] = cf_scale_sign(q, sub ? 0u : 0x80000000u);
+                        }
+                    }
+                    cf s = reduce_scatter<CPL>(v);
+                    const float f = mid ? 1.f : (sub ? 2.f : -2.f);
                     s.rh = __fmul_rn(s.rh, f);
                     s.rl = __fmul_rn(s.rl, f);
                     s.ih = __fmul_rn(s.ih, f);
                     s.il = __fmul_rn(s.il, f);
                     g_add(r, s);
-                } else {
-                    // middle step of the walk: the sign depends on the walk
-                    cf v[CPL];
+                    // column sums: -/+ 2 a_r
+                    const long long m = sub ? -1ll : 0ll;
+                    const longlong2* a = s_a2 + r * NP + g;
 #pragma unroll
                     for (int c = 0; c < CPL; ++c) {
-                        cf q = Q[c];
-                        q.rh = __fmul_rn(q.rh, 2.f);
-                        q.rl = __fmul_rn(q.rl, 2.f);
-                        q.ih = __fmul_rn(q.ih, 2.f);
-                        q.il = __fmul_rn(q.il, 2.f);
-                        v[c] = cf_scale_sign(q, sub ? 0u : 0x80000000u);
+                        longlong2 v2 = a[(c ^ pm) * kGroup];
+                        cre[c] += (v2.x ^ m) - m;
+                        cim[c] += (v2.y ^ m) - m;
                     }
-                    g_add(r, reduce_scatter<CPL>(v, grp));
+                    sbit ^= 0x80000000u;
                 }
-                const longlong2* a = s_a2 + r * NP + j0;
-                if (sub) {
-#pragma unroll
-                    for (int c = 0; c < CPL; ++c) {
-                        longlong2 v = a[c];
-                        cre[c] -= v.x;
-                        cim[c] -= v.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < CPL; ++c) {
-                        longlong2 v = a[c];
-                        cre[c] += v.x;
-                        cim[c] += v.y;
-                    }
-                }
-                sbit ^= 0x80000000u;
-            }
-            // column values (padded columns act as 1)
-            cf x[CPL];
-#pragma unroll
-            for (int c = 0; c < CPL; ++c) {
-                if (j0 + c < n) {
-                    fix_to_df_magic(cre[c], cv, x[c].rh, x[c].rl);
-                    fix_to_df_magic(cim[c], cv, x[c].ih, x[c].il);
-                } else {
-                    x[c] = cf{1.f, 0.f, 0.f, 0.f};
-                }
-            }
-            // prefix products pre[c] = prod_{c' < c} x_c' (pre[0] = 1 is implicit);
-            // the last one times x[CPL-1] is the lane's partial product
-            cf pre[CPL];
-            cf part = x[0];
-            if (CPL > 1) {
-                pre[1] = x[0];
-#pragma unroll
-                for (int c = 2; c < CPL; ++c) pre[c] = cf_mul(pre[c - 1], x[c - 1]);
-                part = cf_mul(pre[CPL - 1], x[CPL - 1]);
-            }
-            // product of the other three lanes' partials (gathered in the group)
-            cf o1 = shfl_cf(part, lbase + ((g + 1) & 3));
-            cf o2 = shfl_cf(part, lbase + ((g + 2) & 3));
-            cf o3 = shfl_cf(part, lbase + ((g + 3) & 3));
-            cf seed = cf_scale_sign(cf_mul(cf_mul(o1, o2), o3), sbit);  // s(delta) folded in once
-            seed.rh = __fmul_rn(seed.rh, wgt);
-            seed.rl = __fmul_rn(seed.rl, wgt);
-            seed.ih = __fmul_rn(seed.ih, wgt);
-            seed.il = __fmul_rn(seed.il, wgt);
-            // permanent term (leader)
-            if (g == 0) {
-                cf t = cf_mul(seed, part);
-                df_add_lazy(prh, prl, t.rh, t.rl);
-                df_add_lazy(pih, pil, t.ih, t.il);
-            }
-            // W_c = seed * prod_{c' > c} x_c' * pre[c]
-            cf suf = seed;
-#pragma unroll
-            for (int c = CPL - 1; c >= 0; --c) {
-                cf w = (c == 0) ? suf : cf_mul(pre[c], suf);
-                Q[c] = cf_add_lazy(Q[c], w);
-                if (c > 0) suf = cf_mul(suf, x[c]);
-            }
-            if ((k & 7ull) == 7ull) {
+                // column values (padded columns act as 1)
+                cf x[CPL];
 #pragma unroll
                 for (int c = 0; c < CPL; ++c) {
-                    df_renorm(Q[c].rh, Q[c].rl);
-                    df_renorm(Q[c].ih, Q[c].il);
+                    if (j0 + (c ^ pm) < n) {
+                        fix_to_df_magic(cre[c], cv, x[c].rh, x[c].rl);
+                        fix_to_df_magic(cim[c], cv, x[c].ih, x[c].il);
+                    } else {
+                        x[c] = cf{1.f, 0.f, 0.f, 0.f};
+                    }
                 }
-                df_renorm(prh, prl);
-                df_renorm(pih, pil);
+                // prefix products pre[c] = prod_{c' < c} x_c' (pre[0] = 1 is implicit);
+                // the last one times x[CPL-1] is the lane's partial product
+                cf pre[CPL];
+                cf part = x[0];
+                if (CPL > 1) {
+                    pre[1] = x[0];
+#pragma unroll
+                    for (int c = 2; c < CPL; ++c) pre[c] = cf_mul(pre[c - 1], x[c - 1]);
+                    part = cf_mul(pre[CPL - 1], x[CPL - 1]);
+                }
+                // product of the other three lanes' partials: the partner's
+                // partial (lane g^1) times the other pair's product (g^2, g^3)
+                const cf o1 = shfl_xor_cf(part, 1);
+                const cf pair = cf_mul(part, o1);
+                const cf o23 = shfl_xor_cf(pair, 2);
+                cf seed = cf_scale_sign(cf_mul(o1, o23), sbit);  // s(delta) folded in once
+                seed.rh = __fmul_rn(seed.rh, wgt);
+                seed.rl = __fmul_rn(seed.rl, wgt);
+                seed.ih = __fmul_rn(seed.ih, wgt);
+                seed.il = __fmul_rn(seed.il, wgt);
+                // W_c = seed * prod_{c' > c} x_c' * pre[c]
+                cf suf = seed;
+#pragma unroll
+                for (int c = CPL - 1; c >= 0; --c) {
+                    cf w = (c == 0) ? suf : cf_mul(pre[c], suf);
+                    Q[c] = cf_add_lazy(Q[c], w);
+                    if (c > 0) suf = cf_mul(suf, x[c]);
+                }
+                if ((k & 7ull) == 7ull) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        df_renorm(Q[c].rh, Q[c].rl);
+                        df_renorm(Q[c].ih, Q[c].il);
+                    }
+                }
             }
+            // end of a chunk (or of the walk): fold Q into every row of G,
+            // G[r] += delta_r(kend-1) * Q, then restart Q
+            const unsigned long long idx = i0 + kend - 1;
+            const unsigned long long gray = idx ^ (idx >> 1);
+            for (int r = 0; r < n; ++r) {
+                // delta_r = -1 when bit (n-1-r) of the Gray code is set (row 0: +1)
+                const bool neg = r > 0 && ((gray >> (n - 1 - r)) & 1ull);
+                cf v[CPL];
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) v[c] = cf_scale_sign(Q[c], neg ? 0x80000000u : 0u);
+                g_add(r, reduce_scatter<CPL>(v));
+            }
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) Q[c] = cf{0.f, 0.f, 0.f, 0.f};
         }
-        // end term of the walk
-        fold_all(i0 + Lsteps - 1);
     }
     __syncwarp();
-    // write the warp's G tile and permanent partial
-    float4* outg = p.warp_g + (size_t)gwarp * n * n;
-    for (int e = lane; e < n * n; e += 32) {
-        int r = e / n, j = e % n;
-        outg[e] = G[r * NP + j];
+    // the hot rows of the warp's tile go to its global tile (the other rows
+    // are there already)
+    for (int e = lane; e < (n - hot0) * n; e += 32) {
+        const int rr = e / n, j = e % n;
+        outg[(hot0 + rr) * n + j] = G[rr * NP + j];
     }
-    // permanent: sum the 8 leaders' partials
-    df_renorm(prh, prl);
-    df_renorm(pih, pil);
-    cf pp{prh, prl, pih, pil};
-#pragma unroll
-    for (int m = kGroup; m < 32; m <<= 1) {
-        cf o = shfl_xor_cf(pp, m);
-        df_acc(pp.rh, pp.rl, o.rh, o.rl);
-        df_acc(pp.ih, pp.il, o.ih, o.il);
-    }
-    if (lane == 0) p.warp_p[gwarp] = make_float4(pp.rh, pp.rl, pp.ih, pp.il);
 }
 
-// First finalize stage: element e < n*n of the gradient (e == n*n: the
-// permanent) summed over kFinWarps consecutive warp tiles, in double-float,
-// one partial per (chunk, element).  Every SM takes part.
-__global__ void grad_partial_kernel(const float4* warp_g, const float4* warp_p, int nwarps, int n,
-                                    float4* part) {
-    const int ne = n * n + 1;
+// First finalize stage: element e of the gradient summed over kFinWarps
+// consecutive warp tiles, in double-float, one partial per (chunk, element).
+// Every SM takes part.
+__global__ void grad_partial_kernel(const float4* warp_g, int nwarps, int n, float4* part) {
+    const int ne = n * n;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
+    const size_t inst = blockIdx.z;  // matrix of a batch
+    warp_g += inst * nwarps * n * n;
+    part += inst * gridDim.y * ne;
     const int w0 = blockIdx.y * kFinWarps;
     const int w1 = min(w0 + kFinWarps, nwarps);
     float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
     for (int w = w0; w < w1; ++w) {
-        const float4 v = e < n * n ? warp_g[(size_t)w * n * n + e] : warp_p[w];
+        const float4 v = warp_g[(size_t)w * n * n + e];
         df_acc(rh, rl, v.x, v.y);
         df_acc(ih, il, v.z, v.w);
     }
@@ -380,19 +363,20 @@ __global__ void grad_partial_kernel(const float4* warp_g, const float4* warp_p, 
 }
 
 // Second stage: sum the chunk partials in a fixed order in double-double,
-// scale, write the gradient (complex128, n x n row-major) and the permanent.
+// scale, write the gradient (complex128, n x n row-major).
 __global__ void grad_finalize_kernel(const float4* part, int nchunks, int n, const int* exp_in, const int* col_e,
-                                     const int* df_info, double* grad, double* perm2, double* perm4) {
-    const int ne = n * n + 1;
+                                     const int* df_info, double* grad) {
+    const int ne = n * n;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
+    const size_t inst = blockIdx.y;  // matrix of a batch
+    part += inst * nchunks * ne;
+    exp_in += inst;
+    col_e += inst * n;
+    df_info += 2 * inst;
+    grad += inst * 2 * n * n;
     if (df_info[1] == 0) {
-        if (e < n * n) {
-            grad[2 * e] = grad[2 * e + 1] = nan("");
-        } else {
-            perm2[0] = perm2[1] = nan("");
-            if (perm4) perm4[0] = perm4[1] = perm4[2] = perm4[3] = nan("");
-        }
+        grad[2 * e] = grad[2 * e + 1] = nan("");
         return;
     }
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
@@ -401,38 +385,103 @@ __global__ void grad_finalize_kernel(const float4* part, int nchunks, int n, con
         acc.re = dd_add(acc.re, dd{(double)v.x, (double)v.y});
         acc.im = dd_add(acc.im, dd{(double)v.z, (double)v.w});
     }
-    if (e < n * n) {
-        const int l = e % n;
-        // W_l omits column l: remove its factor from the permanent's scale
-        const int ex = *exp_in - (col_e[l] - df_info[0]);
-        double r2[2];
-        write_result(acc, ex, r2, nullptr);
-        grad[2 * e] = r2[0];
-        grad[2 * e + 1] = r2[1];
-    } else {
-        write_result(acc, *exp_in, perm2, perm4);
+    const int l = e % n;
+    // W_l omits column l: remove its factor from the permanent's scale
+    const int ex = *exp_in - (col_e[l] - df_info[0]);
+    double r2[2];
+    write_result(acc, ex, r2, nullptr);
+    grad[2 * e] = r2[0];
+    grad[2 * e + 1] = r2[1];
+}
+
+__device__ __forceinline__ dd two_prod(double a, double b) {
+    const double p = a * b;
+    return dd{p, fma(a, b, -p)};
+}
+
+// The permanent from its gradient: perm is linear in every row, so
+// perm = sum_l a_kl dperm/da_kl for each row k (Laplace expansion along k).
+// One warp per matrix, lane k evaluates row k's sum in double-double
+// (products exact by FMA) and its condition sum_l |a_kl| |G_kl| / |sum|; the
+// best-conditioned row gives the result, so the sweep needs no separate
+// permanent term.
+__global__ void grad_perm_kernel(const double2* A, long long ld, long long stride, int n, const double* grad,
+                                 const int* df_info, double* perm2, double* perm4) {
+    const size_t inst = blockIdx.x;
+    const int k = threadIdx.x;
+    A += inst * stride;
+    grad += inst * 2 * n * n;
+    df_info += 2 * inst;
+    perm2 += 2 * inst;
+    if (perm4) perm4 += 4 * inst;
+    if (df_info[1] == 0) {
+        if (k == 0) {
+            perm2[0] = perm2[1] = nan("");
+            if (perm4) perm4[0] = perm4[1] = perm4[2] = perm4[3] = nan("");
+        }
+        return;
+    }
+    cdd s{{0.0, 0.0}, {0.0, 0.0}};
+    double mag = 0.0;
+    if (k < n) {
+        for (int l = 0; l < n; ++l) {
+            const double2 a = A[(long long)k * ld + l];
+            const double gr = grad[2 * (k * n + l)], gi = grad[2 * (k * n + l) + 1];
+            s.re = dd_add(s.re, two_prod(a.x, gr));
+            s.re = dd_add(s.re, two_prod(-a.y, gi));
+            s.im = dd_add(s.im, two_prod(a.x, gi));
+            s.im = dd_add(s.im, two_prod(a.y, gr));
+            mag += hypot(a.x, a.y) * hypot(gr, gi);
+        }
+    }
+    const double absv = hypot(s.re.hi, s.im.hi);
+    double cond = k < n ? (absv > 0.0 ? mag / absv : (mag > 0.0 ? INFINITY : 1.0)) : INFINITY;
+    int best = k;
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        const double oc = __shfl_xor_sync(0xffffffffu, cond, m);
+        const int ob = __shfl_xor_sync(0xffffffffu, best, m);
+        if (oc < cond || (oc == cond && ob < best)) {
+            cond = oc;
+            best = ob;
+        }
+    }
+    if (k == best) {
+        perm2[0] = s.re.hi + s.re.lo;
+        perm2[1] = s.im.hi + s.im.lo;
+        if (perm4) {
+            perm4[0] = s.re.hi;
+            perm4[1] = s.im.hi;
+            perm4[2] = s.re.lo;
+            perm4[3] = s.im.lo;
+        }
     }
 }
 
 template <int CPL>
 size_t grad_smem(int n) {
-    return 2ull * n * CPL * kGroup * sizeof(longlong2) + (size_t)(kThreads / 32) * n * CPL * kGroup * sizeof(float4);
+    return (size_t)n * CPL * kGroup * sizeof(longlong2) + (size_t)(kThreads / 32) * kHot * CPL * kGroup * sizeof(float4);
 }
 
 }  // namespace
 
 struct GradPlan {
     int cpl = 8;
-    int grid = 1;
+    int grid = 1;      // blocks per matrix
     int seg_log2 = 0;
     unsigned long long nseg = 1;
-    int nwarps = 1;
-    int nchunks = 1;  // partials of the first finalize stage
+    int nwarps = 1;    // warps per matrix
+    int nchunks = 1;   // partials per matrix in the first finalize stage
+    int count = 1;     // matrices in one launch
 };
 
-static GradPlan plan_grad(int n) {
+// Largest batch one launch takes (gridDim.y); larger batches are cut.
+constexpr int kMaxBatchLaunch = 65535;
+
+static GradPlan plan_grad(int n, int count) {
     GradPlan gp;
     gp.cpl = n <= 16 ? 4 : 8;
+    gp.count = count;
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = device_sms(dev);
@@ -446,103 +495,135 @@ static GradPlan plan_grad(int n) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, grad_kernel<8>, kThreads, smem);
     }
     if (nb < 1) nb = 1;
-    const int grid_full = sms * nb;
+    const long long grid_full = (long long)sms * nb;
+    const long long gx_max = std::max(1ll, grid_full / std::max(1, count));
     const int slog = n - 1;
-    // walk length 2^l: the walks are dealt to the resident walk slots in
-    // passes, so the time goes as passes x (2^l + per-walk cost), the
-    // per-walk cost (start-up and the final fold of n rows) being about
-    // 0.2 n + 16 steps.  Ties go to the longer walk.
-    const unsigned long long slots = (unsigned long long)grid_full * (kThreads / 32) * kGroups;
+    // walk length 2^l: a matrix's walks are dealt to its blocks' walk slots
+    // in passes, and the matrices' blocks fill the GPU in waves, so the time
+    // goes as waves x passes x (2^l + per-walk cost), the per-walk cost
+    // (start-up and the final fold of n rows) being about 0.2 n + 16 steps.
+    // Ties go to the longer walk.
     double best = 1e300;
     int best_l = slog;
+    long long best_gx = 1;
     for (int l = slog; l >= 0; --l) {
         const unsigned long long nseg = 1ull << (slog - l);
+        const unsigned long long blocks_needed = ((nseg + kGroups - 1) / kGroups + 3) / 4;
+        const long long gx = std::max(1ll, std::min(gx_max, (long long)blocks_needed));
+        const unsigned long long slots = (unsigned long long)gx * (kThreads / 32) * kGroups;
         const double passes = (double)((nseg + slots - 1) / slots);
-        const double cost = passes * (std::ldexp(1.0, l) + 0.2 * n + 16.0);
+        const double waves = std::ceil((double)count * (double)gx / (double)grid_full);
+        const double cost = waves * passes * (std::ldexp(1.0, l) + 0.2 * n + 16.0);
         if (cost < best * (1.0 - 1e-9)) {
             best = cost;
             best_l = l;
+            best_gx = gx;
         }
     }
     gp.seg_log2 = best_l;
     gp.nseg = 1ull << (slog - best_l);
-    unsigned long long warps_needed = (gp.nseg + kGroups - 1) / kGroups;
-    unsigned long long blocks_needed = (warps_needed + 3) / 4;
-    gp.grid = (int)(blocks_needed < (unsigned long long)grid_full ? blocks_needed : (unsigned long long)grid_full);
-    if (gp.grid < 1) gp.grid = 1;
+    gp.grid = (int)best_gx;
     gp.nwarps = gp.grid * (kThreads / 32);
     gp.nchunks = (gp.nwarps + kFinWarps - 1) / kFinWarps;
     return gp;
 }
 
-static size_t grad_ws_bytes(int n, const GradPlan& gp) {
-    size_t mat = align_up((size_t)n * n * sizeof(longlong2), 256);
-    return 2 * mat + 256 + 256 + align_up((size_t)n * sizeof(int), 256) +
-           align_up((size_t)gp.nwarps * n * n * sizeof(float4), 256) + align_up((size_t)gp.nwarps * sizeof(float4), 256) +
-           align_up((size_t)gp.nchunks * (n * n + 1) * sizeof(float4), 256);
+struct GradWs {
+    size_t a1, a2, exp, dfi, cole, warp_g, part, total;
+};
+
+static GradWs grad_ws_layout(int n, const GradPlan& gp) {
+    GradWs w;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += align_up(bytes, 256);
+        return o;
+    };
+    const size_t c = (size_t)gp.count;
+    w.a1 = take(c * n * n * sizeof(longlong2));
+    w.a2 = take(c * n * n * sizeof(longlong2));
+    w.exp = take(c * sizeof(int));
+    w.dfi = take(c * 2 * sizeof(int));
+    w.cole = take(c * n * sizeof(int));
+    w.warp_g = take(c * gp.nwarps * n * n * sizeof(float4));
+    w.part = take(c * gp.nchunks * n * n * sizeof(float4));
+    w.total = off;
+    return w;
 }
 
-// Device-side gradient: dA (n x n complex128, ld), grad out (n x n complex128
-// row-major), perm out (2 doubles) and optional perm dd (4 doubles).
-static int run_grad_dev(const double2* dA, long long ld, int n, void* ws, size_t ws_bytes, double* d_grad,
-                        double* d_perm, double* d_perm4, cudaStream_t st, GradPlan* used) {
-    GradPlan gp = plan_grad(n);
-    if (used) *used = gp;
-    if (ws_bytes < grad_ws_bytes(n, gp)) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad: workspace too small");
-    char* base = static_cast<char*>(ws);
-    size_t mat = align_up((size_t)n * n * sizeof(longlong2), 256);
-    size_t off = 0;
-    longlong2* a1 = reinterpret_cast<longlong2*>(base + off);
-    off += mat;
-    longlong2* a2 = reinterpret_cast<longlong2*>(base + off);
-    off += mat;
-    int* exp_out = reinterpret_cast<int*>(base + off);
-    off += 256;
-    int* df_info = reinterpret_cast<int*>(base + off);
-    off += 256;
-    int* col_e = reinterpret_cast<int*>(base + off);
-    off += align_up((size_t)n * sizeof(int), 256);
-    float4* warp_g = reinterpret_cast<float4*>(base + off);
-    off += align_up((size_t)gp.nwarps * n * n * sizeof(float4), 256);
-    float4* warp_p = reinterpret_cast<float4*>(base + off);
-    off += align_up((size_t)gp.nwarps * sizeof(float4), 256);
-    float4* fin_part = reinterpret_cast<float4*>(base + off);
-    PrepArgs pa;
-    pa.col_e_out = col_e;
-    pa.A = dA;
-    pa.ld = ld;
-    pa.rows = n;
-    pa.cols = n;
-    pa.row_w = nullptr;
-    pa.col_w = nullptr;
-    pa.norm_shift = n - 1;
-    pa.a1 = a1;
-    pa.a2 = a2;
-    pa.exp_out = exp_out;
-    pa.df = 1;
-    pa.df_info = df_info;
-    cudaError_t e = launch_prepare(pa, st);
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: prepare");
-    GradArgs g;
-    g.a1 = a1;
-    g.a2 = a2;
-    g.n = n;
-    g.seg_log2 = gp.seg_log2;
-    g.nseg = gp.nseg;
-    g.df_info = df_info;
-    g.warp_g = warp_g;
-    g.warp_p = warp_p;
-    if (gp.cpl == 4) grad_kernel<4><<<gp.grid, kThreads, grad_smem<4>(n), st>>>(g);
-    else grad_kernel<8><<<gp.grid, kThreads, grad_smem<8>(n), st>>>(g);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: kernel");
-    // the boost is read on the device by the finalize kernel via df_info
-    const int ne = n * n + 1;
-    grad_partial_kernel<<<dim3((ne + 127) / 128, gp.nchunks), 128, 0, st>>>(warp_g, warp_p, gp.nwarps, n, fin_part);
-    grad_finalize_kernel<<<(ne + 127) / 128, 128, 0, st>>>(fin_part, gp.nchunks, n, exp_out, col_e, df_info, d_grad,
-                                                          d_perm, d_perm4);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: finalize");
+static size_t grad_ws_bytes(int n, int count) {
+    size_t most = 256;
+    for (int done = 0; done < count; done += kMaxBatchLaunch) {
+        const int c = std::min(kMaxBatchLaunch, count - done);
+        most = std::max(most, grad_ws_layout(n, plan_grad(n, c)).total);
+        if (count > kMaxBatchLaunch) break;  // all full launches have the same layout; the last is smaller
+    }
+    return most;
+}
+
+// Device-side gradient of `count` matrices: matrix b is dA + b * stride
+// (n x n complex128, leading dimension ld); grad out count x n x n complex128
+// row-major, perm out count x 2 doubles, optional perm dd count x 4 doubles.
+static int run_grad_dev(const double2* dA, long long ld, long long stride, int n, int count, void* ws,
+                        size_t ws_bytes, double* d_grad, double* d_perm, double* d_perm4, cudaStream_t st,
+                        GradPlan* used) {
+    for (int done = 0; done < count; done += kMaxBatchLaunch) {
+        const int c = std::min(kMaxBatchLaunch, count - done);
+        GradPlan gp = plan_grad(n, c);
+        if (used) *used = gp;
+        const GradWs w = grad_ws_layout(n, gp);
+        if (ws_bytes < w.total) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad: workspace too small");
+        char* base = static_cast<char*>(ws);
+        longlong2* a1 = reinterpret_cast<longlong2*>(base + w.a1);
+        longlong2* a2 = reinterpret_cast<longlong2*>(base + w.a2);
+        int* exp_out = reinterpret_cast<int*>(base + w.exp);
+        int* df_info = reinterpret_cast<int*>(base + w.dfi);
+        int* col_e = reinterpret_cast<int*>(base + w.cole);
+        float4* warp_g = reinterpret_cast<float4*>(base + w.warp_g);
+        float4* fin_part = reinterpret_cast<float4*>(base + w.part);
+        PrepArgs pa;
+        pa.col_e_out = col_e;
+        pa.A = dA + (long long)done * stride;
+        pa.ld = ld;
+        pa.rows = n;
+        pa.cols = n;
+        pa.row_w = nullptr;
+        pa.col_w = nullptr;
+        pa.norm_shift = n - 1;
+        pa.a1 = a1;
+        pa.a2 = a2;
+        pa.exp_out = exp_out;
+        pa.df = 1;
+        pa.df_info = df_info;
+        pa.count = c;
+        pa.a_stride = stride;
+        cudaError_t e = launch_prepare(pa, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: prepare");
+        GradArgs g;
+        g.a1 = a1;
+        g.a2 = a2;
+        g.n = n;
+        g.seg_log2 = gp.seg_log2;
+        g.nseg = gp.nseg;
+        g.df_info = df_info;
+        g.warp_g = warp_g;
+        const dim3 grid(gp.grid, c);
+        if (gp.cpl == 4) grad_kernel<4><<<grid, kThreads, grad_smem<4>(n), st>>>(g);
+        else grad_kernel<8><<<grid, kThreads, grad_smem<8>(n), st>>>(g);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: kernel");
+        // the boost is read on the device by the finalize kernel via df_info
+        const int ne = n * n;
+        grad_partial_kernel<<<dim3((ne + 127) / 128, gp.nchunks, c), 128, 0, st>>>(warp_g, gp.nwarps, n, fin_part);
+        double* gout = d_grad + (size_t)done * 2 * n * n;
+        grad_finalize_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(fin_part, gp.nchunks, n, exp_out, col_e,
+                                                                        df_info, gout);
+        grad_perm_kernel<<<c, 32, 0, st>>>(dA + (long long)done * stride, ld, stride, n, gout, df_info,
+                                           d_perm + (size_t)done * 2, d_perm4 ? d_perm4 + (size_t)done * 4 : nullptr);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: finalize");
+    }
     return GBPERM_OK;
 }
 
@@ -554,7 +635,12 @@ extern "C" {
 
 size_t gbperm_perm_grad_workspace_size(int64_t n) {
     if (n <= 0 || n > 32) return 256;
-    return grad_ws_bytes((int)n, plan_grad((int)n));
+    return grad_ws_bytes((int)n, 1);
+}
+
+size_t gbperm_perm_grad_batched_workspace_size(int64_t n, int64_t count) {
+    if (n <= 0 || n > 32 || count <= 0 || count > INT32_MAX) return 256;
+    return grad_ws_bytes((int)n, (int)count);
 }
 
 int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, void* d_perm_dd, void* d_grad,
@@ -564,64 +650,111 @@ int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, vo
     if (ld < n) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_dev: ld < n");
     if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_dev: workspace must be 256-byte aligned");
-    return run_grad_dev(static_cast<const double2*>(dA), ld, (int)n, workspace, workspace_bytes,
+    return run_grad_dev(static_cast<const double2*>(dA), ld, 0, (int)n, 1, workspace, workspace_bytes,
                         static_cast<double*>(d_grad), static_cast<double*>(d_perm), static_cast<double*>(d_perm_dd),
                         static_cast<cudaStream_t>(stream), nullptr);
 }
 
-int gbperm_perm_grad(const double* A, int64_t n, int64_t ld, double* perm, double* perm_dd, double* grad,
-                     gbperm_stats* stats) {
+int gbperm_perm_grad_batched_dev(const void* dA, int64_t n, int64_t count, int64_t ld, int64_t stride, void* d_perm,
+                                 void* d_grad, void* workspace, size_t workspace_bytes, void* stream) {
+    if (n < 1 || n > 32) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_grad_batched: n must be in 1..32");
+    if (count < 0 || count > INT32_MAX) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_batched: bad count");
+    if (count == 0) return GBPERM_OK;
+    if (!dA || !d_perm || !d_grad || !workspace)
+        return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_batched_dev: null pointer");
+    if (ld < n || stride < n * ld) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_batched_dev: ld < n or stride < n ld");
+    if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+        return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_batched_dev: workspace must be 256-byte aligned");
+    return run_grad_dev(static_cast<const double2*>(dA), ld, stride, (int)n, (int)count, workspace, workspace_bytes,
+                        static_cast<double*>(d_grad), static_cast<double*>(d_perm), nullptr,
+                        static_cast<cudaStream_t>(stream), nullptr);
+}
+
+// Host-buffer form shared by the single and batched entry points: count
+// dense n x n matrices (matrix b at A + 2 b stride doubles, leading
+// dimension ld), perms count x 2, grads count x n x n complex128.
+static int perm_grad_host(const double* A, int64_t n, int64_t count, int64_t ld, int64_t stride, double* perms,
+                          double* perm_dd, double* grads, gbperm_stats* stats, const char* who) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
-    if (!perm || !grad) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad: null output");
-    if (n < 1 || n > 32) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_grad: n must be in 1..32");
-    if (!A || ld < n) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad: bad matrix");
-    if (!all_finite(A, n, n, ld)) {
-        perm[0] = perm[1] = NAN;
-        for (int64_t e = 0; e < 2 * n * n; ++e) grad[e] = NAN;
-        return GBPERM_OK;
+    if (!perms || !grads) return fail(GBPERM_ERR_ARG, std::string(who) + ": null output");
+    if (n < 1 || n > 32) return fail(GBPERM_ERR_TOO_LARGE, std::string(who) + ": n must be in 1..32");
+    if (count < 0 || count > INT32_MAX) return fail(GBPERM_ERR_ARG, std::string(who) + ": bad count");
+    if (count == 0) return GBPERM_OK;
+    if (!A || ld < n || stride < n * ld) return fail(GBPERM_ERR_ARG, std::string(who) + ": bad matrix");
+    for (int64_t b = 0; b < count; ++b) {
+        const double* Ab = A + 2 * b * stride;
+        if (!all_finite(Ab, n, n, ld)) continue;  // NaN out, below
+        int boost = 0;
+        if (!df_boost(Ab, n, n, ld, nullptr, nullptr, &boost))
+            return fail(GBPERM_ERR_TOO_LARGE,
+                        std::string(who) + ": matrix dynamic range beyond the double-float product");
     }
-    int boost = 0;
-    if (!df_boost(A, n, n, ld, nullptr, nullptr, &boost))
-        return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_grad: matrix dynamic range beyond the double-float product");
-    GradPlan gp = plan_grad((int)n);
-    size_t mat_bytes = align_up((size_t)n * n * sizeof(double2), 256);
-    size_t ws = grad_ws_bytes((int)n, gp);
+    const size_t nn = (size_t)n * n;
+    const size_t mat_bytes = align_up((size_t)count * nn * sizeof(double2), 256);
+    const size_t perm_bytes = align_up((size_t)count * 6 * sizeof(double), 256);
+    const size_t ws = grad_ws_bytes((int)n, (int)count);
     ThreadCtx& c = thread_ctx();
-    int rc = c.ensure(mat_bytes * 2 + 256 + ws);
+    int rc = c.ensure(mat_bytes * 2 + perm_bytes + ws);
     if (rc) return rc;
     char* base = static_cast<char*>(c.dbuf);
     double2* dA = reinterpret_cast<double2*>(base);
     double* dgrad = reinterpret_cast<double*>(base + mat_bytes);
     double* dperm = reinterpret_cast<double*>(base + 2 * mat_bytes);
-    void* dws = base + 2 * mat_bytes + 256;
-    cudaError_t e = cudaMemcpy2DAsync(dA, n * sizeof(double2), A, ld * sizeof(double2), n * sizeof(double2), n,
-                                      cudaMemcpyHostToDevice, c.stream);
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: upload");
+    void* dws = base + 2 * mat_bytes + perm_bytes;
+    // dense upload: matrix b as n rows of n complex128; non-finite matrices
+    // are replaced by zeros on the device and answered with NaN
+    std::vector<double2> h((size_t)count * nn);
+    std::vector<char> bad((size_t)count, 0);
+    for (int64_t b = 0; b < count; ++b) {
+        const double* Ab = A + 2 * b * stride;
+        bad[b] = !all_finite(Ab, n, n, ld);
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t j = 0; j < n; ++j)
+                h[b * nn + i * n + j] = bad[b] ? make_double2(0.0, 0.0)
+                                               : make_double2(Ab[2 * (i * ld + j)], Ab[2 * (i * ld + j) + 1]);
+    }
+    cudaError_t e = cudaMemcpyAsync(dA, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, (std::string(who) + ": upload").c_str());
     if (stats) cudaEventRecord(c.ev0, c.stream);
     GradPlan used;
-    rc = run_grad_dev(dA, n, (int)n, dws, ws, dgrad, dperm, dperm + 2, c.stream, &used);
+    rc = run_grad_dev(dA, n, (long long)nn, (int)n, (int)count, dws, ws, dgrad, dperm,
+                      count == 1 ? dperm + 2 : nullptr, c.stream, &used);
     if (rc) return rc;
     if (stats) cudaEventRecord(c.ev1, c.stream);
-    double h[6];
-    e = cudaMemcpyAsync(grad, dgrad, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost, c.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, dperm, sizeof(h), cudaMemcpyDeviceToHost, c.stream);
+    std::vector<double> hp(count == 1 ? 6 : 2 * (size_t)count);
+    e = cudaMemcpyAsync(grads, dgrad, (size_t)count * nn * sizeof(double2), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), dperm, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: kernel");
-    perm[0] = h[0];
-    perm[1] = h[1];
-    if (perm_dd) std::memcpy(perm_dd, h + 2, 4 * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, (std::string(who) + ": kernel").c_str());
+    for (int64_t b = 0; b < count; ++b) {
+        perms[2 * b] = bad[b] ? NAN : hp[2 * b];
+        perms[2 * b + 1] = bad[b] ? NAN : hp[2 * b + 1];
+        if (bad[b])
+            for (size_t q = 0; q < 2 * nn; ++q) grads[2 * b * nn + q] = NAN;
+    }
+    if (perm_dd && count == 1) std::memcpy(perm_dd, hp.data() + 2, 4 * sizeof(double));
     if (stats) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c.ev0, c.ev1);
         stats->kernel_ms = ms;
-        stats->steps = std::ldexp(1.0, (int)n - 1);
+        stats->steps = (double)count * std::ldexp(1.0, (int)n - 1);
         stats->flops = 8.0 * (double)n * stats->steps;
-        stats->launches = 4;
+        stats->launches = 5 * (int)((count + kMaxBatchLaunch - 1) / kMaxBatchLaunch);
         stats->grid = used.grid;
         stats->seg_log2 = used.seg_log2;
         stats->arith = GBPERM_ARITH_DF32;
     }
     return GBPERM_OK;
+}
+
+int gbperm_perm_grad(const double* A, int64_t n, int64_t ld, double* perm, double* perm_dd, double* grad,
+                     gbperm_stats* stats) {
+    return perm_grad_host(A, n, 1, ld, n * ld, perm, perm_dd, grad, stats, "gbperm_perm_grad");
+}
+
+int gbperm_perm_grad_batched(const double* A, int64_t n, int64_t count, double* perms, double* grads,
+                             gbperm_stats* stats) {
+    return perm_grad_host(A, n, count, n, n * n, perms, nullptr, grads, stats, "gbperm_perm_grad_batched");
 }
 
 }  // extern "C"

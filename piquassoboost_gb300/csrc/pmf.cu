@@ -72,6 +72,9 @@ __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part)
     __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
     __shared__ long long s_stride[kMaxDigits];
     const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    // launched as the twin of pmf_df_kernel: run only when the range check
+    // sent the product to FP64
+    if (p.df_info && p.df_info[1] != 0) return;
     for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
         int r = e / NP, j = e % NP;
         s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
@@ -250,13 +253,271 @@ __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part)
     }
 }
 
+// ------------------------------------------------ double-float product
+// The same sweep with the product as float pairs on the FP32 pipe (the
+// arithmetic of perm_repeated_df.cu, error ~2^-46 per complex multiply):
+// per step and lane, powers P_c = x_c^(c_c), prefix products (which also give
+// the lane's partial product), the other three lanes' partials by shuffle, a
+// suffix chain seeded with weight x sign x those partials, and
+// LO_c = prefix_c x suffix_c x x_c^(c_c - 1).  Running sums per column are
+// lazily normalised float pairs (renormalised every 8 steps), folded into a
+// double-double accumulator with the high-digit weight every 256 steps.
+// The row tables are interleaved by lane (column g*CPL + c of row r at
+// r*NP + c*4 + g) so a walk's four lanes read adjacent words.  Launched as the
+// twin of pmf_kernel: whichever the range check does not select returns.
+
+__device__ __forceinline__ cf shfl_cf(const cf& v, int src) {
+    return cf{__shfl_sync(0xffffffffu, v.rh, src), __shfl_sync(0xffffffffu, v.rl, src),
+              __shfl_sync(0xffffffffu, v.ih, src), __shfl_sync(0xffffffffu, v.il, src)};
+}
+
+// x^e by squaring (e >= 1)
+__device__ __forceinline__ cf cf_pow_pos(cf x, int e) {
+    cf acc = x;
+    bool have = false;
+    cf y = x;
+    while (e > 0) {
+        if (e & 1) {
+            acc = have ? cf_mul(acc, y) : y;
+            have = true;
+        }
+        e >>= 1;
+        if (e) y = cf_mul(y, y);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void df_add_lazy2(float& ah, float& al, float bh, float bl) {
+    float s, e;
+    two_sum_f(ah, bh, s, e);
+    ah = s;
+    al = __fadd_rn(al, __fadd_rn(bl, e));
+}
+
+__device__ __forceinline__ void df_renorm2(float& h, float& l) {
+    float s, e;
+    two_sum_f(h, l, s, e);
+    h = s;
+    l = e;
+}
+
+template <int CPL>
+__global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_part) {
+    constexpr int G = 4;
+    constexpr int NP = CPL * G;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cdd* s_acc = reinterpret_cast<cdd*>(smem_raw);                           // CPL x kThreads
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(s_acc + CPL * kThreads);  // R x NP (interleaved)
+    longlong2* s_a2 = s_a1 + p.R * NP;                                       // nd x NP (interleaved)
+    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);               // P
+    unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);      // P
+    __shared__ int s_cpow[NP];
+    __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
+    __shared__ long long s_stride[kMaxDigits];
+    const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    if (p.df_info[1] == 0) return;  // range check failed: pmf_kernel runs instead
+    for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
+        const int r = e / NP, qq = e % NP, j = (qq % G) * CPL + qq / G;
+        s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
+    }
+    for (int e = threadIdx.x; e < nd * NP; e += blockDim.x) {
+        const int r = e / NP, qq = e % NP, j = (qq % G) * CPL + qq / G;
+        s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
+    }
+    for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
+        s_w[e] = p.wlow[e];
+        s_seq[e] = p.seq[e];
+    }
+    for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
+    for (int e = threadIdx.x; e < nd; e += blockDim.x) s_D[e] = p.D[e];
+    for (int e = threadIdx.x; e < R; e += blockDim.x) s_r[e] = p.rcoef[e];
+    for (int e = threadIdx.x; e < CPL * kThreads; e += blockDim.x) s_acc[e] = cdd{{0.0, 0.0}, {0.0, 0.0}};
+    if (threadIdx.x == 0) {
+        long long st = 1;
+        for (int i = 0; i < q; ++i) {
+            s_stride[i] = st;
+            st *= (long long)(p.D[i] + 1);
+        }
+    }
+    __syncthreads();
+
+    const DfConv cv = make_dfconv(p.df_info[0]);
+    const int lane = threadIdx.x & 31;
+    const int g = lane % G;
+    const int lbase = lane - g;
+    cdd* my_acc = s_acc + threadIdx.x;  // column c at my_acc[c * kThreads]
+    int cp[CPL];
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) cp[c] = s_cpow[g * CPL + c];
+    const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / G;
+    const unsigned long long lane_seg = (unsigned long long)(lane / G);
+    long long cre[CPL], cim[CPL];
+    cf Q[CPL];
+
+    for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / G;
+         hw < p.nseg; hw += T) {
+        const unsigned long long h_raw = hw + lane_seg;
+        const bool active = h_raw < p.nseg;
+        const unsigned long long h = active ? h_raw : 0ull;
+        int gdig[kMaxDigits];
+        {
+            unsigned long long rem = h;
+            int cnt[kMaxDigits];
+            for (int i = q; i < nd; ++i) {
+                unsigned long long L = (unsigned long long)(s_D[i] + 1);
+                cnt[i] = (int)(rem % L);
+                rem /= L;
+            }
+            int par = 0;
+            for (int i = nd - 1; i >= 0; --i) {
+                int c = i >= q ? cnt[i] : 0;
+                int gg = par ? s_D[i] - c : c;
+                gdig[i] = gg;
+                par ^= gg & 1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cre[c] = 0;
+            cim[c] = 0;
+            Q[c] = cf{0.f, 0.f, 0.f, 0.f};
+        }
+        int gsum = 0;
+        double whigh = 1.0;
+        unsigned long long Gd = 0ull;  // low Gray digits, 4 bits each
+        unsigned int dir = 0u;         // bit i set: low digit i moves up next
+        long long widx = 0;
+        for (int i = 0; i < R; ++i) {
+            int gi = i < nd ? gdig[i] : 0;
+            long long coef = (long long)(s_r[i] - 2 * gi);
+            const longlong2* a = s_a1 + i * NP + g;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                longlong2 v = a[c * G];
+                cre[c] += coef * v.x;
+                cim[c] += coef * v.y;
+            }
+            if (i < nd) {
+                gsum += gi;
+                if (i < q) {
+                    Gd |= (unsigned long long)gi << (4 * i);
+                    if (gi == 0) dir |= 1u << i;
+                    widx += (long long)gi * s_stride[i];
+                } else {
+                    whigh *= p.binom[s_D[i] * kBinomStride + gi];
+                }
+            }
+        }
+        unsigned int sbit = (unsigned int)(gsum & 1) << 31;
+        const float wgt = active ? 1.f : 0.f;
+        for (unsigned long long k = 0; k < p.P; ++k) {
+            if (k != 0) {
+                const int d = s_seq[k];  // warp-uniform
+                const bool up = (dir >> d) & 1u;
+                const int sh = 4 * d;
+                int gv = (int)((Gd >> sh) & 15ull);
+                gv += up ? 1 : -1;
+                Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
+                if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
+                widx += up ? s_stride[d] : -s_stride[d];
+                const long long m = up ? -1ll : 0ll;  // up: one more -1 delta -> subtract 2 a
+                const longlong2* a = s_a2 + d * NP + g;
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    longlong2 v = a[c * G];
+                    cre[c] += (v.x ^ m) - m;
+                    cim[c] += (v.y ^ m) - m;
+                }
+                sbit ^= 0x80000000u;
+                if ((k & 255ull) == 0) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        cdd t = my_acc[c * kThreads];
+                        t.re = dd_add(t.re, dd{(double)Q[c].rh * whigh, (double)Q[c].rl * whigh});
+                        t.im = dd_add(t.im, dd{(double)Q[c].ih * whigh, (double)Q[c].il * whigh});
+                        my_acc[c * kThreads] = t;
+                        Q[c] = cf{0.f, 0.f, 0.f, 0.f};
+                    }
+                }
+            }
+            // P_c = x_c^(c_c) (1 for padding columns)
+            cf x[CPL], P[CPL];
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (cp[c] > 0) {
+                    fix_to_df_magic(cre[c], cv, x[c].rh, x[c].rl);
+                    fix_to_df_magic(cim[c], cv, x[c].ih, x[c].il);
+                    P[c] = cp[c] == 1 ? x[c] : cf_pow_pos(x[c], cp[c]);
+                } else {
+                    x[c] = cf{1.f, 0.f, 0.f, 0.f};
+                    P[c] = x[c];
+                }
+            }
+            // prefix products pre[c] = prod_{c' < c} P_c'; the lane's partial
+            cf pre[CPL];
+            cf part = P[0];
+            if (CPL > 1) {
+                pre[1] = P[0];
+#pragma unroll
+                for (int c = 2; c < CPL; ++c) pre[c] = cf_mul(pre[c - 1], P[c - 1]);
+                part = cf_mul(pre[CPL - 1], P[CPL - 1]);
+            }
+            cf o1 = shfl_cf(part, lbase + ((g + 1) & 3));
+            cf o2 = shfl_cf(part, lbase + ((g + 2) & 3));
+            cf o3 = shfl_cf(part, lbase + ((g + 3) & 3));
+            // low-digit weight: exact integer table entry as a float pair
+            const double w = s_w[widx];
+            const float wh = __fmul_rn((float)w, wgt);
+            const float wl = __fmul_rn((float)(w - (double)(float)w), wgt);
+            cf seed = cf_mul(cf_mul(cf_mul(o1, o2), o3), cf{wh, wl, 0.f, 0.f});
+            seed = cf{__uint_as_float(__float_as_uint(seed.rh) ^ sbit), __uint_as_float(__float_as_uint(seed.rl) ^ sbit),
+                      __uint_as_float(__float_as_uint(seed.ih) ^ sbit), __uint_as_float(__float_as_uint(seed.il) ^ sbit)};
+            // LO_c = seed * prod_{c' > c} P_c' * pre[c] * x_c^(c_c - 1)
+            cf suf = seed;
+#pragma unroll
+            for (int c = CPL - 1; c >= 0; --c) {
+                cf lo = (c == 0) ? suf : cf_mul(pre[c], suf);
+                if (cp[c] > 1) lo = cf_mul(lo, cp[c] == 2 ? x[c] : cf_pow_pos(x[c], cp[c] - 1));
+                df_add_lazy2(Q[c].rh, Q[c].rl, lo.rh, lo.rl);
+                df_add_lazy2(Q[c].ih, Q[c].il, lo.ih, lo.il);
+                if (c > 0) suf = cf_mul(suf, P[c]);
+            }
+            if ((k & 7ull) == 7ull) {
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    df_renorm2(Q[c].rh, Q[c].rl);
+                    df_renorm2(Q[c].ih, Q[c].il);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cdd t = my_acc[c * kThreads];
+            t.re = dd_add(t.re, dd{(double)Q[c].rh * whigh, (double)Q[c].rl * whigh});
+            t.im = dd_add(t.im, dd{(double)Q[c].ih * whigh, (double)Q[c].il * whigh});
+            my_acc[c * kThreads] = t;
+        }
+    }
+    __syncthreads();
+    // column j = g*CPL + c is held by the threads t with t % G == g: sum them
+    // in a fixed order
+    for (int j = threadIdx.x; j < NP; j += blockDim.x) {
+        const int gj = j / CPL, c = j % CPL;
+        cdd b = s_acc[c * kThreads + gj];
+        for (int t = gj + G; t < kThreads; t += G) b = cdd_add(b, s_acc[c * kThreads + t]);
+        if (j < C) col_part[(size_t)blockIdx.x * C + j] = b;
+    }
+}
+
 // Sum the block partials per column in a fixed order and scale: perm_l =
-// sum * 2^(exp - e_l) (column l lost one factor of its 2^-e_l scaling).
+// sum * 2^(exp - e_l + o) (column l lost one factor of its 2^-e_l scaling
+// and, in the double-float product, of the range boost 2^o).
 // Then the contraction with the interferometer and the normalisation, in the
 // reference's order (input modes ascending, total over modes ascending).
 __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* col_part, int nblocks, int C,
                                                                    const int* exp_in, const int* col_e,
-                                                                   const int* col_mode, const double* cin_w,
+                                                                   const int* df_info, const int* col_mode,
+                                                                   const double* cin_w,
                                                                    const double2* U, long long ldu, int m,
                                                                    double* pmf, double2* addends) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -266,7 +527,8 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
         cdd tot{{0.0, 0.0}, {0.0, 0.0}};
         for (int b = 0; b < nblocks; ++b) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
         double o[2];
-        write_result(tot, *exp_in - col_e[j], o, nullptr);
+        const int boost = df_info ? df_info[0] : 0;
+        write_result(tot, *exp_in - (col_e[j] - boost), o, nullptr);
         s_perm[j] = make_double2(o[0], o[1]);
     }
     for (int i = threadIdx.x; i < m; i += blockDim.x) addends[i] = make_double2(0.0, 0.0);
@@ -348,6 +610,42 @@ cudaError_t pmf_launch(const RepArgs& a, int cpl, int grp, cdd* col_part, int gr
     }
 }
 
+template <int CPL>
+int pmf_df_bps_t(const RepArgs& a) {
+    int nb = 0;
+    size_t smem = pmf_smem<CPL, 4>(a);
+    cudaFuncSetAttribute(pmf_df_kernel<CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pmf_df_kernel<CPL>, kThreads, smem);
+    return nb > 0 ? nb : 1;
+}
+
+template <int CPL>
+cudaError_t pmf_df_launch_t(const RepArgs& a, cdd* col_part, int grid, cudaStream_t st) {
+    size_t smem = pmf_smem<CPL, 4>(a);
+    cudaError_t e = cudaFuncSetAttribute(pmf_df_kernel<CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    pmf_df_kernel<CPL><<<grid, kThreads, smem, st>>>(a, col_part);
+    return cudaGetLastError();
+}
+
+int pmf_df_bps(const RepArgs& a, int cpl) {
+    switch (cpl) {
+        case 1: return pmf_df_bps_t<1>(a);
+        case 2: return pmf_df_bps_t<2>(a);
+        case 4: return pmf_df_bps_t<4>(a);
+        default: return pmf_df_bps_t<8>(a);
+    }
+}
+
+cudaError_t pmf_df_launch(const RepArgs& a, int cpl, cdd* col_part, int grid, cudaStream_t st) {
+    switch (cpl) {
+        case 1: return pmf_df_launch_t<1>(a, col_part, grid, st);
+        case 2: return pmf_df_launch_t<2>(a, col_part, grid, st);
+        case 4: return pmf_df_launch_t<4>(a, col_part, grid, st);
+        default: return pmf_df_launch_t<8>(a, col_part, grid, st);
+    }
+}
+
 // FP64 flops of one Gray step of pmf_kernel: per lane CPL-1 (partial
 // product) + G-1 (gather) + CPL-2 (suffix) + 2 (CPL-1) (leave-one-out)
 // complex products of 6 flops, plus 2 adds per column
@@ -363,9 +661,11 @@ double pmf_step_flops(int C, int cpl, int grp) {
 using namespace gbperm;
 
 extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample,
-                                  const int64_t* current_input, double* pmf, double* addends,
+                                  const int64_t* current_input, int arith, double* pmf, double* addends,
                                   gbperm_stats* stats) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+        return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: unknown arithmetic");
     if (m <= 0) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: no modes");
     if (!U || !sample || !current_input || !pmf) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: null argument");
     if (ld < m) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: ld < m");
@@ -400,6 +700,7 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     if (C > 64) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_compute_pmf: more than 64 occupied input modes");
     RepArgs a{};
     int cpl = 1, grp = 4, grid = 1;
+    bool df = false;
     if (!first_photon) {
         a.R = h.R;
         a.C = h.C;
@@ -408,6 +709,12 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         a.P = h.P;
         a.nseg = h.nseg;
         pmf_shape(C, &cpl, &grp);
+        // double-float product for up to 32 columns (4 lanes x 8) when the
+        // dynamic range allows; the device check decides between the twins
+        if (arith == GBPERM_ARITH_DF32 && grp == 4) {
+            int boost = 0;
+            df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), h.cpow.data(), &boost);
+        }
     }
     ThreadCtx& cx = thread_ctx();
     int rc = cx.ensure(0);  // device check before any runtime query
@@ -416,6 +723,7 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     cudaGetDevice(&dev);
     if (!first_photon) {
         int bps = pmf_bps(a, cpl, grp);
+        if (df) bps = std::min(bps, pmf_df_bps(a, cpl));
         unsigned long long full = (unsigned long long)device_sms(dev) * bps;
         unsigned long long per_block = (unsigned long long)(kThreads / grp);
         unsigned long long need = (h.nseg + per_block - 1) / per_block;
@@ -495,8 +803,8 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         pa.a2 = reinterpret_cast<longlong2*>(base + o_a2);
         pa.exp_out = d_exp;
         pa.col_e_out = d_ints + i_cole;
-        pa.df = 0;
-        pa.df_info = nullptr;
+        pa.df = df ? 1 : 0;
+        pa.df_info = df ? d_exp + 4 : nullptr;
         e = launch_prepare(pa, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: prepare");
         a.a1 = pa.a1;
@@ -507,6 +815,11 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         a.wlow = reinterpret_cast<const double*>(base + o_wlow);
         a.seq = reinterpret_cast<const unsigned char*>(base + o_seq);
         a.binom = reinterpret_cast<const double*>(base + o_binom);
+        a.df_info = pa.df_info;
+        if (df) {
+            e = pmf_df_launch(a, cpl, d_part, grid, st);
+            if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: df launch");
+        }
         e = pmf_launch(a, cpl, grp, d_part, grid, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: launch");
     } else {
@@ -521,7 +834,8 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     double* d_pmf = reinterpret_cast<double*>(base + o_pmf);
     double2* d_add = reinterpret_cast<double2*>(base + o_add);
     const size_t fsmem = (size_t)C * sizeof(double2);
-    pmf_finalize_kernel<<<1, kFinThreads, fsmem, st>>>(d_part, nblocks, C, d_exp, d_ints + i_cole, d_ints + i_mode,
+    pmf_finalize_kernel<<<1, kFinThreads, fsmem, st>>>(d_part, nblocks, C, d_exp, d_ints + i_cole,
+                                                       df ? d_exp + 4 : nullptr, d_ints + i_mode,
                                                        reinterpret_cast<const double*>(base + o_cw),
                                                        reinterpret_cast<const double2*>(base + o_U), m, (int)m,
                                                        d_pmf, d_add);
@@ -539,10 +853,12 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         stats->kernel_ms = ms;
         stats->steps = first_photon ? 0.0 : h.steps;
         stats->flops = first_photon ? 0.0 : pmf_step_flops(C, cpl, grp) * h.steps;
-        stats->launches = first_photon ? 1 : 3;
+        stats->launches = first_photon ? 1 : (df ? 4 : 3);
         stats->grid = grid;
         stats->seg_log2 = h.q;
-        stats->arith = GBPERM_ARITH_FP64;
+        int info[2] = {0, 0};
+        if (df) cudaMemcpy(info, d_exp + 4, sizeof(info), cudaMemcpyDeviceToHost);
+        stats->arith = (df && info[1]) ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
     }
     return GBPERM_OK;
 }

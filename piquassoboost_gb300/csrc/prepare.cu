@@ -8,6 +8,15 @@ namespace gbperm {
 namespace {
 
 __global__ void prepare_kernel(PrepArgs p) {
+    const int bt = blockIdx.x;  // matrix of a batch
+    if (bt > 0) {
+        p.A += (long long)bt * p.a_stride;
+        p.a1 += (size_t)bt * p.rows * p.cols;
+        p.a2 += (size_t)bt * p.rows * p.cols;
+        p.exp_out += bt;
+        if (p.col_e_out) p.col_e_out += (size_t)bt * p.cols;
+        if (p.df_info) p.df_info += 2 * bt;
+    }
     __shared__ int s_e[64];
     __shared__ double s_typ[64];
     for (int j = threadIdx.x; j < p.cols; j += blockDim.x) {
@@ -99,7 +108,7 @@ bool df_boost(const double* A, int64_t rows, int64_t cols, int64_t ld, const int
 }
 
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st) {
-    prepare_kernel<<<1, 64, 0, st>>>(a);
+    prepare_kernel<<<a.count, 64, 0, st>>>(a);
     return cudaGetLastError();
 }
 

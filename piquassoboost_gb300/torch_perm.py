@@ -1,9 +1,11 @@
 """PyTorch autograd boundary for the GB300 permanent.
 
 ``permanent(A)`` takes a square complex128 CUDA tensor and returns perm(A) as
-a 0-dim complex tensor.  The forward pass runs the fused permanent+gradient
-sweep of libgbperm (gbperm_perm_grad_dev) on the tensor's current stream and
-keeps dperm/dA for the backward pass, which returns grad_out * conj(dperm/dA)
+a 0-dim complex tensor; given a (B, n, n) stack it returns the B permanents
+from one set of launches.  The forward pass runs the fused
+permanent+gradient sweep of libgbperm (gbperm_perm_grad_dev /
+gbperm_perm_grad_batched_dev) on the tensor's current stream and keeps
+dperm/dA for the backward pass, which returns grad_out * conj(dperm/dA)
 (PyTorch's convention for holomorphic functions).  ``permanent_fwd`` is the
 forward-only plain kernel.  Tensors stay on the device; there is no CPU path.
 """
@@ -59,6 +61,42 @@ def permanent_and_grad(A: torch.Tensor):
     return torch.complex(perm[0], perm[1]), grad
 
 
+def permanents_and_grads(A: torch.Tensor):
+    """(perms[B], dperm/dA[B, n, n]) of a (B, n, n) stack in one sweep per
+    matrix and one set of launches (n <= 32)."""
+    if not A.is_cuda:
+        raise ValueError("permanent: the matrices must be a CUDA tensor (no CPU path)")
+    if A.dim() != 3 or A.shape[1] != A.shape[2]:
+        raise ValueError("permanent: a (B, n, n) stack of square matrices is required")
+    A = A.to(torch.complex128).contiguous()
+    lib = nat.load()
+    count, n = A.shape[0], A.shape[1]
+    perms = torch.empty((count, 2), dtype=torch.float64, device=A.device)
+    grads = torch.empty((count, n, n), dtype=torch.complex128, device=A.device)
+    if count == 0:
+        return torch.complex(perms[:, 0], perms[:, 1]), grads
+    ws_bytes = int(lib.gbperm_perm_grad_batched_workspace_size(n, count))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=A.device)
+    with torch.cuda.device(A.device):
+        nat.check(lib.gbperm_perm_grad_batched_dev(_P(A.data_ptr()), n, count, n, n * n, _P(perms.data_ptr()),
+                                                   _P(grads.data_ptr()), _P(ws.data_ptr()), ws_bytes,
+                                                   _stream_ptr(A)))
+    return torch.complex(perms[:, 0], perms[:, 1]), grads
+
+
+class PermanentBatched(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, A):
+        p, g = permanents_and_grads(A)
+        ctx.save_for_backward(g)
+        return p
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (g,) = ctx.saved_tensors
+        return grad_out[:, None, None] * g.conj()
+
+
 class Permanent(torch.autograd.Function):
     @staticmethod
     def forward(ctx, A):
@@ -73,26 +111,62 @@ class Permanent(torch.autograd.Function):
 
 
 def permanent(A: torch.Tensor) -> torch.Tensor:
-    """Differentiable permanent of a square complex CUDA matrix."""
+    """Differentiable permanent of a square complex CUDA matrix, or the
+    permanents of a (B, n, n) stack."""
+    if A.dim() == 3:
+        return PermanentBatched.apply(A)
     return Permanent.apply(A)
+
+
+_MESH_CACHE: dict = {}
+
+
+def _mesh_indices(m: int, device):
+    """Index tensors of an m-mode Clements mesh: for interferometer t (in
+    phase order) its layer and top mode, plus the identity mask of the modes
+    a layer leaves alone."""
+    key = (m, str(device))
+    if key not in _MESH_CACHE:
+        lay, top = [], []
+        for layer in range(m):
+            for i in range(layer % 2, m - 1, 2):
+                lay.append(layer)
+                top.append(i)
+        lay_t = torch.tensor(lay, device=device)
+        top_t = torch.tensor(top, device=device)
+        base = torch.eye(m, dtype=torch.complex128, device=device).repeat(m, 1, 1)
+        base[lay_t, top_t, top_t] = 0
+        base[lay_t, top_t + 1, top_t + 1] = 0
+        _MESH_CACHE[key] = (lay_t, top_t, base)
+    return _MESH_CACHE[key]
 
 
 def clements_unitary(phases: torch.Tensor, m: int) -> torch.Tensor:
     """m x m unitary of a Clements rectangular mesh of m(m-1)/2 Mach-Zehnder
     interferometers, two phases (theta, phi) each: phases has m(m-1) entries.
-    Built with differentiable torch ops (complex128, on phases.device)."""
+    Layer l holds the interferometers on mode pairs (i, i+1), i = l mod 2,
+    l mod 2 + 2, ...; each maps rows (i, i+1) of the running matrix by
+    [[e^{i phi} cos theta, -sin theta], [e^{i phi} sin theta, cos theta]],
+    so U = L_{m-1} ... L_1 L_0.  The m layer matrices are built in one
+    scatter and multiplied in a binary tree of batched products (about log2 m
+    launches each way).  Differentiable torch ops, complex128, on
+    phases.device."""
     dev = phases.device
-    U = torch.eye(m, dtype=torch.complex128, device=dev)
-    k = 0
-    for layer in range(m):
-        for i in range(layer % 2, m - 1, 2):
-            theta, phi = phases[k], phases[k + 1]
-            k += 2
-            e_phi = torch.exp(1j * phi.to(torch.complex128))
-            c = torch.cos(theta).to(torch.complex128)
-            s = torch.sin(theta).to(torch.complex128)
-            # 2x2 block acting on modes i, i+1
-            T = torch.stack([torch.stack([e_phi * c, -s]), torch.stack([e_phi * s, c])])
-            rows = U[i:i + 2, :]
-            U = torch.cat([U[:i, :], T @ rows, U[i + 2:, :]], dim=0)
-    return U
+    lay, top, base = _mesh_indices(m, dev)
+    theta = phases[0::2]
+    phi = phases[1::2]
+    e_phi = torch.exp(1j * phi.to(torch.complex128))
+    c = torch.cos(theta).to(torch.complex128)
+    s = torch.sin(theta).to(torch.complex128)
+    li = torch.cat([lay, lay, lay, lay])
+    ri = torch.cat([top, top, top + 1, top + 1])
+    ci = torch.cat([top, top + 1, top, top + 1])
+    vals = torch.cat([e_phi * c, -s, e_phi * s, c])
+    D = base.index_put((li, ri, ci), vals, accumulate=True)   # (m, m, m): layer matrices
+    # U = D[m-1] @ ... @ D[0]: pairwise products, later layer on the left
+    while D.shape[0] > 1:
+        k = D.shape[0]
+        even = k - (k % 2)
+        prod = torch.bmm(D[1:even:2], D[0:even:2])
+        D = torch.cat([prod, D[even:]]) if k % 2 else prod   # an odd last layer stays last (leftmost)
+    return D[0]

@@ -63,3 +63,14 @@ def pmf_layer_instance(seed: int, modes: int = 60, photons: int = 30):
     inp[:photons] = 1
     sample = rng.multinomial(photons - 1, np.ones(modes) / modes).astype(np.int64)
     return u, sample, inp
+
+
+def mesh_instance(seed: int, modes: int = 40, photons: int = 12, terms: int = 512):
+    """Phases of a `modes`-mode Clements mesh (modes (modes-1) entries,
+    uniform in [0, 2 pi)) and `terms` pairs of sorted input / output mode
+    sets of `photons` distinct modes each, all seeded."""
+    rng = np.random.default_rng(seed)
+    phases = rng.uniform(0.0, 2.0 * np.pi, modes * (modes - 1))
+    ins = np.stack([np.sort(rng.choice(modes, size=photons, replace=False)) for _ in range(terms)])
+    outs = np.stack([np.sort(rng.choice(modes, size=photons, replace=False)) for _ in range(terms)])
+    return phases, ins.astype(np.int64), outs.astype(np.int64)

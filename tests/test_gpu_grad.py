@@ -76,3 +76,39 @@ def test_torch_autograd():
     # d|p|^2 / d conj(a) convention: grad = 2 * p * conj(G)... torch gives grad_out*conj(dp/dA) chain
     expected = 2 * perm * np.conj(G)
     assert np.allclose(At.grad.cpu().numpy(), expected, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("n,count", [(12, 37), (20, 3), (1, 5), (5, 64)])
+def test_grad_batched_matches_single(n, count):
+    rng = np.random.default_rng(n * 100 + count)
+    mats = np.stack([haar_block(n, seed=int(s)) for s in rng.integers(0, 10**6, size=count)])
+    perms, grads = nat.perm_grad_batched(mats)
+    for b in range(count):
+        p, G = nat.perm_grad(mats[b])
+        assert abs(perms[b] - p) <= 1e-11 * abs(p)
+        assert np.max(np.abs(grads[b] - G)) <= 1e-11 * np.max(np.abs(G))
+
+
+def test_grad_batched_nonfinite_instance_isolated():
+    mats = np.stack([haar_block(8, seed=s) for s in range(4)])
+    mats[2, 3, 1] = np.nan
+    perms, grads = nat.perm_grad_batched(mats)
+    assert np.isnan(perms[2]) and np.all(np.isnan(grads[2]))
+    for b in (0, 1, 3):
+        p, G = nat.perm_grad(mats[b])
+        assert abs(perms[b] - p) <= 1e-11 * abs(p)
+        assert np.allclose(grads[b], G, rtol=1e-11, atol=0)
+
+
+def test_grad_batched_minors():
+    # every gradient entry of a few batch members against oracle minors
+    mats = np.stack([haar_block(9, seed=900 + s) for s in range(6)])
+    perms, grads = nat.perm_grad_batched(mats)
+    for b in range(len(mats)):
+        _, q = orc.bbfg(mats[b], prec=1)
+        assert orc.rel_err(perms[b], q) <= 1e-10
+        gnorm = np.abs(grads[b]).max()
+        for k in range(9):
+            for l in range(9):
+                ref, _ = orc.bbfg(_minor(mats[b], k, l), prec=1)
+                assert abs(grads[b, k, l] - ref) <= 1e-10 * max(abs(ref), 1e-3 * gnorm)

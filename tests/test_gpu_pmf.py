@@ -18,8 +18,8 @@ with open(os.path.join(HERE, "golden", "reference_calculators.json")) as _f:
     PMF_GOLD = json.load(_f).get("pmf", [])
 
 
-def _check(U, sample, cin):
-    pmf, add = nat.compute_pmf(U, sample, cin)
+def _check(U, sample, cin, mode="fp64"):
+    pmf, add = nat.compute_pmf(U, sample, cin, mode=mode)
     rpmf, radd = orc.compute_pmf(U, sample, cin, prec=1)
     assert pmf.shape == rpmf.shape
     assert np.allclose(pmf, rpmf, rtol=TOL, atol=1e-13), np.max(np.abs(pmf - rpmf))
@@ -34,12 +34,13 @@ def _check(U, sample, cin):
     return pmf, add
 
 
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
 @pytest.mark.parametrize("i", range(len(PMF_GOLD)))
-def test_pmf_reference_build_vectors(i):
+def test_pmf_reference_build_vectors(i, mode):
     case = PMF_GOLD[i]
     m = case["m"]
     U = np.array([complex(r, im) for r, im in case["matrix"]]).reshape(m, m)
-    pmf, _ = nat.compute_pmf(U, case["sample"], case["current_input"])
+    pmf, _ = nat.compute_pmf(U, case["sample"], case["current_input"], mode=mode)
     assert np.allclose(pmf, case["pmf"], rtol=TOL, atol=1e-13)
 
 
@@ -60,17 +61,19 @@ def _layer(seed, m, k, max_in=1, bunch=False):
     return U, sample, cin
 
 
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
 @pytest.mark.parametrize("seed", range(24))
-def test_pmf_random_layers(seed):
+def test_pmf_random_layers(seed, mode):
     rng = np.random.default_rng(100 + seed)
     m = int(rng.integers(2, 16))
     k = int(rng.integers(1, min(m, 12) + 1))
     U, sample, cin = _layer(seed, m, k, max_in=int(rng.integers(1, 4)), bunch=bool(seed % 2))
-    _check(U, sample, cin)
+    _check(U, sample, cin, mode)
 
 
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
 @pytest.mark.parametrize("k", [2, 5, 9, 17, 33])
-def test_pmf_lane_group_shapes(k):
+def test_pmf_lane_group_shapes(k, mode):
     # 1, 2, 4, 8 columns per lane with 4 lanes, and 8 x 8 above 32 input modes;
     # a bunched sample keeps the Gray range small at k = 33
     m = max(2 * k, 8)
@@ -83,7 +86,7 @@ def test_pmf_lane_group_shapes(k):
         sample = rng.multinomial(k - 1, np.ones(m) / m).astype(np.int64)
     else:
         sample[3], sample[7], sample[11] = 15, 10, k - 1 - 25
-    _check(U, sample, cin)
+    _check(U, sample, cin, mode)
 
 
 def test_pmf_first_photon():
@@ -94,19 +97,32 @@ def test_pmf_first_photon():
     assert add[1] == 1.0 and np.all(add[[0, 2, 3, 4, 5]] == 0)
 
 
-def test_pmf_repeated_input_and_sample():
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_pmf_repeated_input_and_sample(mode):
     U = haar_unitary(7, 5)
     cin = np.array([3, 0, 2, 0, 1, 0, 0])
     sample = np.array([0, 2, 0, 2, 0, 1, 0])
-    _check(U, sample, cin)
+    _check(U, sample, cin, mode)
 
 
-def test_pmf_amplitude_is_laplace_expansion_at_size():
+def test_pmf_fast_matches_fp64_at_size():
+    # the benchmark's 60-mode / 30-photon layer shape at 40 modes / 20 photons
+    U, sample, cin = _layer(21, 40, 20)
+    st = nat.Stats()
+    a, x = nat.compute_pmf(U, sample, cin, mode="fast", stats=st)
+    b, y = nat.compute_pmf(U, sample, cin, mode="fp64")
+    assert st.arith == nat.ARITH_DF32
+    assert np.allclose(a, b, rtol=1e-10, atol=1e-13)
+    assert np.max(np.abs(x - y)) <= 1e-10 * np.max(np.abs(y))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_pmf_amplitude_is_laplace_expansion_at_size(mode):
     # sum_l input[l] perm_l U[k][l] is the permanent of the sample plus one
     # photon in mode k against the input (expansion along the new row): a
     # size-independent check against the repeated-permanent kernel
     U, sample, cin = _layer(7, 48, 24)
-    pmf, add = nat.compute_pmf(U, sample, cin)
+    pmf, add = nat.compute_pmf(U, sample, cin, mode=mode)
     amps = (cin * add) @ U.T
     mags = np.abs(cin * add) @ np.abs(U.T)   # sum_l |input[l] perm_l U[k][l]|
     ref = np.zeros(48, dtype=np.complex128)
