@@ -110,6 +110,30 @@ int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld
                          int64_t nrow, int arith, double* out, double* out_dd,
                          gbperm_stats* stats);
 
+/* The same permanent by the Chin-Huh form of the sum (CChinHuhPermanent
+ * Calculator::calculate, piquassoboost/sampling/source/CChinHuhPermanent
+ * Calculator.cpp:48-201; repeated lib 0): the digits run over the INPUT
+ * multiplicities with no fixed copy and the prefactor is 2^-N, the product
+ * over the output modes.  A second, independently ordered evaluation of the
+ * repeated permanent, on the same kernels; same arguments and errors as
+ * gbperm_perm_repeated. */
+int gbperm_perm_chinhuh(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
+                        int64_t ncol, const int64_t* row_mult, int64_t nrow, int arith, double* out, double* out_dd,
+                        gbperm_stats* stats);
+
+/* Many repeated permanents of one matrix: pair i is the input state
+ * col_mults[i*ncol .. i*ncol+ncol) and the output state
+ * row_mults[i*nrow .. i*nrow+nrow).  Replaces BatchednPermanentCalculator::
+ * calculate (piquassoboost/sampling/source/BatchedPermanentCalculator.cpp:
+ * 109-296) and the list branch of the repeated wrapper
+ * (ChinHuhPermanentCalculator_Wrapper.hpp:233-323).  Pairs whose plain
+ * expansion is not much longer than their mixed-radix Gray code are expanded
+ * and share one persistent batched launch; the others run as repeated
+ * launches.  out: 2 * count doubles.  Any invalid pair fails the call. */
+int gbperm_perm_repeated_batched(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mults,
+                                 int64_t ncol, const int64_t* row_mults, int64_t nrow, int64_t count, int arith,
+                                 double* out, gbperm_stats* stats);
+
 /* ------------------------------------------------- batched permanents */
 /* Many plain permanents of uneven sizes in one persistent launch (a CUDA
  * graph per plan).  Replaces the list branch of the plain wrapper

@@ -485,6 +485,30 @@ int orc_glynn_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
     return 0;
 }
 
+/* ------------------------------------------------------------- Chin-Huh */
+/* CChinHuhPermanentCalculator::calculate, CChinHuhPermanentCalculator.cpp:
+ * 48-201 (repeated lib 0); see SFX(chinhuh). */
+int orc_chinhuh(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
+                const int64_t* row_mult, int prec, double* out) {
+    int64_t sin_ = 0, sout = 0;
+    double steps = 1.0;
+    for (int64_t j = 0; j < cols; ++j) {
+        sin_ += col_mult[j];
+        steps *= (double)(col_mult[j] + 1);
+    }
+    for (int64_t i = 0; i < rows; ++i) sout += row_mult[i];
+    if (sin_ != sout)
+        return set_err(2, "CChinHuhPermanentCalculator::calculate:  Number of input and output states should be equal");
+    if (rows == 0 || sin_ == 0) {
+        out[0] = 1.0; out[1] = 0.0; out[2] = 0.0; out[3] = 0.0;
+        return 0;
+    }
+    if (steps > 1e8) return set_err(3, "orc_chinhuh: too many terms for the oracle");
+    if (prec == 0) put_d(chinhuh_d(A, rows, cols, ld, col_mult, row_mult, sin_), out);
+    else put_q(chinhuh_q(A, rows, cols, ld, col_mult, row_mult, sin_), out);
+    return 0;
+}
+
 /* ---------------------------------------------------------- simple Glynn */
 /* GlynnPermanentCalculatorSimple.hpp:61-168.  Non-square input returns 0
  * (the reference prints a message and returns 0). */

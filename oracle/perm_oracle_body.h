@@ -346,3 +346,57 @@ static CX SFX(simple)(const double* A, int64_t n, int64_t ld) {
     r.im *= s;
     return r;
 }
+
+/* ------------------------------------------------------------------------
+ * Chin-Huh form of the repeated permanent, CChinHuhPermanentCalculator.cpp:
+ * 48-201: every vector v with 0 <= v_j <= in_j over the input (column)
+ * multiplicities, in odometer order, contributes
+ *   (-1)^{|v|} prod_j C(in_j, v_j) prod_i (sum_j (in_j - 2 v_j) a_ij)^{out_i}
+ * (rows i with out_i = 0 skipped), and the sum is divided by 2^N.  The
+ * powers are repeated products here.
+ * ---------------------------------------------------------------------- */
+static CX SFX(chinhuh)(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* in,
+                       const int64_t* out, int64_t photons) {
+    int64_t* v = (int64_t*)calloc((size_t)(cols > 0 ? cols : 1), sizeof(int64_t));
+    SFX(acc_t) acc = {0, 0, 0, 0};
+    for (;;) {
+        int64_t vs = 0;
+        R w = (R)1;
+        for (int64_t j = 0; j < cols; ++j) {
+            vs += v[j];
+            w *= (R)orc_binom128((int)in[j], (int)v[j]);
+        }
+        if (vs & 1) w = -w;
+        CX prod = {(R)1, (R)0};
+        for (int64_t i = 0; i < rows; ++i) {
+            if (out[i] == 0) continue;
+            CX s = {(R)0, (R)0};
+            for (int64_t j = 0; j < cols; ++j) {
+                CX a = SFX(ld)(A, ld, i, j);
+                R coef = (R)(in[j] - 2 * v[j]);
+                s.re += coef * a.re;
+                s.im += coef * a.im;
+            }
+            for (int64_t q = 0; q < out[i]; ++q) prod = SFX(cx_mul)(prod, s);
+        }
+        prod.re *= w;
+        prod.im *= w;
+        SFX(acc_add)(&acc, prod);
+        int64_t j = 0;
+        while (j < cols) {
+            if (v[j] < in[j]) {
+                v[j]++;
+                break;
+            }
+            v[j] = 0;
+            ++j;
+        }
+        if (j == cols) break;
+    }
+    free(v);
+    CX r = SFX(acc_get)(&acc);
+    R s = SFX(pow2_neg)(photons);
+    r.re *= s;
+    r.im *= s;
+    return r;
+}

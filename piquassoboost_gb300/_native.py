@@ -93,7 +93,11 @@ _SIGNATURES = [
     ("gbperm_perm_noalloc_scratch_bytes", ctypes.c_size_t, []),
     ("gbperm_perm_repeated", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
+    ("gbperm_perm_chinhuh", ctypes.c_int,
+     [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, ctypes.c_int, _P, _P, _P]),
     ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, ctypes.c_int, _P, _P, _P]),
+    ("gbperm_perm_repeated_batched", ctypes.c_int,
+     [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _I64, ctypes.c_int, _P, _P]),
 ]
 
 _lib = None
@@ -190,31 +194,53 @@ def as_state(state) -> np.ndarray:
 
 
 def perm_repeated(matrix, input_state, output_state, mode="fp64", return_dd: bool = False,
-                  stats: Stats | None = None):
-    """Repeated-multiplicity permanent on the GPU (gbperm_perm_repeated).
+                  stats: Stats | None = None, form: str = "bbfg"):
+    """Repeated-multiplicity permanent on the GPU (gbperm_perm_repeated, or
+    gbperm_perm_chinhuh with form="chinhuh").
 
     input_state gives the column multiplicities, output_state the row
     multiplicities (the reference's convention)."""
     lib = load()
+    fn = {"bbfg": lib.gbperm_perm_repeated, "chinhuh": lib.gbperm_perm_chinhuh}[form]
     a = as_matrix(matrix)
     cm = as_state(input_state)
     rm = as_state(output_state)
     rows, cols = a.shape
     out = np.zeros(2)
     dd = np.zeros(4)
-    rc = lib.gbperm_perm_repeated(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), len(cm),
-                                  rm.ctypes.data_as(_P), len(rm), arith_of(mode), out.ctypes.data_as(_P),
-                                  dd.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None)
+    rc = fn(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), len(cm), rm.ctypes.data_as(_P), len(rm),
+            arith_of(mode), out.ctypes.data_as(_P), dd.ctypes.data_as(_P),
+            ctypes.byref(stats) if stats is not None else None)
     check(rc)
     if return_dd:
         return complex(out[0], out[1]), dd
     return complex(out[0], out[1])
 
 
-def perm_repeated_many(matrix, pairs, mode="fp64"):
+def perm_repeated_many(matrix, pairs, mode="fp64", stats: Stats | None = None):
     """Repeated permanents of one matrix for a list of (input, output) state
-    pairs, in order."""
-    return [perm_repeated(matrix, i, o, mode=mode) for i, o in pairs]
+    pairs, in order, through one batched call (gbperm_perm_repeated_batched).
+    States shorter than the longest are zero-padded."""
+    lib = load()
+    a = as_matrix(matrix)
+    rows, cols = a.shape
+    if len(pairs) == 0:
+        return []
+    ins = [as_state(i) for i, _ in pairs]
+    outs = [as_state(o) for _, o in pairs]
+    ncol = max(len(x) for x in ins)
+    nrow = max(len(x) for x in outs)
+    cm = np.zeros((len(pairs), ncol), dtype=np.int64)
+    rm = np.zeros((len(pairs), nrow), dtype=np.int64)
+    for k, (x, y) in enumerate(zip(ins, outs)):
+        cm[k, :len(x)] = x
+        rm[k, :len(y)] = y
+    out = np.zeros(2 * len(pairs))
+    check(lib.gbperm_perm_repeated_batched(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), ncol,
+                                           rm.ctypes.data_as(_P), nrow, len(pairs), arith_of(mode),
+                                           out.ctypes.data_as(_P),
+                                           ctypes.byref(stats) if stats is not None else None))
+    return [complex(out[2 * k], out[2 * k + 1]) for k in range(len(pairs))]
 
 
 class BatchPlan:

@@ -70,6 +70,7 @@ bool plain_trivial(int64_t rows, int64_t cols, double* out, double* out_dd);
 struct RepHost {
     bool transpose = false;
     int R = 0, C = 0, nd = 0, q = 0, photons = 0;
+    int norm_shift = 0;           // the sum is scaled by 2^-norm_shift
     unsigned long long P = 1, nseg = 1;
     double steps = 0.0, flops = 0.0;
     std::vector<double> M;        // R x C complex128 (interleaved), digit rows first
@@ -81,9 +82,13 @@ struct RepHost {
 struct RepWs {
     size_t M = 0, a1 = 0, a2 = 0, ints = 0, wlow = 0, seq = 0, binom = 0, exp = 0, out = 0, kern = 0;
 };
+// col_surplus: photons the column side holds beyond the row side (1 for the
+// leave-one-out sums of the pmf layer).  chinhuh: the Chin-Huh form of the
+// same sum -- Gray digits over the input (column) side, no fixed copy, so the
+// prefactor is 2^-N (CChinHuhPermanentCalculator.cpp:48-201).
 int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
                   int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
-                  bool* is_trivial, bool allow_transpose, int col_surplus);
+                  bool* is_trivial, bool allow_transpose, int col_surplus, bool chinhuh = false);
 const std::vector<double>& binom_table();
 size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w);
 

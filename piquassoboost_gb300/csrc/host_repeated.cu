@@ -42,7 +42,7 @@ const std::vector<double>& binom_table() {
 
 int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
                   int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
-                  bool* is_trivial, bool allow_transpose, int col_surplus) {
+                  bool* is_trivial, bool allow_transpose, int col_surplus, bool chinhuh) {
     *is_trivial = false;
     if (rows == 0) {
         trivial[0] = 1.0;
@@ -94,7 +94,7 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
         return t * (long double)mn / (long double)(mn + 1);
     };
     long double t_rows = gray_len(ri, row_mult), t_cols = gray_len(ci, col_mult);
-    bool transpose = allow_transpose && t_cols < t_rows;
+    bool transpose = chinhuh || (allow_transpose && t_cols < t_rows);
     h->transpose = transpose;
     const std::vector<int>& gi = transpose ? ci : ri;   // Gray-code side (rows of M)
     const std::vector<int>& pj = transpose ? ri : ci;   // product side (columns of M)
@@ -103,10 +103,12 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
     int R = (int)gi.size(), C = (int)pj.size();
     if (C > GBPERM_MAX_DIM) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_repeated: more than 64 occupied modes");
 
-    // fixed copy: first occurrence of the smallest multiplicity
+    // fixed copy: first occurrence of the smallest multiplicity (none in the
+    // Chin-Huh form)
     int fixed = 0;
     for (int i = 1; i < R; ++i)
         if (gm[gi[i]] < gm[gi[fixed]]) fixed = i;
+    if (chinhuh) fixed = -1;
 
     struct RowInfo {
         int src;   // index into gi
@@ -158,6 +160,7 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
     h->nseg = T / P;
     h->steps = (double)T;
     h->photons = (int)sr;
+    h->norm_shift = chinhuh ? (int)sr : (int)sr - 1;
     // matrix M (rows: digits then constants) as complex128, dense
     h->M.assign((size_t)R * C * 2, 0.0);
     h->rcoef.clear();
@@ -240,10 +243,9 @@ size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w) {
 
 using namespace gbperm;
 
-extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
-                                    const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
-                                    int64_t nrow, int arith, double* out, double* out_dd,
-                                    gbperm_stats* stats) {
+static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
+                        int64_t ncol, const int64_t* row_mult, int64_t nrow, int arith, double* out, double* out_dd,
+                        gbperm_stats* stats, bool chinhuh) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
     if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: unknown arithmetic");
@@ -252,7 +254,7 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     RepHost h;
     double triv[2];
     bool is_triv = false;
-    int rc = repeated_plan(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, &h, triv, &is_triv, true, 0);
+    int rc = repeated_plan(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, &h, triv, &is_triv, true, 0, chinhuh);
     if (rc) return rc;
     if (is_triv) {
         out[0] = triv[0];
@@ -325,7 +327,7 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
     pa.cols = h.C;
     pa.row_w = d_ints;
     pa.col_w = d_ints + h.R + h.nd;
-    pa.norm_shift = h.photons - 1;
+    pa.norm_shift = h.norm_shift;
     pa.a1 = reinterpret_cast<longlong2*>(base + w.a1);
     pa.a2 = reinterpret_cast<longlong2*>(base + w.a2);
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
@@ -373,4 +375,17 @@ extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols,
         stats->arith = df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
     }
     return GBPERM_OK;
+}
+
+extern "C" int gbperm_perm_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
+                                    const int64_t* col_mult, int64_t ncol, const int64_t* row_mult,
+                                    int64_t nrow, int arith, double* out, double* out_dd,
+                                    gbperm_stats* stats) {
+    return run_repeated(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, arith, out, out_dd, stats, false);
+}
+
+extern "C" int gbperm_perm_chinhuh(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
+                                   int64_t ncol, const int64_t* row_mult, int64_t nrow, int arith, double* out,
+                                   double* out_dd, gbperm_stats* stats) {
+    return run_repeated(A, rows, cols, ld, col_mult, ncol, row_mult, nrow, arith, out, out_dd, stats, true);
 }

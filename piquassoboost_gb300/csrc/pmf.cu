@@ -798,7 +798,7 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         pa.cols = C;
         pa.row_w = d_ints;
         pa.col_w = d_ints + h.R + h.nd;
-        pa.norm_shift = h.photons - 1;
+        pa.norm_shift = h.norm_shift;
         pa.a1 = reinterpret_cast<longlong2*>(base + o_a1);
         pa.a2 = reinterpret_cast<longlong2*>(base + o_a2);
         pa.exp_out = d_exp;

@@ -36,6 +36,9 @@ PLAIN_LIBS = {0: "fp64", 6: "fp64", 7: "fp64", 8: "fp64", 10: "fp64", 11: "fp64"
 # repeated ids served on the GPU (lib 9 constructs but cannot calculate)
 REPEATED_LIBS = {0: "fp64", 1: "fp64", 6: "fp64", 7: "fp64", 8: "fp64", 20: "fp64", 21: "fast"}
 REPEATED_CONSTRUCT_ONLY = {9}
+# lib 0 (ChinHuhPermanentCalculator) evaluates the Chin-Huh form of the sum
+# (CChinHuhPermanentCalculator.cpp:48-201) on the same kernels
+REPEATED_FORM = {0: "chinhuh"}
 
 
 def _coerce_matrix(m):
@@ -125,7 +128,7 @@ class ChinHuhPermanentCalculator_wrapper:
             return res
         if isinstance(ins, list) or isinstance(outs, list):
             raise TypeError("input_state and output_state must both be lists, or both arrays")
-        return nat.perm_repeated(self._matrix, ins, outs, mode=mode)
+        return nat.perm_repeated(self._matrix, ins, outs, mode=mode, form=REPEATED_FORM.get(self.lib, "bbfg"))
 
 
 class RepeatedPermanentCalculator(ChinHuhPermanentCalculator_wrapper):

@@ -77,6 +77,16 @@ def glynn_repeated(A, col_mult, row_mult, prec=0):
     return _ret(rc, out)
 
 
+def chinhuh(A, col_mult, row_mult, prec=0):
+    """The Chin-Huh form of the repeated permanent (repeated lib 0)."""
+    a = _mat(A); out = np.zeros(4)
+    c = np.ascontiguousarray(col_mult, dtype=np.int64)
+    r = np.ascontiguousarray(row_mult, dtype=np.int64)
+    rc = lib().orc_chinhuh(a.ctypes.data_as(_P), _I(a.shape[0]), _I(a.shape[1]), _I(a.shape[1]),
+                           c.ctypes.data_as(_P), r.ctypes.data_as(_P), ctypes.c_int(prec), out.ctypes.data_as(_P))
+    return _ret(rc, out)
+
+
 def glynn_simple(A, prec=0):
     a = _mat(A); out = np.zeros(4)
     rc = lib().orc_glynn_simple(a.ctypes.data_as(_P), _I(a.shape[0]), _I(a.shape[1]), _I(a.shape[1]),

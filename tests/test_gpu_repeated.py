@@ -86,3 +86,77 @@ def test_repeated_low_digit_override(force_q):
         nat.set_option("repeated.low_digits", -1)
     _, dref = orc.bbfg_repeated(A, cin, rout, prec=1)
     assert orc.rel_err(v, dref) <= TOL
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_repeated_batched_matches_single(mode):
+    # sampler-style pairs on one interferometer: mostly single occupations
+    # (expanded into the batched plain launch) and some bunched states (run
+    # as repeated launches)
+    rng = np.random.default_rng(5)
+    m = 16
+    U = haar_unitary(m, 9)
+    pairs = []
+    for q in range(60):
+        k = int(rng.integers(0, 11))
+        if q % 5 == 0:
+            inp = rng.multinomial(k, np.ones(3) / 3)
+            inp = np.concatenate([inp, np.zeros(m - 3, dtype=np.int64)])
+        else:
+            inp = np.zeros(m, dtype=np.int64)
+            inp[rng.choice(m, size=k, replace=False)] = 1
+        out = rng.multinomial(k, np.ones(m) / m).astype(np.int64)
+        pairs.append((inp, out))
+    st = nat.Stats()
+    vals = nat.perm_repeated_many(U, pairs, mode=mode, stats=st)
+    for (i, o), v in zip(pairs, vals):
+        ref = nat.perm_repeated(U, i, o, mode=mode)
+        assert abs(v - ref) <= 1e-10 * max(abs(ref), 1e-300) + 1e-15, (i, o, v, ref)
+    _, dref = orc.bbfg_repeated(U, pairs[1][0], pairs[1][1], prec=1)
+    assert orc.rel_err(vals[1], dref) <= TOL
+
+
+def test_repeated_batched_mismatch_raises():
+    U = haar_unitary(6, 1)
+    pairs = [([1, 1, 0, 0, 0, 0], [0, 1, 1, 0, 0, 0]), ([1, 1, 1, 0, 0, 0], [0, 1, 1, 0, 0, 0])]
+    with pytest.raises(nat.GBPermError):
+        nat.perm_repeated_many(U, pairs)
+
+
+def test_repeated_list_branch_uses_batch():
+    from piquassoboost_gb300.sampling.Boson_Sampling_Utilities import BBFGRepeatedPermanentCalculatorDouble
+    U = haar_unitary(8, 4)
+    inp = [np.array([1, 1, 0, 1, 0, 0, 0, 0])]
+    # one input state against a 2-D array of output states (one per row)
+    outs = [np.array([[0, 1, 0, 0, 1, 1, 0, 0], [3, 0, 0, 0, 0, 0, 0, 0], [0, 0, 0, 0, 0, 0, 1, 2]])]
+    res = BBFGRepeatedPermanentCalculatorDouble(U, inp, outs).calculate()
+    assert len(res) == 1 and len(res[0]) == 3
+    for v, o in zip(res[0], outs[0]):
+        ref, _ = orc.bbfg_repeated(U, inp[0], o, prec=1)
+        assert abs(v - ref) <= TOL * abs(ref)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_chinhuh_form_vs_reference_build(mode):
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_calculators.json")) as f:
+        cases = json.load(f)["repeated"]
+    for case in cases:
+        vals = {int(k): complex(*v) for k, v in case["values"].items()}
+        if 0 not in vals:
+            continue
+        A = np.array([complex(r, i) for r, i in case["matrix"]]).reshape(case["shape"])
+        v = nat.perm_repeated(A, case["input_state"], case["output_state"], mode=mode, form="chinhuh")
+        assert abs(v - vals[0]) <= TOL * max(abs(vals[0]), 1e-300), (v, vals[0])
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_chinhuh_form_vs_oracle(seed):
+    A, cin, rout = _random_case(seed)
+    v = nat.perm_repeated(A, cin, rout, form="chinhuh")
+    ref, dref = orc.chinhuh(A, cin, rout, prec=1)
+    if abs(ref) < 1e-300:
+        assert abs(v) < 1e-12
+    else:
+        assert orc.rel_err(v, dref) <= TOL, (v, ref)

@@ -135,3 +135,16 @@ def test_oracle_compute_pmf_vs_reference_build(i):
     U = np.array([complex(r, im) for r, im in case["matrix"]]).reshape(m, m)
     pmf, _ = orc.compute_pmf(U, case["sample"], case["current_input"], prec=1)
     assert np.allclose(pmf, case["pmf"], rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("i", range(len(CALC["repeated"])))
+def test_oracle_chinhuh_vs_reference_build(i):
+    # CChinHuhPermanentCalculator.cpp:48-201 (repeated lib 0)
+    case = CALC["repeated"][i]
+    ref = {int(k): _c(v) for k, v in case["values"].items()}
+    if 0 not in ref:
+        pytest.skip("no lib 0 value")
+    A = _mat(case)
+    for prec in (0, 1):
+        v, _ = orc.chinhuh(A, case["input_state"], case["output_state"], prec=prec)
+        assert _close(v, ref[0], 1e-10), (prec, v, ref[0])
