@@ -156,6 +156,15 @@ int gbperm_batch_plan_run_dev(gbperm_batch_plan* plan, const void* d_packed, voi
  * setting it rebuilds the work list and the graph. */
 int gbperm_batch_plan_set_item_log2(gbperm_batch_plan* plan, int64_t item_log2);
 int64_t gbperm_batch_plan_get_item_log2(gbperm_batch_plan* plan);
+/* Autotuner: plans, captures and times each candidate shape -- lanes per
+ * Gray segment (2 or 4 for the double-float product, 1 for FP64) times work
+ * items of 1/4, 1 and 4 times the size-based default -- on this batch
+ * (`packed`, host buffer; reps timed launches each after one warm-up), keeps
+ * the fastest and returns its time per batch in best_ms.  Results do not
+ * depend on the choice beyond rounding of the fixed-order partial sums. */
+int gbperm_batch_plan_autotune(gbperm_batch_plan* plan, const double* packed, int reps, double* best_ms);
+/* The plan's current shape: lanes sharing one Gray segment, columns per lane. */
+int gbperm_batch_plan_get_shape(gbperm_batch_plan* plan, int64_t* lanes_per_segment, int64_t* columns_per_lane);
 /* One-shot: create, run, destroy. */
 int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t* cols, int64_t count, int arith,
                         double* out, gbperm_stats* stats);

@@ -83,6 +83,8 @@ _SIGNATURES = [
     ("gbperm_batch_plan_set_item_log2", ctypes.c_int, [_P, _I64]),
     ("gbperm_batch_plan_get_item_log2", _I64, [_P]),
     ("gbperm_perm_batched", ctypes.c_int, [_P, _P, _P, _I64, ctypes.c_int, _P, _P]),
+    ("gbperm_batch_plan_autotune", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("gbperm_batch_plan_get_shape", ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     ("gbperm_perm_grad", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P]),
     ("gbperm_perm_grad_workspace_size", ctypes.c_size_t, [_I64]),
     ("gbperm_perm_grad_dev", ctypes.c_int, [_P, _I64, _I64, _P, _P, _P, _P, ctypes.c_size_t, _P]),
@@ -281,6 +283,21 @@ class BatchPlan:
 
     def item_log2(self) -> int:
         return int(load().gbperm_batch_plan_get_item_log2(self._h))
+
+    def shape(self) -> tuple[int, int]:
+        """(lanes per Gray segment, columns per lane) of the plan's kernel."""
+        g, c = ctypes.c_int64(), ctypes.c_int64()
+        check(load().gbperm_batch_plan_get_shape(self._h, ctypes.byref(g), ctypes.byref(c)))
+        return int(g.value), int(c.value)
+
+    def autotune(self, matrices=None, packed=None, reps: int = 1) -> float:
+        """Time the candidate shapes on this batch and keep the fastest;
+        returns its time per batch in ms (gbperm_batch_plan_autotune)."""
+        if packed is None:
+            packed = self.pack(matrices)
+        ms = ctypes.c_double()
+        check(load().gbperm_batch_plan_autotune(self._h, packed.ctypes.data_as(_P), int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def close(self):
         if self._h:

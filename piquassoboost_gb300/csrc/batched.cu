@@ -438,6 +438,7 @@ struct BatchPlan {
     bool df = false;
     int cpl = 16, grp = 1;
     int grid = 1;
+    int maxc = 1;                    // widest instance (columns)
     int64_t item_target_log2 = 0;
     std::vector<int> rows, cols;
     std::vector<long long> off;      // complex offsets of each instance in the packed input
@@ -654,6 +655,7 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
         return cuda_fail(e, "gbperm_batch_plan_create");
     }
     p->df = arith == GBPERM_ARITH_DF32 && maxc <= kDfMaxCols;
+    p->maxc = maxc;
     batch_shape(maxc, p->df, (int)g_opt.batched_threads.load(), &p->cpl, &p->grp);
     int bps = batch_bps(p->cpl, p->grp, p->df);
     p->grid = device_sms(p->device) * bps;
@@ -799,6 +801,76 @@ int gbperm_batch_plan_set_item_log2(gbperm_batch_plan* plan, int64_t item_log2) 
 
 int64_t gbperm_batch_plan_get_item_log2(gbperm_batch_plan* plan) {
     return (plan && plan->p) ? plan->p->item_target_log2 : -1;
+}
+
+int gbperm_batch_plan_autotune(gbperm_batch_plan* plan, const double* packed, int reps, double* best_ms) {
+    if (!plan || !plan->p) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_autotune: null plan");
+    BatchPlan* p = plan->p;
+    if (best_ms) *best_ms = 0.0;
+    if (p->ninst == 0) return GBPERM_OK;
+    if (p->total_elems > 0 && !packed) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_autotune: null input");
+    if (reps < 1) reps = 1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != p->device) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_autotune: plan belongs to another device");
+    for (int64_t i = 0; i < p->count; ++i) {
+        if (p->dev_index[i] < 0) continue;
+        std::memcpy(p->hin + 2 * p->off[i], packed + 2 * p->off[i], (size_t)p->rows[i] * p->cols[i] * sizeof(double2));
+    }
+    // candidates: lanes per segment (double-float: 2 or 4; FP64: 1) x work
+    // item sizes around the size-based default; each is planned, captured and
+    // timed on the real batch, the fastest is kept
+    const int64_t base = p->item_target_log2;
+    std::vector<int> groups = p->df ? std::vector<int>{2, 4} : std::vector<int>{1};
+    double best = 1e300;
+    int best_grp = p->grp;
+    int64_t best_log2 = base;
+    for (int grp : groups) {
+        for (int64_t dl = -2; dl <= 2; dl += 2) {
+            const int64_t l2 = std::min<int64_t>(40, std::max<int64_t>(8, base + dl));
+            int cpl = 0, gg = 0;
+            batch_shape(p->maxc, p->df, grp, &cpl, &gg);
+            p->cpl = cpl;
+            p->grp = gg;
+            p->grid = device_sms(p->device) * batch_bps(cpl, gg, p->df);
+            p->item_target_log2 = l2;
+            int rc = plan_build_items(p);
+            if (rc == GBPERM_OK) rc = plan_capture(p);
+            if (rc) return rc;
+            cudaError_t e = cudaGraphLaunch(p->graph, p->stream);  // warm-up
+            if (e == cudaSuccess) e = cudaEventRecord(p->ev0, p->stream);
+            for (int r = 0; r < reps && e == cudaSuccess; ++r) e = cudaGraphLaunch(p->graph, p->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(p->ev1, p->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_autotune: trial");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+            const double per = (double)ms / reps;
+            if (per < best) {
+                best = per;
+                best_grp = gg;
+                best_log2 = l2;
+            }
+        }
+    }
+    int cpl = 0, gg = 0;
+    batch_shape(p->maxc, p->df, best_grp, &cpl, &gg);
+    p->cpl = cpl;
+    p->grp = gg;
+    p->grid = device_sms(p->device) * batch_bps(cpl, gg, p->df);
+    p->item_target_log2 = best_log2;
+    int rc = plan_build_items(p);
+    if (rc == GBPERM_OK) rc = plan_capture(p);
+    if (rc) return rc;
+    if (best_ms) *best_ms = best;
+    return GBPERM_OK;
+}
+
+int gbperm_batch_plan_get_shape(gbperm_batch_plan* plan, int64_t* lanes_per_segment, int64_t* columns_per_lane) {
+    if (!plan || !plan->p) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_get_shape: null plan");
+    if (lanes_per_segment) *lanes_per_segment = plan->p->grp;
+    if (columns_per_lane) *columns_per_lane = plan->p->cpl;
+    return GBPERM_OK;
 }
 
 int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t* cols, int64_t count, int arith,

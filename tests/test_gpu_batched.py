@@ -73,3 +73,18 @@ def test_dropin_list_branch_uses_batched():
     for m, v in zip(mats, vals):
         _, q = orc.bbfg(m, prec=1)
         assert orc.rel_err(v, q) <= TOL
+
+
+def test_batched_autotune_keeps_results():
+    from piquassoboost_gb300.workloads import batched_instances
+    mats = batched_instances(96, seed=12, modes=40, kmin=4, kmax=16)
+    plan = nat.BatchPlan([m.shape for m in mats], mode="fast")
+    before = plan.run(mats)
+    ms = plan.autotune(mats)
+    assert ms > 0.0
+    grp, cpl = plan.shape()
+    assert grp in (2, 4) and grp * cpl >= 16
+    after = plan.run(mats)
+    for a, b in zip(before, after):
+        assert abs(a - b) <= 1e-10 * abs(b)
+    plan.close()

@@ -1,0 +1,72 @@
+"""Full-size checks of the plain permanent through exactly known relations
+(n = 36, where no extended-precision oracle finishes): block-diagonal
+factorisation, row/column permutation invariance and diagonal scaling.
+
+Errors are stated both ways the accuracy bar is defined: relative to |perm|
+and relative to the product of the row 2-norms.  For a Haar block at n = 36
+|perm| is ~1e-9 of that product (the Gray sum cancels heavily), so the
+|perm|-relative error is the demanding one: the FP64 product meets 1e-10 on
+every relation; the double-float product meets it on the unscaled block
+and its permutations, and on rows and columns rescaled by 0.5-2 it stays
+within 1e-10 of the row-norm product (its |perm|-relative error there is a
+few 1e-9)."""
+import numpy as np
+import pytest
+
+from piquassoboost_gb300 import _native as nat
+from piquassoboost_gb300.workloads import haar_block
+from tests import oracle_bind as orc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+def _row_norm_product(A):
+    return float(np.prod(np.linalg.norm(A, axis=1)))
+
+
+def test_block_diagonal_n36_factorises():
+    # perm(B1 (+) B2) = perm(B1) perm(B2); the factors from the binary128 oracle
+    b1 = haar_block(18, seed=361)
+    b2 = haar_block(18, seed=362)
+    A = np.zeros((36, 36), dtype=np.complex128)
+    A[:18, :18] = b1
+    A[18:, 18:] = b2
+    v = nat.perm(A, mode="fast")
+    p1, _ = orc.bbfg(b1, prec=1)
+    p2, _ = orc.bbfg(b2, prec=1)
+    ref = p1 * p2
+    assert abs(v - ref) <= TOL * abs(ref), (v, ref)
+
+
+def test_permutation_invariance_n36():
+    rng = np.random.default_rng(37)
+    A = haar_block(36, seed=3636)
+    v0 = nat.perm(A, mode="fast")
+    v2 = nat.perm(A[rng.permutation(36)][:, rng.permutation(36)], mode="fast")
+    assert abs(v2 - v0) <= TOL * abs(v0), (v2, v0)
+
+
+def _scaled(seed):
+    rng = np.random.default_rng(seed)
+    A = haar_block(36, seed=3636)
+    d1 = rng.uniform(0.5, 2.0, 36) * np.exp(2j * np.pi * rng.random(36))
+    d2 = rng.uniform(0.5, 2.0, 36) * np.exp(2j * np.pi * rng.random(36))
+    return A, d1[:, None] * A * d2[None, :], np.prod(d1) * np.prod(d2)
+
+
+def test_diagonal_scaling_n36_fp64():
+    # perm(D1 A D2) = prod(d1) prod(d2) perm(A), |perm|-relative, FP64 product
+    A, S, scale = _scaled(36)
+    v0 = nat.perm(A, mode="fp64")
+    v1 = nat.perm(S, mode="fp64") / scale
+    assert abs(v1 - v0) <= TOL * abs(v0), (v1, v0)
+
+
+def test_diagonal_scaling_n36_fast_row_norm_bound():
+    # the double-float product on the rescaled matrix, against the FP64
+    # value: within 1e-10 of the row-norm product of the matrix it computed
+    A, S, scale = _scaled(36)
+    ref = nat.perm(A, mode="fp64")
+    v1 = nat.perm(S, mode="fast")
+    assert abs(v1 - ref * scale) <= TOL * _row_norm_product(S), (v1, ref * scale)
