@@ -149,8 +149,9 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
 void gbperm_batch_plan_destroy(gbperm_batch_plan* plan);
 int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double* out, gbperm_stats* stats);
 /* Device-pointer form: d_packed and d_out on the device, enqueued on
- * stream; slots of trivial instances (an empty side, or rows >= cols + 2)
- * are not written. */
+ * stream (a copy into the plan's buffer, the kernels and one scatter launch
+ * into the caller's slot order; trivial instances -- an empty side, or
+ * rows >= cols + 2 -- get 1 or 0). */
 int gbperm_batch_plan_run_dev(gbperm_batch_plan* plan, const void* d_packed, void* d_out, void* stream);
 /* log2 of the Gray steps in one work item (the load-balancing grain);
  * setting it rebuilds the work list and the graph. */

@@ -358,6 +358,19 @@ __global__ void batched_finalize_kernel(BArgs p) {
     }
 }
 
+// Device-pointer results in the caller's slot order: slot i takes device
+// instance dev_index[i], or the host-decided value trivial[i] (1, or 0 for
+// rows >= cols + 2) when the instance never reached the device.
+__global__ void batched_scatter_kernel(const double* dout, const int* dev_index, const double* trivial,
+                                       long long count, double* out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int d = dev_index[i];
+        out[2 * i] = d >= 0 ? dout[2 * d] : trivial[i];
+        out[2 * i + 1] = d >= 0 ? dout[2 * d + 1] : 0.0;
+    }
+}
+
 template <int CPL, int GROUP, bool DF>
 int bps_t() {
     int nb = 0;
@@ -460,6 +473,8 @@ struct BatchPlan {
     unsigned int* dcounter = nullptr;
     cdd* dpart = nullptr;
     double* dout = nullptr;
+    int* ddev_index = nullptr;       // dev_index on the device (slot -> device instance)
+    double* dtrivial = nullptr;      // trivial values on the device
     // pinned host staging and the captured graph
     double* hin = nullptr;
     double* hout = nullptr;
@@ -649,6 +664,15 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
         }
     }
     p->steps = total_steps;
+    if (p->ninst > 0) {
+        // a device is needed from here on: report its absence as such
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+            cudaGetLastError();
+            plan_free(p);
+            return fail(GBPERM_ERR_NO_DEVICE, "no CUDA device visible: the GB300 permanent library needs a GPU");
+        }
+    }
     cudaError_t e = cudaGetDevice(&p->device);
     if (e != cudaSuccess) {
         plan_free(p);
@@ -681,6 +705,8 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
     size_t oO = take((size_t)std::max(1, p->ninst) * sizeof(BInstOut));
     size_t oC = take(sizeof(unsigned int));
     size_t oR = take((size_t)std::max(1, p->ninst) * 2 * sizeof(double));
+    size_t oX = take((size_t)std::max<int64_t>(1, p->count) * sizeof(int));
+    size_t oT = take((size_t)std::max<int64_t>(1, p->count) * sizeof(double));
     p->dbytes = off;
     e = cudaMalloc(&p->dbuf, p->dbytes);
     if (e == cudaSuccess) e = cudaMallocHost(&p->hin, std::max<size_t>(1, (size_t)p->total_elems) * sizeof(double2));
@@ -698,6 +724,17 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
     p->dinst = reinterpret_cast<BInst*>(p->dbuf + oI);
     p->diout = reinterpret_cast<BInstOut*>(p->dbuf + oO);
     p->dcounter = reinterpret_cast<unsigned int*>(p->dbuf + oC);
+    p->ddev_index = reinterpret_cast<int*>(p->dbuf + oX);
+    p->dtrivial = reinterpret_cast<double*>(p->dbuf + oT);
+    if (p->count > 0) {
+        e = cudaMemcpy(p->ddev_index, p->dev_index.data(), (size_t)p->count * sizeof(int), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(p->dtrivial, p->trivial.data(), (size_t)p->count * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            plan_free(p);
+            return cuda_fail(e, "gbperm_batch_plan_create: upload");
+        }
+    }
     p->dout = reinterpret_cast<double*>(p->dbuf + oR);
     int rc = plan_build_items(p);
     if (rc == GBPERM_OK) rc = plan_capture(p);
@@ -766,26 +803,27 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
 int gbperm_batch_plan_run_dev(gbperm_batch_plan* plan, const void* d_packed, void* d_out, void* stream) {
     if (!plan || !plan->p) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run_dev: null plan");
     BatchPlan* p = plan->p;
-    if (p->ninst == 0) return GBPERM_OK;
+    if (p->count == 0) return GBPERM_OK;
+    if (!d_out || (p->total_elems > 0 && !d_packed)) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_run_dev: null pointer");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // device-to-device gather of the non-trivial instances is the identity
-    // on the packed layout; results for trivial instances are left to the caller
-    cudaError_t e = cudaMemcpyAsync(p->dA, d_packed, (size_t)p->total_elems * sizeof(double2),
-                                    cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: copy");
-    cudaStream_t saved = p->stream;
-    p->stream = st;
-    e = plan_enqueue(p);
-    p->stream = saved;
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: launch");
-    // scatter: device instance d -> output slot i
-    for (int64_t i = 0; i < p->count; ++i) {
-        int d = p->dev_index[i];
-        if (d < 0) continue;
-        e = cudaMemcpyAsync(static_cast<double*>(d_out) + 2 * i, p->dout + 2 * d, 2 * sizeof(double),
-                            cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: scatter");
+    cudaError_t e = cudaSuccess;
+    if (p->ninst > 0) {
+        // device-to-device gather of the non-trivial instances is the identity
+        // on the packed layout
+        e = cudaMemcpyAsync(p->dA, d_packed, (size_t)p->total_elems * sizeof(double2), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: copy");
+        cudaStream_t saved = p->stream;
+        p->stream = st;
+        e = plan_enqueue(p);
+        p->stream = saved;
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: launch");
     }
+    // scatter: device instance d -> output slot i (trivial slots get their value)
+    const long long cnt = (long long)p->count;
+    const int sb = (int)std::min<long long>((cnt + 255) / 256, 1024);
+    batched_scatter_kernel<<<sb, 256, 0, st>>>(p->dout, p->ddev_index, p->dtrivial, cnt, static_cast<double*>(d_out));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run_dev: scatter");
     return GBPERM_OK;
 }
 

@@ -21,8 +21,10 @@ __device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
               __shfl_xor_sync(0xffffffffu, v.ih, m), __shfl_xor_sync(0xffffffffu, v.il, m)};
 }
 
-// x^e by squaring (e >= 1)
-__device__ __forceinline__ cf cf_pow(cf x, int e) {
+// x^e by squaring (e >= 1).  Not inlined: it is reached only for columns
+// of multiplicity > 1, and one copy instead of one per unrolled column keeps
+// the kernel's loop body in the instruction cache.
+__device__ __noinline__ cf cf_pow(cf x, int e) {
     cf acc = x;
     bool have = false;
     cf y = x;
@@ -43,7 +45,7 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);            // R x NP
     longlong2* s_a2 = s_a1 + p.R * NP;                                   // nd x NP
-    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);           // P
+    float2* s_w = reinterpret_cast<float2*>(s_a2 + p.nd * NP);           // P: weights as float pairs
     unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);  // P
     __shared__ int s_cpow[NP];
     __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
@@ -58,8 +60,12 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
         int r = e / NP, j = e % NP;
         s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
     }
+    // low-digit weights (exact integers) as float pairs, converted once here
+    // instead of on the FP64 pipe every step
     for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
-        s_w[e] = p.wlow[e];
+        const double w = p.wlow[e];
+        const float wh = (float)w;
+        s_w[e] = make_float2(wh, (float)(w - (double)wh));
         s_seq[e] = p.seq[e];
     }
     for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
@@ -148,6 +154,8 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
                 Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
                 if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
                 widx += up ? s_stride[d] : -s_stride[d];
+                // the direction differs between segments; a branch measured
+                // faster here than a sign mask (fewer ALU instructions)
                 const longlong2* a = s_a2 + d * NP + j0;
                 if (up) {
 #pragma unroll
@@ -189,10 +197,8 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
             for (int m = 1; m < GROUP; m <<= 1) pa = cf_mul(pa, shfl_xor_cf(pa, m));
             if (leader && active) {
                 // weight: exact integer table entry (<= 2^53 here) as a float pair
-                const double w = s_w[widx];
-                const float wh = (float)w;
-                const float wl = (float)(w - (double)wh);
-                cf t = cf_mul(pa, cf{wh, wl, 0.f, 0.f});
+                const float2 w = s_w[widx];
+                cf t = cf_mul(pa, cf{w.x, w.y, 0.f, 0.f});
                 df_acc(brh, brl, __uint_as_float(__float_as_uint(t.rh) ^ sbit),
                        __uint_as_float(__float_as_uint(t.rl) ^ sbit));
                 df_acc(bih, bil, __uint_as_float(__float_as_uint(t.ih) ^ sbit),
@@ -233,7 +239,7 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
 
 template <int CPL, int GROUP>
 size_t rep_df_smem(const RepArgs& a) {
-    return (size_t)(a.R + a.nd) * CPL * GROUP * sizeof(longlong2) + (size_t)a.P * (sizeof(double) + 1) + 16;
+    return (size_t)(a.R + a.nd) * CPL * GROUP * sizeof(longlong2) + (size_t)a.P * (sizeof(float2) + 1) + 16;
 }
 
 template <int CPL, int GROUP>

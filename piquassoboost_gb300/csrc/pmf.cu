@@ -271,8 +271,10 @@ __device__ __forceinline__ cf shfl_cf(const cf& v, int src) {
               __shfl_sync(0xffffffffu, v.ih, src), __shfl_sync(0xffffffffu, v.il, src)};
 }
 
-// x^e by squaring (e >= 1)
-__device__ __forceinline__ cf cf_pow_pos(cf x, int e) {
+// x^e by squaring (e >= 1).  Not inlined: it is reached only for columns
+// of multiplicity > 1, and one copy instead of one per unrolled column keeps
+// the kernel's loop body in the instruction cache.
+__device__ __noinline__ cf cf_pow_pos(cf x, int e) {
     cf acc = x;
     bool have = false;
     cf y = x;
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
     cdd* s_acc = reinterpret_cast<cdd*>(smem_raw);                           // CPL x kThreads
     longlong2* s_a1 = reinterpret_cast<longlong2*>(s_acc + CPL * kThreads);  // R x NP (interleaved)
     longlong2* s_a2 = s_a1 + p.R * NP;                                       // nd x NP (interleaved)
-    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);               // P
+    float2* s_w = reinterpret_cast<float2*>(s_a2 + p.nd * NP);               // P: weights as float pairs
     unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);      // P
     __shared__ int s_cpow[NP];
     __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
@@ -325,7 +327,9 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
         s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
     }
     for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
-        s_w[e] = p.wlow[e];
+        const double w = p.wlow[e];
+        const float wh = (float)w;
+        s_w[e] = make_float2(wh, (float)(w - (double)wh));
         s_seq[e] = p.seq[e];
     }
     for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
@@ -466,9 +470,9 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
             cf o2 = shfl_cf(part, lbase + ((g + 2) & 3));
             cf o3 = shfl_cf(part, lbase + ((g + 3) & 3));
             // low-digit weight: exact integer table entry as a float pair
-            const double w = s_w[widx];
-            const float wh = __fmul_rn((float)w, wgt);
-            const float wl = __fmul_rn((float)(w - (double)(float)w), wgt);
+            const float2 w = s_w[widx];
+            const float wh = __fmul_rn(w.x, wgt);
+            const float wl = __fmul_rn(w.y, wgt);
             cf seed = cf_mul(cf_mul(cf_mul(o1, o2), o3), cf{wh, wl, 0.f, 0.f});
             seed = cf{__uint_as_float(__float_as_uint(seed.rh) ^ sbit), __uint_as_float(__float_as_uint(seed.rl) ^ sbit),
                       __uint_as_float(__float_as_uint(seed.ih) ^ sbit), __uint_as_float(__float_as_uint(seed.il) ^ sbit)};

@@ -129,3 +129,38 @@ def test_connector_empty_list_quirk():
 
     assert cpp_permanent_function(np.eye(2), [], []) == 1.0
     assert cpp_permanent_function(np.eye(2), np.zeros(2, np.int64), np.zeros(2, np.int64)) == 1
+
+
+def test_new_entry_points_validate_before_the_device(lib):
+    # argument and state errors are reported without a GPU, as for the permanents
+    U = np.eye(4, dtype=np.complex128)
+    with pytest.raises(nat.GBPermError) as e:
+        nat.compute_pmf(U, [1, 1, 0, 0], [1, 1, 0, 0])
+    assert e.value.code == nat.GBPERM_ERR_STATE_SUM
+    with pytest.raises(nat.GBPermError) as e:
+        nat.compute_pmf(U, [-1, 1, 0, 0], [1, 1, 0, 0])
+    assert e.value.code == nat.GBPERM_ERR_ARG
+    with pytest.raises(nat.GBPermError) as e:
+        nat.perm_repeated_many(U, [([1, 0, 0, 0], [1, 0, 0, 0]), ([1, 1, 0, 0], [1, 0, 0, 0])])
+    assert e.value.code == nat.GBPERM_ERR_STATE_SUM
+    assert nat.perm_repeated_many(U, [([0, 0, 0, 0], [0, 0, 0, 0])]) == [1]
+    assert nat.perm_repeated(U, [0, 0, 0, 0], [0, 0, 0, 0], form="chinhuh") == 1
+    with pytest.raises(nat.GBPermError) as e:
+        nat.perm_repeated(U, [1, 1, 0, 0], [1, 0, 0, 0], form="chinhuh")
+    assert e.value.code == nat.GBPERM_ERR_STATE_SUM
+    with pytest.raises(nat.GBPermError) as e:
+        nat.perm_grad_batched(np.zeros((2, 40, 40), dtype=np.complex128))
+    assert e.value.code == nat.GBPERM_ERR_TOO_LARGE
+
+
+@pytest.mark.skipif(nat.load(build_if_missing=True).gbperm_device_count() > 0, reason="a GPU is present")
+def test_new_entry_points_need_a_gpu():
+    rng = np.random.default_rng(1)
+    U = np.linalg.qr(rng.standard_normal((6, 6)) + 1j * rng.standard_normal((6, 6)))[0]
+    for call in (lambda: nat.compute_pmf(U, [1, 0, 0, 0, 0, 0], [1, 1, 0, 0, 0, 0]),
+                 lambda: nat.perm_repeated_many(U, [([1, 1, 0, 0, 0, 0], [0, 1, 1, 0, 0, 0])]),
+                 lambda: nat.perm_repeated(U, [1, 1, 0, 0, 0, 0], [0, 1, 1, 0, 0, 0], form="chinhuh"),
+                 lambda: nat.perm_grad_batched(np.stack([U, U]))):
+        with pytest.raises(nat.GBPermError) as e:
+            call()
+        assert e.value.code == nat.GBPERM_ERR_NO_DEVICE

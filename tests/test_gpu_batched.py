@@ -88,3 +88,25 @@ def test_batched_autotune_keeps_results():
     for a, b in zip(before, after):
         assert abs(a - b) <= 1e-10 * abs(b)
     plan.close()
+
+
+def test_batched_device_pointer_run_with_trivial_slots():
+    torch = pytest.importorskip("torch")
+    import ctypes
+    rng = np.random.default_rng(21)
+    mats = [rng.standard_normal((k, k)) + 1j * rng.standard_normal((k, k)) for k in (5, 9, 12)]
+    mats.insert(1, np.zeros((0, 0), dtype=np.complex128))          # empty -> 1
+    mats.append(rng.standard_normal((6, 3)) + 0j)                   # rows >= cols + 2 -> 0
+    plan = nat.BatchPlan([m.shape for m in mats], mode="fast")
+    host = plan.run(mats)
+    packed = torch.from_numpy(plan.pack(mats)).to("cuda")
+    out = torch.full((2 * len(mats),), 7.0, dtype=torch.float64, device="cuda")
+    P = ctypes.c_void_p
+    nat.check(nat.load().gbperm_batch_plan_run_dev(plan._h, P(packed.data_ptr()), P(out.data_ptr()),
+                                                   P(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    dev = out.cpu().numpy().reshape(-1, 2)
+    for (re, im), h in zip(dev, host):
+        assert abs(complex(re, im) - h) <= 1e-12 * max(abs(h), 1.0)
+    assert complex(*dev[1]) == 1.0 and complex(*dev[-1]) == 0.0
+    plan.close()
