@@ -29,6 +29,23 @@ namespace {
 
 constexpr int kThreads = 128;
 
+// x^e by squaring (e >= 1).  Out of line: reached only for multiplicities
+// above 1, and it keeps speculated multiplies off the common path.
+__device__ __noinline__ cd cd_pow(cd x, int e) {
+    cd acc = x;
+    bool have = false;
+    cd y = x;
+    while (e > 0) {
+        if (e & 1) {
+            acc = have ? cmul(acc, y) : y;
+            have = true;
+        }
+        e >>= 1;
+        if (e) y = cmul(y, y);
+    }
+    return acc;
+}
+
 template <int NMAX>
 __global__ void __launch_bounds__(kThreads) repeated_kernel(RepArgs p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -155,34 +172,24 @@ __global__ void __launch_bounds__(kThreads) repeated_kernel(RepArgs p) {
                     bim = 0.0;
                 }
             }
-            // prod_j colsum_j^(c_j), powers by squaring; sign in factor 0
+            // prod_j colsum_j^(c_j); the sign goes into factor 0; powers above
+            // 1 (rare) through an out-of-line helper, so the common path holds
+            // exactly one complex multiply per column
             cd pr;
-            pr.re = __longlong_as_double((long long)neg | __double_as_longlong(1.0));
-            pr.im = 0.0;
-            bool first = true;
+            {
+                cd x0{fix_to_double(cre[0]), fix_to_double(cim[0])};
+                const int e0 = s_cpow[0];
+                if (e0 != 1) x0 = cd_pow(x0, e0);
+                pr.re = __longlong_as_double(__double_as_longlong(x0.re) ^ (long long)neg);
+                pr.im = __longlong_as_double(__double_as_longlong(x0.im) ^ (long long)neg);
+            }
 #pragma unroll
-            for (int j = 0; j < NMAX; ++j) {
+            for (int j = 1; j < NMAX; ++j) {
                 if (j < C) {
                     cd x{fix_to_double(cre[j]), fix_to_double(cim[j])};
-                    int e = s_cpow[j];
-                    cd y = x;
-                    bool have = false;
-                    cd acc_pow{1.0, 0.0};
-                    while (e > 0) {
-                        if (e & 1) {
-                            acc_pow = have ? cmul(acc_pow, y) : y;
-                            have = true;
-                        }
-                        e >>= 1;
-                        if (e) y = cmul(y, y);
-                    }
-                    if (first) {
-                        pr.re = __longlong_as_double(__double_as_longlong(acc_pow.re) ^ (long long)neg);
-                        pr.im = __longlong_as_double(__double_as_longlong(acc_pow.im) ^ (long long)neg);
-                        first = false;
-                    } else {
-                        pr = cmul(pr, acc_pow);
-                    }
+                    const int e = s_cpow[j];
+                    if (e != 1) x = cd_pow(x, e);
+                    pr = cmul(pr, x);
                 }
             }
             const double w = s_w[widx];

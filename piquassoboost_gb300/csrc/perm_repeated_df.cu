@@ -179,8 +179,9 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
                     brh = brl = bih = bil = 0.f;
                 }
             }
+            // a lane's columns are contiguous, so padding (power 0) only ever
+            // follows its real columns: the first one starts the product
             cf pa{1.f, 0.f, 0.f, 0.f};
-            bool first = true;
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
                 const int e = s_cpow[j0 + c];  // 0 for padded columns
@@ -189,8 +190,7 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
                     fix_to_df_magic(cre[c], cv, x.rh, x.rl);
                     fix_to_df_magic(cim[c], cv, x.ih, x.il);
                     if (e > 1) x = cf_pow(x, e);
-                    pa = first ? x : cf_mul(pa, x);
-                    first = false;
+                    pa = c == 0 ? x : cf_mul(pa, x);
                 }
             }
 #pragma unroll

@@ -43,8 +43,14 @@ __device__ __forceinline__ cd shfl_cd(cd v, int src) {
     return cd{__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src)};
 }
 
-// x^e for e >= 1 by squaring
-__device__ __forceinline__ cd cpow_pos(cd x, int e) {
+// x^e for e >= 1 by squaring.  Out of line: reached only for multiplicities
+// above 1, and it keeps speculated multiplies off the common path.
+__device__ __noinline__ cd cpow_pos(cd x, int e);
+
+// z * x^e (e >= 1), out of line for the same reason
+__device__ __noinline__ cd cmul_pow(cd z, cd x, int e) { return cmul(z, cpow_pos(x, e)); }
+
+__device__ __noinline__ cd cpow_pos(cd x, int e) {
     cd acc = x;
     bool have = false;
     cd y = x;
@@ -227,7 +233,7 @@ __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part)
                 cd lo = c == CPL - 1 ? run : cmul(run, suf[c]);
                 if (e > 1) {
                     cd x{fix_to_double(cre[c]), fix_to_double(cim[c])};
-                    lo = cmul(lo, cpow_pos(x, e - 1));
+                    lo = cmul_pow(lo, x, e - 1);
                 }
                 blk[c].re += lo.re;
                 blk[c].im += lo.im;
@@ -274,6 +280,11 @@ __device__ __forceinline__ cf shfl_cf(const cf& v, int src) {
 // x^e by squaring (e >= 1).  Not inlined: it is reached only for columns
 // of multiplicity > 1, and one copy instead of one per unrolled column keeps
 // the kernel's loop body in the instruction cache.
+__device__ __noinline__ cf cf_pow_pos(cf x, int e);
+
+// z * x^e (e >= 1), out of line for the same reason
+__device__ __noinline__ cf cf_mul_pow(cf z, cf x, int e) { return cf_mul(z, cf_pow_pos(x, e)); }
+
 __device__ __noinline__ cf cf_pow_pos(cf x, int e) {
     cf acc = x;
     bool have = false;
@@ -481,7 +492,7 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
 #pragma unroll
             for (int c = CPL - 1; c >= 0; --c) {
                 cf lo = (c == 0) ? suf : cf_mul(pre[c], suf);
-                if (cp[c] > 1) lo = cf_mul(lo, cp[c] == 2 ? x[c] : cf_pow_pos(x[c], cp[c] - 1));
+                if (cp[c] > 1) lo = cf_mul_pow(lo, x[c], cp[c] - 1);
                 df_add_lazy2(Q[c].rh, Q[c].rl, lo.rh, lo.rl);
                 df_add_lazy2(Q[c].ih, Q[c].il, lo.ih, lo.il);
                 if (c > 0) suf = cf_mul(suf, P[c]);
