@@ -56,9 +56,21 @@ int ThreadCtx::ensure(size_t bytes) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (device != dev) {
-        // a new device for this thread: drop the old resources (they belong
-        // to the old device's context)
+        // a new device for this thread: release the old device's stream,
+        // events and workspace with that device current, then start afresh
+        if (device >= 0) {
+            if (cudaSetDevice(device) == cudaSuccess) {
+                if (dbuf) cudaFree(dbuf);
+                if (ev0) cudaEventDestroy(ev0);
+                if (ev1) cudaEventDestroy(ev1);
+                if (stream) cudaStreamDestroy(stream);
+            }
+            cudaGetLastError();
+            e = cudaSetDevice(dev);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+        }
         stream = nullptr;
+        ev0 = ev1 = nullptr;
         dbuf = nullptr;
         dcap = 0;
         device = dev;

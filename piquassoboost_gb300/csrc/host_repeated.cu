@@ -84,16 +84,16 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
     if (ri.size() > (size_t)kMaxRows || ci.size() > (size_t)GBPERM_MAX_DIM)
         return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_repeated: more than 64 occupied modes");
 
-    // Gray length of one orientation: prod (D_i + 1) with the fixed copy on
-    // the smallest multiplicity
+    // log2 of the Gray length of one orientation: prod (D_i + 1) with the
+    // fixed copy on the smallest multiplicity
     auto gray_len = [](const std::vector<int>& idx, const int64_t* mult) {
         int64_t mn = INT64_MAX;
         for (int i : idx) mn = std::min(mn, mult[i]);
-        long double t = 1.0L;
-        for (int i : idx) t *= (long double)(mult[i] + 1);
-        return t * (long double)mn / (long double)(mn + 1);
+        double t = 0.0;
+        for (int i : idx) t += std::log2((double)(mult[i] + 1));
+        return t + std::log2((double)mn / (double)(mn + 1));
     };
-    long double t_rows = gray_len(ri, row_mult), t_cols = gray_len(ci, col_mult);
+    const double t_rows = gray_len(ri, row_mult), t_cols = gray_len(ci, col_mult);
     bool transpose = chinhuh || (allow_transpose && t_cols < t_rows);
     h->transpose = transpose;
     const std::vector<int>& gi = transpose ? ci : ri;   // Gray-code side (rows of M)

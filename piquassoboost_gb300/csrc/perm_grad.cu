@@ -56,11 +56,6 @@ __device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
               __shfl_xor_sync(0xffffffffu, v.ih, m), __shfl_xor_sync(0xffffffffu, v.il, m)};
 }
 
-__device__ __forceinline__ cf shfl_cf(const cf& v, int src) {
-    return cf{__shfl_sync(0xffffffffu, v.rh, src), __shfl_sync(0xffffffffu, v.rl, src),
-              __shfl_sync(0xffffffffu, v.ih, src), __shfl_sync(0xffffffffu, v.il, src)};
-}
-
 // a += b without renormalisation: exact two-sum of the high parts, the low
 // parts and the rounding error collected in the low word.  Over m such adds
 // the low word stays below ~m 2^-24 of the running magnitude, so a
