@@ -2,6 +2,7 @@
 #pragma once
 #include <atomic>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -89,6 +90,16 @@ struct RepWs {
 int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
                   int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
                   bool* is_trivial, bool allow_transpose, int col_surplus, bool chinhuh = false);
+// Split the Gray range into segments of P = prod_{i<q} (D_i + 1) steps: the
+// q low digits walk inside a segment from the tables wlow / seq, the high
+// digits are decoded once per segment.  q minimises
+//   ceil(nseg / slots(P)) * (P + seg_cost)
+// over P <= 4096 -- the passes of the slowest segment slot times its steps
+// plus the per-segment setup expressed in steps -- where slots(P) is the
+// number of segments the launch runs at once for that table size.  Fills q,
+// P, nseg, wlow and seq.
+void repeated_low_digits(RepHost* h, const std::function<unsigned long long(unsigned long long)>& slots,
+                         double seg_cost);
 const std::vector<double>& binom_table();
 size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w);
 

@@ -131,33 +131,12 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
     unsigned long long T = 1ull;
     for (auto& d : digits) T *= (unsigned long long)(d.D + 1);
 
-    // low digits: grow P while segments stay plentiful (>= 64 per thread of
-    // a full grid) and the weight table small (<= 4096 entries)
-    int dev = 0;
-    cudaGetDevice(&dev);
-    unsigned long long threads = (unsigned long long)device_sms(dev) * 2ull * 128ull;
-    int64_t force_q = g_opt.repeated_low_digits.load();
-    int q = 0;
-    unsigned long long P = 1ull;
-    for (size_t i = 0; i < digits.size() && i < 16; ++i) {
-        if (digits[i].D > 15) break;
-        unsigned long long L = (unsigned long long)(digits[i].D + 1);
-        if (force_q >= 0) {
-            if ((int64_t)q >= force_q) break;
-        } else {
-            if (P * L > 4096ull) break;
-            if (T / (P * L) < 64ull * threads && P >= 16ull) break;
-        }
-        P *= L;
-        ++q;
-    }
-
     h->R = R;
     h->C = C;
     h->nd = (int)digits.size();
-    h->q = q;
-    h->P = P;
-    h->nseg = T / P;
+    h->q = 0;
+    h->P = 1;
+    h->nseg = T;
     h->steps = (double)T;
     h->photons = (int)sr;
     h->norm_shift = chinhuh ? (int)sr : (int)sr - 1;
@@ -184,7 +163,52 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
         h->cpow.push_back((int)pm[pj[c]]);
         h->col_src.push_back(pj[c]);
     }
-    // low-digit tables
+    double fl = 0.0;  // algorithmic flops: colsum updates + product + accumulate
+    int mults = 0;
+    for (int c = 0; c < C; ++c) mults += h->cpow[c];
+    mults -= 1;
+    fl = (2.0 * C + 6.0 * mults + 2.0) * (double)T;
+    h->flops = fl;
+    return GBPERM_OK;
+}
+
+void repeated_low_digits(RepHost* h, const std::function<unsigned long long(unsigned long long)>& slots,
+                         double seg_cost) {
+    const unsigned long long T = h->nseg * h->P;
+    // candidates: prefixes of the digit list with ranges <= 15 (4-bit packed
+    // in the kernels) and at most 4096 table entries
+    int qmax = 0;
+    unsigned long long Pmax = 1ull;
+    while (qmax < h->nd && qmax < 16 && h->D[qmax] <= 15 &&
+           Pmax * (unsigned long long)(h->D[qmax] + 1) <= 4096ull) {
+        Pmax *= (unsigned long long)(h->D[qmax] + 1);
+        ++qmax;
+    }
+    int q = 0;
+    const int64_t force_q = g_opt.repeated_low_digits.load();
+    if (force_q >= 0) {
+        q = (int)std::min<int64_t>(force_q, qmax);
+    } else {
+        double best = 0.0;
+        unsigned long long P = 1ull;
+        for (int c = 0; c <= qmax; ++c) {
+            if (c > 0) P *= (unsigned long long)(h->D[c - 1] + 1);
+            const unsigned long long nseg = T / P;
+            const unsigned long long s = std::max(1ull, slots(P));
+            const double cost = (double)((nseg + s - 1) / s) * ((double)P + seg_cost);
+            if (c == 0 || cost < best) {
+                best = cost;
+                q = c;
+            }
+        }
+    }
+    unsigned long long P = 1ull;
+    for (int i = 0; i < q; ++i) P *= (unsigned long long)(h->D[i] + 1);
+    h->q = q;
+    h->P = P;
+    h->nseg = T / P;
+    // low-digit tables: binomial weight of each low-digit combination and the
+    // digit that moves at each step of the reflected mixed-radix Gray walk
     h->wlow.assign(P, 1.0);
     h->seq.assign(P, 0);
     const std::vector<double>& bt = binom_table();
@@ -208,13 +232,6 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
             h->seq[k] = (unsigned char)d;
         }
     }
-    double fl = 0.0;  // algorithmic flops: colsum updates + product + accumulate
-    int mults = 0;
-    for (int c = 0; c < C; ++c) mults += h->cpow[c];
-    mults -= 1;
-    fl = (2.0 * C + 6.0 * mults + 2.0) * (double)T;
-    h->flops = fl;
-    return GBPERM_OK;
 }
 
 size_t repeated_ws_layout(const RepHost& h, int grid, RepWs* w) {
@@ -271,20 +288,6 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         if (out_dd) out_dd[0] = out_dd[1] = out_dd[2] = out_dd[3] = NAN;
         return GBPERM_OK;
     }
-    // launch geometry
-    RepArgs a{};
-    a.R = h.R;
-    a.C = h.C;
-    a.nd = h.nd;
-    a.q = h.q;
-    a.P = h.P;
-    a.nseg = h.nseg;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int bps = repeated_blocks_per_sm(a);
-    unsigned long long grid_full = (unsigned long long)device_sms(dev) * bps;
-    unsigned long long need = (h.nseg + 127ull) / 128ull;
-    int grid = (int)std::max(1ull, std::min(grid_full, need));
     // double-float product when requested and the dynamic range allows it
     bool df = false;
     int dcpl = 0, dgrp = 0, grid_df = 1;
@@ -293,9 +296,35 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         std::vector<int> cw(h.cpow.begin(), h.cpow.end());
         df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), cw.data(), &boost);
     }
+    if (df) repeated_df_shape(h.C, &dcpl, &dgrp);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long sms = (unsigned long long)device_sms(dev);
+    RepArgs a{};
+    a.R = h.R;
+    a.C = h.C;
+    a.nd = h.nd;
+    // segment length for the kernel that does the work: one thread per
+    // segment in the FP64 kernel, dgrp lanes per segment in the double-float
+    // one; setup costs (in steps) fitted to kernel times at 30 photons
+    repeated_low_digits(
+        &h,
+        [&](unsigned long long P) {
+            RepArgs t = a;
+            t.P = P;
+            if (df) return sms * (unsigned long long)repeated_df_blocks_per_sm(t, dcpl, dgrp) * (128ull / dgrp);
+            return sms * (unsigned long long)repeated_blocks_per_sm(t) * 128ull;
+        },
+        df ? 6.5 : 2.0);
+    a.q = h.q;
+    a.P = h.P;
+    a.nseg = h.nseg;
+    int bps = repeated_blocks_per_sm(a);
+    unsigned long long grid_full = sms * bps;
+    unsigned long long need = (h.nseg + 127ull) / 128ull;
+    int grid = (int)std::max(1ull, std::min(grid_full, need));
     if (df) {
-        repeated_df_shape(h.C, &dcpl, &dgrp);
-        unsigned long long gfull = (unsigned long long)device_sms(dev) * repeated_df_blocks_per_sm(a, dcpl, dgrp);
+        unsigned long long gfull = sms * repeated_df_blocks_per_sm(a, dcpl, dgrp);
         unsigned long long per_block = 128ull / (unsigned long long)dgrp;
         unsigned long long need_df = (h.nseg + per_block - 1) / per_block;
         grid_df = (int)std::max(1ull, std::min(gfull, need_df));

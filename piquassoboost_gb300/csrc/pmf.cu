@@ -720,9 +720,6 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         a.R = h.R;
         a.C = h.C;
         a.nd = h.nd;
-        a.q = h.q;
-        a.P = h.P;
-        a.nseg = h.nseg;
         pmf_shape(C, &cpl, &grp);
         // double-float product for up to 32 columns (4 lanes x 8) when the
         // dynamic range allows; the device check decides between the twins
@@ -737,6 +734,24 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     int dev = 0;
     cudaGetDevice(&dev);
     if (!first_photon) {
+        // both twins launch on one grid of grp lanes per segment; setup costs
+        // (in steps) fitted to kernel times of 60-mode, 30-photon layers --
+        // the double-float one flushes its per-column double-double
+        // accumulators once per segment
+        const unsigned long long sms = (unsigned long long)device_sms(dev);
+        repeated_low_digits(
+            &h,
+            [&](unsigned long long P) {
+                RepArgs t = a;
+                t.P = P;
+                int b = pmf_bps(t, cpl, grp);
+                if (df) b = std::min(b, pmf_df_bps(t, cpl));
+                return sms * (unsigned long long)b * (unsigned long long)(kThreads / grp);
+            },
+            df ? 20.0 : 2.0);
+        a.q = h.q;
+        a.P = h.P;
+        a.nseg = h.nseg;
         int bps = pmf_bps(a, cpl, grp);
         if (df) bps = std::min(bps, pmf_df_bps(a, cpl));
         unsigned long long full = (unsigned long long)device_sms(dev) * bps;
