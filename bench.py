@@ -126,7 +126,12 @@ def traffic_from_profile(n: int, mode: str):
 
 # --------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region."""
+    """nvidia-smi clock/throttle sampling during the timed region.
+
+    start() returns once the first sample has arrived; stop() waits for the
+    first sample after the region.  The report covers the samples inside the
+    region plus the last one before it and the first one after it, so a
+    region shorter than the 100 ms sampling interval is still bracketed."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -135,27 +140,37 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
         self.thread = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        deadline = time.perf_counter() + 5.0
+        while not self.lines and time.perf_counter() < deadline and self.proc.poll() is None:
+            time.sleep(0.005)
+        self.t0 = time.perf_counter()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.t1 = time.perf_counter()
+        deadline = self.t1 + 1.0
+        while (not self.lines or self.lines[-1][0] <= self.t1) and time.perf_counter() < deadline \
+                and self.proc.poll() is None:
+            time.sleep(0.005)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -163,9 +178,14 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
+        lines = list(self.lines)
+        before = [ln for ln in lines if ln[0] <= self.t0]
+        inside = [ln for ln in lines if self.t0 < ln[0] <= self.t1]
+        after = [ln for ln in lines if ln[0] > self.t1]
+        window = before[-1:] + inside + after[:1]
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in window:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -178,7 +198,7 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_inside": len(inside)}
 
 
 # ------------------------------------------------------------ reference arm
@@ -703,7 +723,7 @@ def _mesh(args, rank, world, torch):
     permanents and full gradients (one batched sweep), the loss and the phase
     gradient."""
     from piquassoboost_gb300.torch_perm import clements_unitary, permanent
-    from piquassoboost_gb300.workloads import mesh_instance
+    from piquassoboost_gb300.workloads import mesh_instance, mesh_unitary
 
     m, k, terms = 40, 12, 512
     insts = [mesh_instance(seed=args.seed + 1000 * rank + s, modes=m, photons=k, terms=terms)
@@ -771,7 +791,7 @@ def _mesh(args, rank, world, torch):
         from concurrent.futures import ThreadPoolExecutor
 
         orc = _oracle()
-        Uc = clements_unitary(torch.tensor(insts[args.warmup][0]), m).numpy()
+        Uc = mesh_unitary(insts[args.warmup][0], m)
         _, ins, outs = insts[args.warmup]
 
         def one_term(q):
@@ -798,7 +818,7 @@ def _mesh(args, rank, world, torch):
                "l2": "inputs < 1 MB; launch- and compute-bound, no flush"},
               _roof(flops, perm_ms, peak, "grad_kernel (batched; forward flops only)"),
               cpu, {"value": e2e, "unit": "(loss+grad)/s", "h2d_bytes_per_step": 1560 * 8,
-                    "d2h_bytes_per_step": 1560 * 8 + 8}, 5 * args.steps,
+                    "d2h_bytes_per_step": 1560 * 8 + 8}, 9 * args.steps,
               {"step_ms": ms, "permanent_kernels_ms": perm_ms}, clocks=clocks)
     return 0
 
@@ -837,13 +857,10 @@ def _reference_secondary(args, world):
     elif args.workload == "mesh":
         from concurrent.futures import ThreadPoolExecutor
 
-        import torch
-
-        from piquassoboost_gb300.torch_perm import clements_unitary
-        from piquassoboost_gb300.workloads import mesh_instance
+        from piquassoboost_gb300.workloads import mesh_instance, mesh_unitary
 
         ph, ins, outs = mesh_instance(seed=args.seed, modes=40, photons=12, terms=512)
-        Uc = clements_unitary(torch.tensor(ph), 40).numpy()
+        Uc = mesh_unitary(ph, 40)
 
         def one_term(q):
             A = Uc[np.ix_(outs[q], ins[q])]

@@ -215,6 +215,25 @@ size_t gbperm_perm_grad_batched_workspace_size(int64_t n, int64_t count);
 int gbperm_perm_grad_batched_dev(const void* dA, int64_t n, int64_t count, int64_t ld, int64_t stride, void* d_perm,
                                  void* d_grad, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------- Clements mesh */
+/* No reference counterpart: the differentiable interferometer in front of
+ * the batched gradient.  An m-mode Clements rectangular mesh (1 <= m <= 64)
+ * of m(m-1)/2 interferometers; layer l = 0..m-1 holds the pairs (i, i+1),
+ * i = l mod 2, l mod 2 + 2, ..., and interferometer t (layer by layer, then
+ * by i) with phases (theta, phi) = (phases[2t], phases[2t+1]) maps rows
+ * (i, i+1) by [[e^{i phi} cos theta, -sin theta], [e^{i phi} sin theta,
+ * cos theta]]; U = L_{m-1} ... L_0 (m x m complex128, row-major).
+ * The forward call keeps the layer states in the workspace
+ * (gbperm_mesh_workspace_size(m) bytes, 256-byte aligned); the backward
+ * call, given gU = dL/dRe(U) + i dL/dIm(U) for a real L, reads them back and
+ * writes dL/dphases (m(m-1) doubles), so the same workspace must pass
+ * unchanged from one to the other.  Both enqueue on `stream` and return. */
+size_t gbperm_mesh_workspace_size(int64_t m);
+int gbperm_mesh_unitary_dev(const void* d_phases, int64_t m, void* d_U, void* workspace, size_t workspace_bytes,
+                            void* stream);
+int gbperm_mesh_unitary_backward_dev(const void* d_phases, int64_t m, const void* d_gU, void* d_gphases,
+                                     void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------- allocation-free plain permanent */
 /* No counterpart in the reference.  The plain permanent for callers that
  * cannot allocate device memory (their pool belongs to another allocator, or

@@ -100,6 +100,9 @@ _SIGNATURES = [
     ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, ctypes.c_int, _P, _P, _P]),
     ("gbperm_perm_repeated_batched", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _I64, ctypes.c_int, _P, _P]),
+    ("gbperm_mesh_workspace_size", ctypes.c_size_t, [_I64]),
+    ("gbperm_mesh_unitary_dev", ctypes.c_int, [_P, _I64, _P, _P, ctypes.c_size_t, _P]),
+    ("gbperm_mesh_unitary_backward_dev", ctypes.c_int, [_P, _I64, _P, _P, _P, ctypes.c_size_t, _P]),
 ]
 
 _lib = None

@@ -396,10 +396,11 @@ __device__ __forceinline__ dd two_prod(double a, double b) {
 
 // The permanent from its gradient: perm is linear in every row, so
 // perm = sum_l a_kl dperm/da_kl for each row k (Laplace expansion along k).
-// One warp per matrix, lane k evaluates row k's sum in double-double
-// (products exact by FMA) and its condition sum_l |a_kl| |G_kl| / |sum|; the
-// best-conditioned row gives the result, so the sweep needs no separate
-// permanent term.
+// One warp per matrix: lane k estimates the condition
+// sum_l |a_kl| |G_kl| / |sum| of row k in plain FP64, and the
+// best-conditioned row is then summed in double-double (products exact by
+// FMA) with one term per lane, so the sweep needs no separate permanent
+// term.
 __global__ void grad_perm_kernel(const double2* A, long long ld, long long stride, int n, const double* grad,
                                  const int* df_info, double* perm2, double* perm4) {
     const size_t inst = blockIdx.x;
@@ -416,21 +417,21 @@ __global__ void grad_perm_kernel(const double2* A, long long ld, long long strid
         }
         return;
     }
-    cdd s{{0.0, 0.0}, {0.0, 0.0}};
-    double mag = 0.0;
+    // condition estimate of every row's expansion in plain FP64 (it only
+    // picks the row): |sum| and sum_l |a_kl| |G_kl| in the 1-norm of C
+    double cond = INFINITY;
     if (k < n) {
+        double sr = 0.0, si = 0.0, mag = 0.0;
         for (int l = 0; l < n; ++l) {
             const double2 a = A[(long long)k * ld + l];
             const double gr = grad[2 * (k * n + l)], gi = grad[2 * (k * n + l) + 1];
-            s.re = dd_add(s.re, two_prod(a.x, gr));
-            s.re = dd_add(s.re, two_prod(-a.y, gi));
-            s.im = dd_add(s.im, two_prod(a.x, gi));
-            s.im = dd_add(s.im, two_prod(a.y, gr));
-            mag += hypot(a.x, a.y) * hypot(gr, gi);
+            sr = fma(a.x, gr, fma(-a.y, gi, sr));
+            si = fma(a.x, gi, fma(a.y, gr, si));
+            mag += (fabs(a.x) + fabs(a.y)) * (fabs(gr) + fabs(gi));
         }
+        const double absv = fabs(sr) + fabs(si);
+        cond = absv > 0.0 ? mag / absv : (mag > 0.0 ? INFINITY : 1.0);
     }
-    const double absv = hypot(s.re.hi, s.im.hi);
-    double cond = k < n ? (absv > 0.0 ? mag / absv : (mag > 0.0 ? INFINITY : 1.0)) : INFINITY;
     int best = k;
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) {
@@ -441,7 +442,26 @@ __global__ void grad_perm_kernel(const double2* A, long long ld, long long strid
             best = ob;
         }
     }
-    if (k == best) {
+    // the chosen row exactly: lane l holds a_bl G_bl (exact products as
+    // double-doubles), summed by a butterfly; fl addition commutes and TwoSum
+    // is exact, so every lane ends with the same total
+    cdd s{{0.0, 0.0}, {0.0, 0.0}};
+    if (k < n) {
+        const double2 a = A[(long long)best * ld + k];
+        const double gr = grad[2 * (best * n + k)], gi = grad[2 * (best * n + k) + 1];
+        s.re = dd_add(two_prod(a.x, gr), two_prod(-a.y, gi));
+        s.im = dd_add(two_prod(a.x, gi), two_prod(a.y, gr));
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        cdd o;
+        o.re.hi = __shfl_xor_sync(0xffffffffu, s.re.hi, m);
+        o.re.lo = __shfl_xor_sync(0xffffffffu, s.re.lo, m);
+        o.im.hi = __shfl_xor_sync(0xffffffffu, s.im.hi, m);
+        o.im.lo = __shfl_xor_sync(0xffffffffu, s.im.lo, m);
+        s = cdd_add(s, o);
+    }
+    if (k == 0) {
         perm2[0] = s.re.hi + s.re.lo;
         perm2[1] = s.im.hi + s.im.lo;
         if (perm4) {

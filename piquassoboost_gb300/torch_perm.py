@@ -118,55 +118,51 @@ def permanent(A: torch.Tensor) -> torch.Tensor:
     return Permanent.apply(A)
 
 
-_MESH_CACHE: dict = {}
+class ClementsMesh(torch.autograd.Function):
+    """The mesh unitary (gbperm_mesh_unitary_dev) and its phase adjoint
+    (gbperm_mesh_unitary_backward_dev); the layer states stay in a device
+    workspace from the forward pass to the backward pass."""
 
+    @staticmethod
+    def forward(ctx, phases, m):
+        lib = nat.load()
+        ws_bytes = int(lib.gbperm_mesh_workspace_size(m))
+        if ws_bytes == 0:
+            raise ValueError("clements_unitary: modes must be in 1..64")
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=phases.device)
+        U = torch.empty((m, m), dtype=torch.complex128, device=phases.device)
+        with torch.cuda.device(phases.device):
+            nat.check(lib.gbperm_mesh_unitary_dev(_P(phases.data_ptr()), m, _P(U.data_ptr()), _P(ws.data_ptr()),
+                                                  ws_bytes, _stream_ptr(phases)))
+        ctx.save_for_backward(phases)
+        ctx.ws = ws
+        ctx.m = m
+        return U
 
-def _mesh_indices(m: int, device):
-    """Index tensors of an m-mode Clements mesh: for interferometer t (in
-    phase order) its layer and top mode, plus the identity mask of the modes
-    a layer leaves alone."""
-    key = (m, str(device))
-    if key not in _MESH_CACHE:
-        lay, top = [], []
-        for layer in range(m):
-            for i in range(layer % 2, m - 1, 2):
-                lay.append(layer)
-                top.append(i)
-        lay_t = torch.tensor(lay, device=device)
-        top_t = torch.tensor(top, device=device)
-        base = torch.eye(m, dtype=torch.complex128, device=device).repeat(m, 1, 1)
-        base[lay_t, top_t, top_t] = 0
-        base[lay_t, top_t + 1, top_t + 1] = 0
-        _MESH_CACHE[key] = (lay_t, top_t, base)
-    return _MESH_CACHE[key]
+    @staticmethod
+    def backward(ctx, gU):
+        (phases,) = ctx.saved_tensors
+        lib = nat.load()
+        gU = gU.to(torch.complex128).contiguous()
+        g = torch.empty_like(phases)
+        with torch.cuda.device(phases.device):
+            nat.check(lib.gbperm_mesh_unitary_backward_dev(_P(phases.data_ptr()), ctx.m, _P(gU.data_ptr()),
+                                                           _P(g.data_ptr()), _P(ctx.ws.data_ptr()), ctx.ws.numel(),
+                                                           _stream_ptr(phases)))
+        return g, None
 
 
 def clements_unitary(phases: torch.Tensor, m: int) -> torch.Tensor:
-    """m x m unitary of a Clements rectangular mesh of m(m-1)/2 Mach-Zehnder
-    interferometers, two phases (theta, phi) each: phases has m(m-1) entries.
-    Layer l holds the interferometers on mode pairs (i, i+1), i = l mod 2,
-    l mod 2 + 2, ...; each maps rows (i, i+1) of the running matrix by
+    """m x m unitary (complex128) of a Clements rectangular mesh of m(m-1)/2
+    Mach-Zehnder interferometers, two phases (theta, phi) each: phases has
+    m(m-1) entries, on a CUDA device.  Layer l holds the interferometers on
+    mode pairs (i, i+1), i = l mod 2, l mod 2 + 2, ...; each maps rows
+    (i, i+1) of the running matrix by
     [[e^{i phi} cos theta, -sin theta], [e^{i phi} sin theta, cos theta]],
-    so U = L_{m-1} ... L_1 L_0.  The m layer matrices are built in one
-    scatter and multiplied in a binary tree of batched products (about log2 m
-    launches each way).  Differentiable torch ops, complex128, on
-    phases.device."""
-    dev = phases.device
-    lay, top, base = _mesh_indices(m, dev)
-    theta = phases[0::2]
-    phi = phases[1::2]
-    e_phi = torch.exp(1j * phi.to(torch.complex128))
-    c = torch.cos(theta).to(torch.complex128)
-    s = torch.sin(theta).to(torch.complex128)
-    li = torch.cat([lay, lay, lay, lay])
-    ri = torch.cat([top, top, top + 1, top + 1])
-    ci = torch.cat([top, top + 1, top, top + 1])
-    vals = torch.cat([e_phi * c, -s, e_phi * s, c])
-    D = base.index_put((li, ri, ci), vals, accumulate=True)   # (m, m, m): layer matrices
-    # U = D[m-1] @ ... @ D[0]: pairwise products, later layer on the left
-    while D.shape[0] > 1:
-        k = D.shape[0]
-        even = k - (k % 2)
-        prod = torch.bmm(D[1:even:2], D[0:even:2])
-        D = torch.cat([prod, D[even:]]) if k % 2 else prod   # an odd last layer stays last (leftmost)
-    return D[0]
+    so U = L_{m-1} ... L_1 L_0.  Differentiable with respect to the phases
+    (hand-written forward and adjoint kernels; no CPU path)."""
+    if not phases.is_cuda:
+        raise ValueError("clements_unitary: the phases must be a CUDA tensor (no CPU path)")
+    if phases.dim() != 1 or phases.numel() != m * (m - 1):
+        raise ValueError("clements_unitary: phases must hold m(m-1) entries")
+    return ClementsMesh.apply(phases.to(torch.float64).contiguous(), int(m))

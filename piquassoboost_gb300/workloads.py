@@ -74,3 +74,24 @@ def mesh_instance(seed: int, modes: int = 40, photons: int = 12, terms: int = 51
     ins = np.stack([np.sort(rng.choice(modes, size=photons, replace=False)) for _ in range(terms)])
     outs = np.stack([np.sort(rng.choice(modes, size=photons, replace=False)) for _ in range(terms)])
     return phases, ins.astype(np.int64), outs.astype(np.int64)
+
+
+def mesh_unitary(phases: np.ndarray, m: int) -> np.ndarray:
+    """Host (numpy) copy of the Clements mesh unitary that
+    ``torch_perm.clements_unitary`` builds on the device, for host-side
+    baselines: layer l holds the pairs (i, i+1), i = l mod 2, l mod 2 + 2, ...,
+    interferometer t (layer by layer, then by i) maps rows (i, i+1) by
+    [[e^{i phi} cos theta, -sin theta], [e^{i phi} sin theta, cos theta]]
+    with (theta, phi) = (phases[2t], phases[2t+1]); U = L_{m-1} ... L_0."""
+    u = np.eye(m, dtype=np.complex128)
+    t = 0
+    for layer in range(m):
+        for i in range(layer % 2, m - 1, 2):
+            th, ph = phases[2 * t], phases[2 * t + 1]
+            e = np.exp(1j * ph)
+            a, b, c, d = e * np.cos(th), -np.sin(th), e * np.sin(th), np.cos(th)
+            ri, ri1 = u[i].copy(), u[i + 1].copy()
+            u[i] = a * ri + b * ri1
+            u[i + 1] = c * ri + d * ri1
+            t += 1
+    return u

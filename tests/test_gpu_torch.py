@@ -17,6 +17,48 @@ def _modes(seed, m, k, count):
     return ins, outs
 
 
+@pytest.mark.parametrize("m", [1, 2, 3, 9, 16, 40, 64])
+def test_mesh_kernel_matches_torch_reference(m):
+    # forward: the native mesh against the plain-torch construction;
+    # backward: the phase adjoint against torch autograd through it, for a
+    # real loss with a random complex upstream weight
+    from piquassoboost_gb300.torch_perm import clements_unitary
+    from tests.mesh_reference import clements_unitary_torch
+    rng = np.random.default_rng(100 + m)
+    ph0 = rng.uniform(0, 2 * np.pi, m * (m - 1))
+    W = torch.tensor(rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m)), device="cuda")
+    pa = torch.tensor(ph0, device="cuda", requires_grad=True)
+    Ua = clements_unitary(pa, m)
+    pb = torch.tensor(ph0, device="cuda", requires_grad=True)
+    Ub = clements_unitary_torch(pb, m)
+    assert (Ua - Ub).abs().max().item() <= 1e-13
+    if m == 1:
+        return
+    (Ua * W).sum().abs().pow(2).backward()
+    (Ub * W).sum().abs().pow(2).backward()
+    scale = pb.grad.abs().max().item()
+    assert (pa.grad - pb.grad).abs().max().item() <= 1e-12 * max(1.0, scale)
+
+
+def test_mesh_kernel_deterministic_and_checked():
+    from piquassoboost_gb300.torch_perm import clements_unitary
+    m = 40
+    ph0 = np.random.default_rng(5).uniform(0, 2 * np.pi, m * (m - 1))
+    grads = []
+    for _ in range(2):
+        ph = torch.tensor(ph0, device="cuda", requires_grad=True)
+        U = clements_unitary(ph, m)
+        (U.real.sum() + U[3, 7].imag).backward()
+        grads.append(ph.grad.clone())
+    assert torch.equal(grads[0], grads[1])
+    with pytest.raises(ValueError):
+        clements_unitary(torch.zeros(65 * 64, device="cuda", dtype=torch.float64), 65)
+    with pytest.raises(ValueError):
+        clements_unitary(torch.zeros(12, dtype=torch.float64), 4)
+    with pytest.raises(ValueError):
+        clements_unitary(torch.zeros(11, device="cuda", dtype=torch.float64), 4)
+
+
 def test_clements_unitary_is_unitary():
     from piquassoboost_gb300.torch_perm import clements_unitary
     m = 10
