@@ -41,6 +41,31 @@ int device_sms(int dev) {
     return sms;
 }
 
+cudaError_t allow_max_dynamic_smem(const void* kernel) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, unsigned long long> done;  // kernel -> bitmask of devices
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    std::lock_guard<std::mutex> g(mu);
+    auto it = done.find(kernel);
+    if (it != done.end() && (it->second & bit)) return cudaSuccess;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa{};
+    e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (dyn > 0) {
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+        if (e != cudaSuccess) return e;
+    }
+    done[kernel] |= bit;
+    return cudaSuccess;
+}
+
 ThreadCtx& thread_ctx() {
     thread_local ThreadCtx c;
     return c;

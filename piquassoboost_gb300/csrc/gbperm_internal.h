@@ -10,6 +10,14 @@ namespace gbperm {
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Lift a kernel's dynamic shared-memory limit to the device's opt-in maximum
+// (less the kernel's static shared memory), once per kernel and device.  The
+// attribute is process-wide: setting it to each launch's own size lets a
+// second host thread lower it between another thread's set and launch.  The
+// size passed at launch (and to the occupancy query) still decides
+// occupancy.
+cudaError_t allow_max_dynamic_smem(const void* kernel);
+
 // ---------------------------------------------------------------- prepare
 // Per-matrix fixed-point preparation (device).  For each column j with
 // weight sum  B_j = max(sum_i w_i |Re a_ij|, sum_i w_i |Im a_ij|)  the column

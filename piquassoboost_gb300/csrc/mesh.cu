@@ -247,7 +247,7 @@ extern "C" int gbperm_mesh_unitary_dev(const void* d_phases, int64_t m, void* d_
     double2* coef = reinterpret_cast<double2*>(base + w.coef);
     if (nmzi > 0) mesh_coef_kernel<<<(nmzi + 127) / 128, 128, 0, st>>>(static_cast<const double*>(d_phases), nmzi, coef);
     const size_t smem = ((size_t)nmzi * 4 + kMeshMax) * sizeof(double2);
-    cudaError_t e = cudaFuncSetAttribute(mesh_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)mesh_forward_kernel);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_mesh_unitary_dev: shared memory");
     mesh_forward_kernel<<<(int)m, kMeshThreads, smem, st>>>(coef, (int)m, nmzi, static_cast<double2*>(d_U),
                                                             reinterpret_cast<double2*>(base + w.states));
@@ -272,7 +272,7 @@ extern "C" int gbperm_mesh_unitary_backward_dev(const void* d_phases, int64_t m,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double2* part = reinterpret_cast<double2*>(base + w.part);
     const size_t smem = ((size_t)nmzi * 4 + (size_t)m * m + kMeshMax) * sizeof(double2);
-    cudaError_t e = cudaFuncSetAttribute(mesh_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)mesh_backward_kernel);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_mesh_unitary_backward_dev: shared memory");
     mesh_backward_kernel<<<(int)m, kMeshThreads, smem, st>>>(reinterpret_cast<const double2*>(base + w.coef), (int)m,
                                                              nmzi, reinterpret_cast<const double2*>(base + w.states),

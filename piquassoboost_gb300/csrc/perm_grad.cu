@@ -503,10 +503,10 @@ static GradPlan plan_grad(int n, int count) {
     int nb = 0;
     size_t smem = gp.cpl == 4 ? grad_smem<4>(n) : grad_smem<8>(n);
     if (gp.cpl == 4) {
-        cudaFuncSetAttribute(grad_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)grad_kernel<4>);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, grad_kernel<4>, kThreads, smem);
     } else {
-        cudaFuncSetAttribute(grad_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)grad_kernel<8>);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, grad_kernel<8>, kThreads, smem);
     }
     if (nb < 1) nb = 1;

@@ -158,7 +158,7 @@ template <int NMAX>
 cudaError_t launch_plain_t(const PlainArgs& a, int grid, cudaStream_t st) {
     size_t smem = 2ull * a.rows * NMAX * sizeof(longlong2);
     auto kern = plain_kernel<NMAX>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)kern);
     if (e != cudaSuccess) return e;
     kern<<<grid, kThreads, smem, st>>>(a);
     return cudaGetLastError();
@@ -169,7 +169,7 @@ int blocks_per_sm_t(int rows) {
     int nb = 0;
     size_t smem = 2ull * rows * NMAX * sizeof(longlong2);
     auto kern = plain_kernel<NMAX>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)kern);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kThreads, smem);
     return nb > 0 ? nb : 1;
 }

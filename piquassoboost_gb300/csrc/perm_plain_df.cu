@@ -193,8 +193,7 @@ size_t df_smem(int rows) {
 template <int CPL, int GROUP>
 cudaError_t launch_df_t(const PlainArgs& a, int grid, cudaStream_t st) {
     size_t smem = df_smem<CPL, GROUP>(a.rows);
-    cudaError_t e = cudaFuncSetAttribute(plain_df_kernel<CPL, GROUP>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)plain_df_kernel<CPL, GROUP>);
     if (e != cudaSuccess) return e;
     plain_df_kernel<CPL, GROUP><<<grid, kThreads, smem, st>>>(a);
     return cudaGetLastError();
@@ -204,7 +203,7 @@ template <int CPL, int GROUP>
 int df_bps_t(int rows) {
     int nb = 0;
     size_t smem = df_smem<CPL, GROUP>(rows);
-    cudaFuncSetAttribute(plain_df_kernel<CPL, GROUP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)plain_df_kernel<CPL, GROUP>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, plain_df_kernel<CPL, GROUP>, kThreads, smem);
     return nb > 0 ? nb : 1;
 }

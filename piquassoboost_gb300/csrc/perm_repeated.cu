@@ -236,8 +236,7 @@ size_t rep_smem(const RepArgs& a) {
 template <int NMAX>
 cudaError_t launch_rep_t(const RepArgs& a, int grid, cudaStream_t st) {
     size_t smem = rep_smem<NMAX>(a);
-    cudaError_t e = cudaFuncSetAttribute(repeated_kernel<NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)repeated_kernel<NMAX>);
     if (e != cudaSuccess) return e;
     repeated_kernel<NMAX><<<grid, kThreads, smem, st>>>(a);
     return cudaGetLastError();
@@ -247,7 +246,7 @@ template <int NMAX>
 int rep_bps_t(const RepArgs& a) {
     int nb = 0;
     size_t smem = rep_smem<NMAX>(a);
-    cudaFuncSetAttribute(repeated_kernel<NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)repeated_kernel<NMAX>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, repeated_kernel<NMAX>, kThreads, smem);
     return nb > 0 ? nb : 1;
 }

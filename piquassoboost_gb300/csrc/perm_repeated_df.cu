@@ -245,8 +245,7 @@ size_t rep_df_smem(const RepArgs& a) {
 template <int CPL, int GROUP>
 cudaError_t launch_rep_df_t(const RepArgs& a, int grid, cudaStream_t st) {
     size_t smem = rep_df_smem<CPL, GROUP>(a);
-    cudaError_t e = cudaFuncSetAttribute(repeated_df_kernel<CPL, GROUP>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)repeated_df_kernel<CPL, GROUP>);
     if (e != cudaSuccess) return e;
     repeated_df_kernel<CPL, GROUP><<<grid, kThreads, smem, st>>>(a);
     return cudaGetLastError();
@@ -256,7 +255,7 @@ template <int CPL, int GROUP>
 int rep_df_bps_t(const RepArgs& a) {
     int nb = 0;
     size_t smem = rep_df_smem<CPL, GROUP>(a);
-    cudaFuncSetAttribute(repeated_df_kernel<CPL, GROUP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)repeated_df_kernel<CPL, GROUP>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, repeated_df_kernel<CPL, GROUP>, kThreads, smem);
     return nb > 0 ? nb : 1;
 }

@@ -580,7 +580,7 @@ template <int CPL, int G>
 int pmf_bps_t(const RepArgs& a) {
     int nb = 0;
     size_t smem = pmf_smem<CPL, G>(a);
-    cudaFuncSetAttribute(pmf_kernel<CPL, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)pmf_kernel<CPL, G>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pmf_kernel<CPL, G>, kThreads, smem);
     return nb > 0 ? nb : 1;
 }
@@ -589,7 +589,7 @@ template <int CPL, int G>
 cudaError_t pmf_launch_t(const RepArgs& a, cdd* col_part, int grid, cudaStream_t st) {
     size_t smem = pmf_smem<CPL, G>(a);
     cudaError_t e =
-        cudaFuncSetAttribute(pmf_kernel<CPL, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_dynamic_smem((const void*)pmf_kernel<CPL, G>);
     if (e != cudaSuccess) return e;
     pmf_kernel<CPL, G><<<grid, kThreads, smem, st>>>(a, col_part);
     return cudaGetLastError();
@@ -629,7 +629,7 @@ template <int CPL>
 int pmf_df_bps_t(const RepArgs& a) {
     int nb = 0;
     size_t smem = pmf_smem<CPL, 4>(a);
-    cudaFuncSetAttribute(pmf_df_kernel<CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_dynamic_smem((const void*)pmf_df_kernel<CPL>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pmf_df_kernel<CPL>, kThreads, smem);
     return nb > 0 ? nb : 1;
 }
@@ -637,7 +637,7 @@ int pmf_df_bps_t(const RepArgs& a) {
 template <int CPL>
 cudaError_t pmf_df_launch_t(const RepArgs& a, cdd* col_part, int grid, cudaStream_t st) {
     size_t smem = pmf_smem<CPL, 4>(a);
-    cudaError_t e = cudaFuncSetAttribute(pmf_df_kernel<CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem((const void*)pmf_df_kernel<CPL>);
     if (e != cudaSuccess) return e;
     pmf_df_kernel<CPL><<<grid, kThreads, smem, st>>>(a, col_part);
     return cudaGetLastError();
