@@ -214,6 +214,22 @@ __device__ __forceinline__ void fix_to_df_magic(long long x, const DfConv& k, fl
     l = __fadd_rn(e, f0);
 }
 
+// Segment of work slot u for the mixed-radix Gray sweeps.  Consecutive
+// segments differ by +-1 in one high Gray digit, so the parity of the high
+// digits is h & 1, and that parity alone fixes the start of the low digits
+// and hence the whole walk inside a segment (which digit moves, up or down).
+// A warp's S consecutive slots (S a power of two: segments per warp) are
+// given segments of one parity -- within each block of 2S slots the first S
+// take the block's even segments and the last S its odd ones -- so every
+// step's direction is warp-uniform.  Slots at or past `full` (nseg rounded
+// down to a multiple of 2S) keep u.
+__device__ __forceinline__ unsigned long long parity_slot(unsigned long long u, unsigned long long S,
+                                                          unsigned long long full) {
+    if (u >= full) return u;
+    const unsigned long long r = u & (2 * S - 1);
+    return (u - r) + (r < S ? 2 * r : 2 * (r - S) + 1);
+}
+
 // df accumulator: a += (h, l), renormalised
 __device__ __forceinline__ void df_acc(float& ah, float& al, float h, float l) {
     float s, e;

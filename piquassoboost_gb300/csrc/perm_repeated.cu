@@ -88,7 +88,9 @@ __global__ void __launch_bounds__(kThreads) repeated_kernel(RepArgs p) {
     const unsigned long long T = (unsigned long long)gridDim.x * blockDim.x;
     long long cre[NMAX], cim[NMAX];
 
-    for (unsigned long long h = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; h < p.nseg; h += T) {
+    const unsigned long long full = p.nseg / 64ull * 64ull;  // parity blocks of two warps' segments
+    for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; u < p.nseg; u += T) {
+        const unsigned long long h = parity_slot(u, 32ull, full);
         // --- decode the segment: high counter digits from h, Gray digits
         // from the top down (reflected when the digits above sum to odd);
         // low digits start at counter 0, i.e. at one end.
@@ -154,14 +156,26 @@ __global__ void __launch_bounds__(kThreads) repeated_kernel(RepArgs p) {
                 G = (G & ~(15ull << sh)) | ((unsigned long long)g << sh);
                 if (g == 0 || g == s_D[d]) dir ^= 1u << d;
                 widx += up ? s_stride[d] : -s_stride[d];
-                const long long m = up ? -1ll : 0ll;  // up: one more -1 delta -> subtract 2 a
+                // up: one more -1 delta -> subtract 2 a (warp-uniform: a
+                // warp's segments share their parity)
                 const longlong2* a = s_a2 + d * NMAX;
+                if (up) {
 #pragma unroll
-                for (int j = 0; j < NMAX; ++j) {
-                    if (j < C) {
-                        longlong2 v = a[j];
-                        cre[j] += (v.x ^ m) - m;
-                        cim[j] += (v.y ^ m) - m;
+                    for (int j = 0; j < NMAX; ++j) {
+                        if (j < C) {
+                            longlong2 v = a[j];
+                            cre[j] -= v.x;
+                            cim[j] -= v.y;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NMAX; ++j) {
+                        if (j < C) {
+                            longlong2 v = a[j];
+                            cre[j] += v.x;
+                            cim[j] += v.y;
+                        }
                     }
                 }
                 neg ^= 0x8000000000000000ull;

@@ -87,11 +87,13 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
     const unsigned long long lane_seg = (threadIdx.x & 31) / GROUP;
+    constexpr unsigned long long S = 32 / GROUP;  // segments per warp
+    const unsigned long long full = p.nseg / (2 * S) * (2 * S);
     long long cre[CPL], cim[CPL];
 
     for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / GROUP;
          hw < p.nseg; hw += T) {
-        const unsigned long long h_raw = hw + lane_seg;
+        const unsigned long long h_raw = parity_slot(hw + lane_seg, S, full);
         const bool active = h_raw < p.nseg;
         const unsigned long long h = active ? h_raw : 0ull;
         int gdig[kMaxDigits];
@@ -154,8 +156,7 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
                 Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
                 if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
                 widx += up ? s_stride[d] : -s_stride[d];
-                // the direction differs between segments; a branch measured
-                // faster here than a sign mask (fewer ALU instructions)
+                // warp-uniform: a warp's segments share their parity
                 const longlong2* a = s_a2 + d * NP + j0;
                 if (up) {
 #pragma unroll

@@ -115,11 +115,13 @@ __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part)
     // bound is warp-uniform so every shuffle runs with the full warp
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / G;
     const unsigned long long lane_seg = (unsigned long long)(lane / G);
+    constexpr unsigned long long S = 32 / G;  // segments per warp
+    const unsigned long long full = p.nseg / (2 * S) * (2 * S);
     long long cre[CPL], cim[CPL];
 
     for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / G;
          hw < p.nseg; hw += T) {
-        const unsigned long long h_raw = hw + lane_seg;
+        const unsigned long long h_raw = parity_slot(hw + lane_seg, S, full);
         const bool active = h_raw < p.nseg;
         const unsigned long long h = active ? h_raw : 0ull;
         int gdig[kMaxDigits];
@@ -185,13 +187,23 @@ __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part)
                 Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
                 if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
                 widx += up ? s_stride[d] : -s_stride[d];
-                const long long m = up ? -1ll : 0ll;  // up: one more -1 delta -> subtract 2 a
+                // up: one more -1 delta -> subtract 2 a (warp-uniform: a
+                // warp's segments share their parity)
                 const longlong2* a = s_a2 + d * NP + j0;
+                if (up) {
 #pragma unroll
-                for (int c = 0; c < CPL; ++c) {
-                    longlong2 v = a[c];
-                    cre[c] += (v.x ^ m) - m;
-                    cim[c] += (v.y ^ m) - m;
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] -= v.x;
+                        cim[c] -= v.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] += v.x;
+                        cim[c] += v.y;
+                    }
                 }
                 sgn = -sgn;
                 if ((k & 255ull) == 0) {
@@ -366,12 +378,14 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
     for (int c = 0; c < CPL; ++c) cp[c] = s_cpow[g * CPL + c];
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / G;
     const unsigned long long lane_seg = (unsigned long long)(lane / G);
+    constexpr unsigned long long S = 32 / G;  // segments per warp
+    const unsigned long long full = p.nseg / (2 * S) * (2 * S);
     long long cre[CPL], cim[CPL];
     cf Q[CPL];
 
     for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / G;
          hw < p.nseg; hw += T) {
-        const unsigned long long h_raw = hw + lane_seg;
+        const unsigned long long h_raw = parity_slot(hw + lane_seg, S, full);
         const bool active = h_raw < p.nseg;
         const unsigned long long h = active ? h_raw : 0ull;
         int gdig[kMaxDigits];
@@ -435,13 +449,23 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
                 Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
                 if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
                 widx += up ? s_stride[d] : -s_stride[d];
-                const long long m = up ? -1ll : 0ll;  // up: one more -1 delta -> subtract 2 a
+                // up: one more -1 delta -> subtract 2 a (warp-uniform: a
+                // warp's segments share their parity)
                 const longlong2* a = s_a2 + d * NP + g;
+                if (up) {
 #pragma unroll
-                for (int c = 0; c < CPL; ++c) {
-                    longlong2 v = a[c * G];
-                    cre[c] += (v.x ^ m) - m;
-                    cim[c] += (v.y ^ m) - m;
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c * G];
+                        cre[c] -= v.x;
+                        cim[c] -= v.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c * G];
+                        cre[c] += v.x;
+                        cim[c] += v.y;
+                    }
                 }
                 sbit ^= 0x80000000u;
                 if ((k & 255ull) == 0) {
