@@ -721,7 +721,8 @@ def _mesh(args, rank, world, torch):
     uniform phases, backpropagated to the 1560 phases.  A step is the whole
     forward and backward pass: mesh unitary, the 512 12 x 12 submatrices, their
     permanents and full gradients (one batched sweep), the loss and the phase
-    gradient."""
+    gradient, written as ordinary torch autograd code and replayed as one
+    CUDA graph (captured once; the eager step is timed beside it)."""
     from piquassoboost_gb300.torch_perm import clements_unitary, permanent
     from piquassoboost_gb300.workloads import mesh_instance, mesh_unitary
 
@@ -730,51 +731,85 @@ def _mesh(args, rank, world, torch):
              for s in range(args.warmup + args.steps)]
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.current_stream()
+    from piquassoboost_gb300.torch_perm import capture_graph
 
-    def step(ph_dev, ins, outs):
-        ph = ph_dev.detach().requires_grad_(True)
+    # the step over static input buffers: phases and the two index sets
+    s_ph = torch.zeros(m * (m - 1), dtype=torch.float64, device=dev)
+    s_o = torch.zeros((terms, k), dtype=torch.long, device=dev)
+    s_i = torch.zeros((terms, k), dtype=torch.long, device=dev)
+
+    def step():
+        ph = s_ph.detach().requires_grad_(True)
         U = clements_unitary(ph, m)
-        o = torch.as_tensor(outs, device=dev)
-        i = torch.as_tensor(ins, device=dev)
-        p = permanent(U[o[:, :, None], i[:, None, :]])
+        p = permanent(U[s_o[:, :, None], s_i[:, None, :]])
         loss = torch.log((p * p.conj()).real).sum()
-        loss.backward()
-        return loss.detach(), ph.grad
+        (g,) = torch.autograd.grad(loss, ph)
+        return loss.detach(), g
 
-    dev_in = [(torch.tensor(ph, device=dev), ins, outs) for ph, ins, outs in insts]
-    for ph, ins, outs in dev_in[:args.warmup]:
-        step(ph, ins, outs)
+    def load(ph, o, i, non_blocking=False):
+        s_ph.copy_(ph, non_blocking=non_blocking)
+        s_o.copy_(o, non_blocking=non_blocking)
+        s_i.copy_(i, non_blocking=non_blocking)
+
+    dev_in = [(torch.tensor(ph, device=dev), torch.tensor(outs, device=dev), torch.tensor(ins, device=dev))
+              for ph, ins, outs in insts]
+    load(*dev_in[0])
+    for q in range(args.warmup):
+        load(*dev_in[q])
+        step()
     torch.cuda.synchronize()
+    # eager (one launch per op, host-side autograd between launches)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for q in range(args.steps):
+        ev[q][0].record(stream)
+        load(*dev_in[args.warmup + q])
+        step()
+        ev[q][1].record(stream)
+    torch.cuda.synchronize()
+    eager_ms = [a.elapsed_time(b) for a, b in ev]
+    # the same step captured once as a CUDA graph; its replay must reproduce
+    # the eager result of the same inputs
+    graph, (g_loss, g_grad) = capture_graph(step, warmup=3)
+    load(*dev_in[args.warmup])
+    e_loss, e_grad = step()
+    graph.replay()
+    torch.cuda.synchronize()
+    if abs(e_loss.item() - g_loss.item()) > 1e-12 * abs(e_loss.item()) or \
+            (e_grad - g_grad).abs().max().item() > 1e-12 * max(1.0, e_grad.abs().max().item()):
+        raise RuntimeError("mesh step: CUDA-graph replay differs from the eager step")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clk = ClockSampler(torch.cuda.current_device())
     clk.start()
     t0 = time.perf_counter()
     for q in range(args.steps):
-        ph, ins, outs = dev_in[args.warmup + q]
         ev[q][0].record(stream)
-        step(ph, ins, outs)
+        load(*dev_in[args.warmup + q])
+        graph.replay()
         ev[q][1].record(stream)
     torch.cuda.synchronize()
     wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
     clocks = clk.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
     value = world * args.steps / (sum(ms) * 1e-3)
-    # e2e: phases from pinned host memory, loss and phase gradient back to the host
-    pinned = [torch.tensor(ph).pin_memory() for ph, _, _ in insts[args.warmup:]]
+    # e2e: phases and index sets from pinned host memory, loss and phase
+    # gradient back to the host, every step
+    pinned = [(torch.tensor(ph).pin_memory(), torch.tensor(outs).pin_memory(), torch.tensor(ins).pin_memory())
+              for ph, ins, outs in insts[args.warmup:]]
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for q in range(args.steps):
-        _, ins, outs = insts[args.warmup + q]
-        loss, g = step(pinned[q].to(dev, non_blocking=True), ins, outs)
-        loss.item()
-        g.cpu()
+        load(*pinned[q], non_blocking=True)
+        graph.replay()
+        g_loss.item()
+        g_grad.cpu()
     e2e = world * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
+    h2d = (m * (m - 1) + 2 * terms * k) * 8
     # the permanent kernels alone on the same 512 submatrices
     from piquassoboost_gb300.torch_perm import permanents_and_grads
-    ph, ins, outs = dev_in[args.warmup]
+    ph, o, i = dev_in[args.warmup]
     with torch.no_grad():
         U = clements_unitary(ph, m)
-        subs = U[torch.as_tensor(outs, device=dev)[:, :, None], torch.as_tensor(ins, device=dev)[:, None, :]]
+        subs = U[o[:, :, None], i[:, None, :]]
     permanents_and_grads(subs)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -815,11 +850,14 @@ def _mesh(args, rank, world, torch):
         _line(args, world, value, "(loss+grad)/s", 1000 * wall / args.steps,
               {"workload": "512 terms log|perm(U_S)|^2, 12 photons in a 40-mode Clements mesh (seeded uniform "
                            "phases, seeded mode sets), forward + backward to the 1560 phases", "arith": "fast",
+               "launch": "forward + backward captured once as a CUDA graph, one replay per step (checked equal "
+                         "to the eager step); eager timing in eager_step_ms",
                "l2": "inputs < 1 MB; launch- and compute-bound, no flush"},
               _roof(flops, perm_ms, peak, "grad_kernel (batched; forward flops only)"),
-              cpu, {"value": e2e, "unit": "(loss+grad)/s", "h2d_bytes_per_step": 1560 * 8,
+              cpu, {"value": e2e, "unit": "(loss+grad)/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 1560 * 8 + 8}, 9 * args.steps,
-              {"step_ms": ms, "permanent_kernels_ms": perm_ms}, clocks=clocks)
+              {"step_ms": ms, "eager_step_ms": eager_ms, "eager_steps_per_s": world * args.steps / (sum(eager_ms) * 1e-3),
+               "permanent_kernels_ms": perm_ms}, clocks=clocks)
     return 0
 
 

@@ -166,3 +166,24 @@ def clements_unitary(phases: torch.Tensor, m: int) -> torch.Tensor:
     if phases.dim() != 1 or phases.numel() != m * (m - 1):
         raise ValueError("clements_unitary: phases must hold m(m-1) entries")
     return ClementsMesh.apply(phases.to(torch.float64).contiguous(), int(m))
+
+
+def capture_graph(fn, warmup: int = 3):
+    """Capture ``fn()`` -- e.g. a forward + backward step built from
+    ``clements_unitary``, ``permanent`` and torch ops over static input
+    tensors -- as one CUDA graph.  The library's device entry points only
+    enqueue on the current stream and allocate through torch, so such a step
+    captures whole; one-time setup runs in the ``warmup`` eager calls, which
+    go to a side stream as torch's capture rules ask.  Returns
+    ``(graph, outputs)``: copy new inputs into the same tensors and call
+    ``graph.replay()``; ``outputs`` are then overwritten in place."""
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(warmup):
+            fn()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        outputs = fn()
+    return graph, outputs
