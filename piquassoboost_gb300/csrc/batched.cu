@@ -343,18 +343,25 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
     }
 }
 
+// warp per instance: lane l sums items l, l + 32, ... in order, then a fixed
+// butterfly (deterministic; a large instance has thousands of items)
 __global__ void batched_finalize_kernel(BArgs p) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.ninst; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.ninst; i += nw) {  // warp-uniform
         const BInst in = p.inst[i];
         const BInstOut io = p.iout[i];
         if (!io.finite) {
-            p.out[2 * i] = nan("");
-            p.out[2 * i + 1] = nan("");
+            if (lane == 0) {
+                p.out[2 * i] = nan("");
+                p.out[2 * i + 1] = nan("");
+            }
             continue;
         }
         cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (int k = 0; k < in.nitems; ++k) tot = cdd_add(tot, p.item_part[in.item0 + k]);
-        write_result(tot, io.exp, p.out + 2 * i, nullptr);
+        for (int k = lane; k < in.nitems; k += 32) tot = cdd_add(tot, p.item_part[in.item0 + k]);
+        tot = warp_sum_cdd(tot);
+        if (lane == 0) write_result(tot, io.exp, p.out + 2 * i, nullptr);
     }
 }
 
@@ -526,7 +533,7 @@ static cudaError_t plan_enqueue(BatchPlan* p) {
     if (e != cudaSuccess) return e;
     e = batch_launch(a, p->cpl, p->grp, p->df, p->grid, p->stream);
     if (e != cudaSuccess) return e;
-    batched_finalize_kernel<<<(p->ninst + 127) / 128, 128, 0, p->stream>>>(a);
+    batched_finalize_kernel<<<(p->ninst + 3) / 4, 128, 0, p->stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -172,16 +172,27 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
         s_last = (t == gridDim.x - 1);
     }
     __syncthreads();
-    if (s_last && threadIdx.x == 0) {
+    if (s_last) {
+        // the last block sums the block partials: thread t takes partials
+        // t, t + blockDim, ... in order, then a fixed butterfly and the warp
+        // order -- deterministic, and not one thread's serial chain of L2
+        // loads and dependent double-double adds
         __threadfence();
         cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (unsigned int bk = 0; bk < gridDim.x; ++bk) {
+        for (unsigned int bk = threadIdx.x; bk < gridDim.x; bk += blockDim.x) {
             const volatile double* q = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
             cdd v{{q[0], q[1]}, {q[2], q[3]}};
             tot = cdd_add(tot, v);
         }
-        write_result(tot, *p.exp_in, p.out2, p.out4);
-        *p.done = 0u;
+        tot = warp_sum_cdd(tot);
+        if (lane == 0) s_warp[warp] = tot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cdd all = s_warp[0];
+            for (int w = 1; w < kThreads / 32; ++w) all = cdd_add(all, s_warp[w]);
+            write_result(all, *p.exp_in, p.out2, p.out4);
+            *p.done = 0u;
+        }
     }
 }
 

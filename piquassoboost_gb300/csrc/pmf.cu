@@ -562,13 +562,19 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2* s_perm = reinterpret_cast<double2*>(smem_raw);  // C
     __shared__ double s_tot;
-    for (int j = threadIdx.x; j < C; j += blockDim.x) {
+    // column j: a warp sums the block partials (lane l takes blocks l, l + 32,
+    // ... in order, then a fixed butterfly: deterministic)
+    const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (int j = threadIdx.x >> 5; j < C; j += nwarps) {
         cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (int b = 0; b < nblocks; ++b) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
-        double o[2];
-        const int boost = df_info ? df_info[0] : 0;
-        write_result(tot, *exp_in - (col_e[j] - boost), o, nullptr);
-        s_perm[j] = make_double2(o[0], o[1]);
+        for (int b = lane; b < nblocks; b += 32) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
+        tot = warp_sum_cdd(tot);
+        if (lane == 0) {
+            double o[2];
+            const int boost = df_info ? df_info[0] : 0;
+            write_result(tot, *exp_in - (col_e[j] - boost), o, nullptr);
+            s_perm[j] = make_double2(o[0], o[1]);
+        }
     }
     for (int i = threadIdx.x; i < m; i += blockDim.x) addends[i] = make_double2(0.0, 0.0);
     __syncthreads();
