@@ -708,7 +708,7 @@ def _pmf(args, rank, world, torch):
                     "pmf_df_kernel (FP64-equivalent flops of the FP64 form)" if args.mode == "fast"
                     else "pmf_kernel (executed FP64 flops)"),
               cpu, {"value": e2e, "unit": "layers/s", "h2d_bytes_per_step": 60 * 60 * 16 + 2 * 60 * 8,
-                    "d2h_bytes_per_step": 60 * 8 + 60 * 16}, (4 if args.mode == "fast" else 3) * args.steps,
+                    "d2h_bytes_per_step": 60 * 8 + 60 * 16}, (5 if args.mode == "fast" else 3) * args.steps,
               {"permanents_per_s": value * nperm / args.steps,
                "kernel_ms": kms}, clocks=clocks)
     return 0

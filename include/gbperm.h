@@ -58,6 +58,13 @@ typedef struct gbperm_stats {
     int32_t grid;          /* blocks of the main launch */
     int32_t seg_log2;      /* log2 of the Gray segment length (plain / grad) */
     int32_t arith;         /* arithmetic actually used (GBPERM_ARITH_*) */
+    double err_est;        /* when the double-float product ran (plain, repeated, pmf, batched):
+                              estimated relative rounding error of its result,
+                              sqrt(n) 2^-46 sqrt(sum |term|^2) / |perm| (pmf: the largest over the
+                              layer's permanents; batched: the largest over the results kept in
+                              double-float).  Above 1e-10 the FP64 product recomputed the result (on
+                              the device; batched host calls: per instance on the host path) and
+                              arith reports FP64.  0 when only the FP64 product ran */
 } gbperm_stats;
 
 /* ------------------------------------------------------------- library */
@@ -72,6 +79,9 @@ int gbperm_device_count(void);
  *   "batched.threads"     force threads per instance of the batched kernel (0 = autotuned)
  *   "plain.df_group"      lanes sharing one Gray segment in the double-float kernel
  *                         (1, 2, 4 or 8; 0 = by column count)
+ *   "df.escalate"         1 (default): a double-float result whose error estimate exceeds
+ *                         1e-10 is recomputed by the FP64 kernel; 0: keep it (stats.err_est
+ *                         still reports the estimate)
  */
 int gbperm_set_option(const char* key, int64_t value);
 int64_t gbperm_get_option(const char* key);
@@ -88,8 +98,10 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
 /* Device-pointer form.  dA: device complex128 matrix; d_out: 2 doubles on
  * the device; d_out_dd: NULL or 4 doubles on the device.  The workspace must
  * hold gbperm_perm_workspace_size(rows, cols) bytes, 256-byte aligned.  With
- * GBPERM_ARITH_DF32 the range check runs on the device and the kernel falls
- * back to the FP64 product when it fails. */
+ * GBPERM_ARITH_DF32 the range check runs on the device and the FP64 product
+ * takes over when it fails, or when the double-float result's estimated
+ * relative rounding error exceeds 1e-10 (decided on the device, no host
+ * round trip). */
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols);
 int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
                     void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream);

@@ -51,6 +51,7 @@ class Stats(ctypes.Structure):
         ("grid", ctypes.c_int32),
         ("seg_log2", ctypes.c_int32),
         ("arith", ctypes.c_int32),
+        ("err_est", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:

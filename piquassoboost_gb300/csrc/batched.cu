@@ -68,7 +68,9 @@ struct BArgs {
     int ninst;
     unsigned int* counter;
     cdd* item_part;
+    double* item_s2;        // per item: sum of |term 2^40|^2 of its double-float terms
     double* out;            // 2 doubles per instance (device)
+    double* inst_est;       // per instance: relative error estimate (-1: FP64 product)
     int df;
 };
 
@@ -183,11 +185,13 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
             }
         }
         cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+        double s2 = 0.0;  // double-float items: sum of |term 2^40|^2 (error estimate)
         const bool use_df = DF && io.ok;
         if (use_df) {
             const DfConv cv = make_dfconv(io.boost);
             unsigned int sbit = (unsigned int)(__popcll(g0) & 1) << 31;
             float brh = 0.f, brl = 0.f, bih = 0.f, bil = 0.f;
+            float s2f = 0.f;  // sum of |term 2^40|^2 since the last fold
             for (unsigned long long k = 0; k < L; ++k) {
                 if (k != 0) {
                     const int b = __ffsll((long long)k) - 1;
@@ -212,6 +216,8 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
                         acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
                         acc.im = dd_add(acc.im, dd{(double)bih, (double)bil});
                         brh = brl = bih = bil = 0.f;
+                        s2 += (double)s2f;
+                        s2f = 0.f;
                     }
                 }
                 cf pa{1.f, 0.f, 0.f, 0.f}, pb{1.f, 0.f, 0.f, 0.f};
@@ -235,10 +241,13 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
                            __uint_as_float(__float_as_uint(pa.rl) ^ sbit));
                     df_acc(bih, bil, __uint_as_float(__float_as_uint(pa.ih) ^ sbit),
                            __uint_as_float(__float_as_uint(pa.il) ^ sbit));
+                    const float ur = pa.rh * 0x1p40f, ui = pa.ih * 0x1p40f;
+                    s2f = fmaf(ur, ur, fmaf(ui, ui, s2f));
                 }
             }
             acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
             acc.im = dd_add(acc.im, dd{(double)bih, (double)bil});
+            s2 += (double)s2f;
         } else if (GROUP == 1) {
             // FP64 product (also the double-float fallback)
             unsigned long long neg = (unsigned long long)(__popcll(g0) & 1) << 63;
@@ -339,7 +348,11 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
             acc.im = dd_add_d(acc.im, bim);
         }
         acc = warp_sum_cdd(acc);
-        if (lane == 0) p.item_part[it] = acc;
+        s2 = warp_sum_d(s2);
+        if (lane == 0) {
+            p.item_part[it] = acc;
+            p.item_s2[it] = s2;
+        }
     }
 }
 
@@ -355,13 +368,26 @@ __global__ void batched_finalize_kernel(BArgs p) {
             if (lane == 0) {
                 p.out[2 * i] = nan("");
                 p.out[2 * i + 1] = nan("");
+                p.inst_est[i] = -1.0;
             }
             continue;
         }
         cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (int k = lane; k < in.nitems; k += 32) tot = cdd_add(tot, p.item_part[in.item0 + k]);
+        double q = 0.0;
+        for (int k = lane; k < in.nitems; k += 32) {
+            tot = cdd_add(tot, p.item_part[in.item0 + k]);
+            q += p.item_s2[in.item0 + k];
+        }
         tot = warp_sum_cdd(tot);
-        if (lane == 0) write_result(tot, io.exp, p.out + 2 * i, nullptr);
+        q = warp_sum_d(q);
+        if (lane == 0) {
+            write_result(tot, io.exp, p.out + 2 * i, nullptr);
+            // relative rounding-error estimate of a double-float result, as
+            // in the single-permanent kernels (-1: the FP64 product ran)
+            p.inst_est[i] = (p.df && io.ok)
+                                ? sqrt((double)in.cols) * 0x1p-46 * sqrt(q) * 0x1p-40 / hypot(tot.re.hi, tot.im.hi)
+                                : -1.0;
+        }
     }
 }
 
@@ -479,12 +505,15 @@ struct BatchPlan {
     BItem* ditems = nullptr;
     unsigned int* dcounter = nullptr;
     cdd* dpart = nullptr;
+    double* ds2 = nullptr;           // per item |term|^2 sums
     double* dout = nullptr;
+    double* dest = nullptr;          // per instance error estimates
     int* ddev_index = nullptr;       // dev_index on the device (slot -> device instance)
     double* dtrivial = nullptr;      // trivial values on the device
     // pinned host staging and the captured graph
     double* hin = nullptr;
     double* hout = nullptr;
+    double* hest = nullptr;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -497,6 +526,7 @@ static void plan_free(BatchPlan* p) {
     if (p->item_buf) cudaFree(p->item_buf);
     if (p->hin) cudaFreeHost(p->hin);
     if (p->hout) cudaFreeHost(p->hout);
+    if (p->hest) cudaFreeHost(p->hest);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -515,7 +545,9 @@ static BArgs plan_args(BatchPlan* p) {
     a.ninst = p->ninst;
     a.counter = p->dcounter;
     a.item_part = p->dpart;
+    a.item_s2 = p->ds2;
     a.out = p->dout;
+    a.inst_est = p->dest;
     a.df = p->df ? 1 : 0;
     return a;
 }
@@ -583,11 +615,14 @@ static int plan_build_items(BatchPlan* p) {
         p->item_buf = nullptr;
         p->item_cap = 0;
         size_t want = items.size() + items.size() / 4 + 64;
-        cudaError_t ea = cudaMalloc(&p->item_buf, align_up(want * sizeof(BItem), 256) + want * sizeof(cdd));
+        cudaError_t ea = cudaMalloc(&p->item_buf, align_up(want * sizeof(BItem), 256) +
+                                                      align_up(want * sizeof(cdd), 256) + want * sizeof(double));
         if (ea != cudaSuccess) return cuda_fail(ea, "batched: work list allocation");
         p->item_cap = want;
         p->ditems = reinterpret_cast<BItem*>(p->item_buf);
         p->dpart = reinterpret_cast<cdd*>(p->item_buf + align_up(want * sizeof(BItem), 256));
+        p->ds2 = reinterpret_cast<double*>(p->item_buf + align_up(want * sizeof(BItem), 256) +
+                                           align_up(want * sizeof(cdd), 256));
     }
     cudaError_t e = cudaMemcpy(p->dinst, inst.data(), inst.size() * sizeof(BInst), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !items.empty())
@@ -611,6 +646,8 @@ static int plan_capture(BatchPlan* p) {
                          ? cudaMemcpyAsync(p->hout, p->dout, (size_t)p->ninst * 2 * sizeof(double),
                                            cudaMemcpyDeviceToHost, p->stream)
                          : e2;
+    if (e3 == cudaSuccess && p->df)
+        e3 = cudaMemcpyAsync(p->hest, p->dest, (size_t)p->ninst * sizeof(double), cudaMemcpyDeviceToHost, p->stream);
     e = cudaStreamEndCapture(p->stream, &g);
     if (e3 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -712,12 +749,14 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
     size_t oO = take((size_t)std::max(1, p->ninst) * sizeof(BInstOut));
     size_t oC = take(sizeof(unsigned int));
     size_t oR = take((size_t)std::max(1, p->ninst) * 2 * sizeof(double));
+    size_t oE = take((size_t)std::max(1, p->ninst) * sizeof(double));
     size_t oX = take((size_t)std::max<int64_t>(1, p->count) * sizeof(int));
     size_t oT = take((size_t)std::max<int64_t>(1, p->count) * sizeof(double));
     p->dbytes = off;
     e = cudaMalloc(&p->dbuf, p->dbytes);
     if (e == cudaSuccess) e = cudaMallocHost(&p->hin, std::max<size_t>(1, (size_t)p->total_elems) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMallocHost(&p->hout, (size_t)std::max(1, p->ninst) * 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&p->hest, (size_t)std::max(1, p->ninst) * sizeof(double));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
@@ -743,6 +782,7 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
         }
     }
     p->dout = reinterpret_cast<double*>(p->dbuf + oR);
+    p->dest = reinterpret_cast<double*>(p->dbuf + oE);
     int rc = plan_build_items(p);
     if (rc == GBPERM_OK) rc = plan_capture(p);
     if (rc) {
@@ -783,6 +823,8 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         e = cudaStreamSynchronize(p->stream);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run: kernels");
     }
+    int escalated = 0;
+    double worst = 0.0;  // largest estimate among the double-float results kept
     for (int64_t i = 0; i < p->count; ++i) {
         int d = p->dev_index[i];
         if (d < 0) {
@@ -791,6 +833,17 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         } else {
             out[2 * i] = p->hout[2 * d];
             out[2 * i + 1] = p->hout[2 * d + 1];
+            // a double-float result whose error estimate is above the bar
+            // is recomputed with the FP64 product (rare: one in thousands
+            // of the uneven k = 8..28 batches)
+            if (p->df && p->hest[d] >= 0.0 && !(p->hest[d] <= kDfEscalate) && g_opt.df_escalate.load() != 0) {
+                int rc = gbperm_perm(packed + 2 * p->off[i], p->rows[i], p->cols[i], p->cols[i], GBPERM_ARITH_FP64,
+                                     out + 2 * i, nullptr, nullptr);
+                if (rc) return rc;
+                ++escalated;
+            } else if (p->df && p->hest[d] >= 0.0) {
+                worst = std::max(worst, p->hest[d]);
+            }
         }
     }
     if (stats && p->ninst > 0) {
@@ -799,7 +852,8 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         stats->kernel_ms = ms;
         stats->steps = p->steps;
         stats->flops = p->flops;
-        stats->launches = 3;
+        stats->launches = 3 + 2 * escalated;  // + prepare and FP64 kernel per recomputed instance
+        stats->err_est = worst;
         stats->grid = p->grid;
         stats->seg_log2 = (int)p->item_target_log2;
         stats->arith = p->df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;

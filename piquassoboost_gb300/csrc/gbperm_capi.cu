@@ -187,7 +187,7 @@ size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w) {
 }
 
 int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, size_t ws_bytes,
-                  double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan) {
+                  double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan, double* d_err) {
     PlainWs w;
     size_t need = plain_ws_layout(rows, cols, plan.max_grid(), &w);
     if (ws_bytes < need) return fail(GBPERM_ERR_ARG, "gbperm: workspace too small");
@@ -206,16 +206,23 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
     pa.df = plan.df ? 1 : 0;
     pa.df_info = reinterpret_cast<int*>(base + w.scale);
+    // the Gray sum is multilinear in the rows only for square matrices
+    // (for rows != cols it is a different polynomial of the entries)
+    pa.row_balance = rows == cols ? 1 : 0;
+    pa.exp_fp64_out = pa.exp_out + 1;
     cudaError_t e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
     if (plan.df) {
         // the double-float kernel returns at once if the device range check
         // failed; its FP64 twin below returns at once if it passed
+        double* err = d_err ? d_err : reinterpret_cast<double*>(base + w.scale + 8);
+        e = cudaMemsetAsync(err, 0, sizeof(double), st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain df error slot");
         e = launch_plain_df(pa.a1, pa.a2, pa.exp_out, pa.df_info, rows, cols, plan.cpl, plan.grp, plan.grid_df,
-                            plan.seg_log2_df, base + w.kern, d_out2, d_out4, st);
+                            plan.seg_log2_df, base + w.kern, d_out2, d_out4, err, g_opt.df_escalate.load() != 0, st);
         if (e != cudaSuccess) return cuda_fail(e, "plain df launch");
     }
-    e = launch_plain(pa.a1, pa.a2, pa.exp_out, plan.df ? pa.df_info : nullptr, rows, cols, plan.grid,
+    e = launch_plain(pa.a1, pa.a2, pa.exp_fp64_out, plan.df ? pa.df_info : nullptr, rows, cols, plan.grid,
                      plan.seg_log2, base + w.kern, d_out2, d_out4, st);
     if (e != cudaSuccess) return cuda_fail(e, "plain launch");
     return GBPERM_OK;
@@ -326,7 +333,7 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
     bool df = false;
     int boost = 0;
     if (arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols)
-        df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost);
+        df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost, rows == cols);
     PlainPlan plan = plan_plain((int)rows, (int)cols, df);
     size_t mat_bytes = align_up((size_t)rows * cols * sizeof(double2), 256);
     size_t ws = plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
@@ -341,11 +348,11 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
                                       cols * sizeof(double2), rows, cudaMemcpyHostToDevice, c.stream);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm: upload");
     if (stats) cudaEventRecord(c.ev0, c.stream);
-    rc = run_plain_dev(dA, cols, (int)rows, (int)cols, dws, ws, dout, dout + 2, c.stream, plan);
+    rc = run_plain_dev(dA, cols, (int)rows, (int)cols, dws, ws, dout, dout + 2, c.stream, plan, dout + 6);
     if (rc) return rc;
     if (stats) cudaEventRecord(c.ev1, c.stream);
-    double h[6];
-    e = cudaMemcpyAsync(h, dout, sizeof(h), cudaMemcpyDeviceToHost, c.stream);
+    double h[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    e = cudaMemcpyAsync(h, dout, (df ? 7 : 6) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm: download");
     e = cudaStreamSynchronize(c.stream);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm: kernel");
@@ -361,7 +368,12 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         stats->launches = df ? 3 : 2;
         stats->grid = df ? plan.grid_df : plan.grid;
         stats->seg_log2 = df ? plan.seg_log2_df : plan.seg_log2;
-        stats->arith = df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        // h[6]: the double-float estimate, -1 when the range check sent the
+        // matrix to the FP64 kernel; above the bar the FP64 twin recomputed
+        const bool ran_df = df && h[6] >= 0.0;
+        const bool used_df = ran_df && (h[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
+        stats->arith = used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->err_est = ran_df ? h[6] : 0.0;
     }
     return GBPERM_OK;
 }

@@ -21,6 +21,7 @@ struct Options {
     std::atomic<int64_t> batched_threads{0};
     std::atomic<int64_t> plain_df_group{0};
     std::atomic<int64_t> batched_item_log2{0};
+    std::atomic<int64_t> df_escalate{1};
     std::atomic<int64_t>* find(const char* key) {
         if (!std::strcmp(key, "plain.seg_log2")) return &plain_seg_log2;
         if (!std::strcmp(key, "plain.grid")) return &plain_grid;
@@ -28,6 +29,7 @@ struct Options {
         if (!std::strcmp(key, "batched.threads")) return &batched_threads;
         if (!std::strcmp(key, "plain.df_group")) return &plain_df_group;
         if (!std::strcmp(key, "batched.item_log2")) return &batched_item_log2;
+        if (!std::strcmp(key, "df.escalate")) return &df_escalate;
         return nullptr;
     }
 };
@@ -63,8 +65,11 @@ struct PlainWs {
 };
 PlainPlan plan_plain(int rows, int cols, bool df);
 size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w);
+// d_err: optional device double that receives the double-float product's
+// relative rounding-error estimate (0 when the FP64 product runs)
 int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, size_t ws_bytes,
-                  double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan);
+                  double* d_out2, double* d_out4, cudaStream_t st, const PlainPlan& plan,
+                  double* d_err = nullptr);
 bool plain_trivial(int64_t rows, int64_t cols, double* out, double* out_dd);
 
 // Repeated-multiplicity plan built on the host (host_repeated.cu).

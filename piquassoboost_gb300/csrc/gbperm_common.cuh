@@ -67,6 +67,13 @@ __device__ __forceinline__ cdd warp_sum_cdd(cdd v) {
     return v;
 }
 
+// Warp-wide double sum (every lane ends with the total).
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    return v;
+}
+
 // Exact int64 fixed point (unit 2^-62) -> double, round-to-nearest-up on the
 // dropped bits, using integer instructions only.  x == 0 maps to +0.0.
 __device__ __forceinline__ double fix_to_double(long long x) {

@@ -44,6 +44,17 @@ struct PrepArgs {
     // col_e_out + b*cols, df_info + 2b
     int count = 1;
     long long a_stride = 0;
+    // 1: scale row i by 2^-k_i first (k_i: binary exponent of its largest
+    // component) and add sum_i w_i k_i to exp_out.  Exact, and it removes
+    // the cancellation that unequal row norms cause in the Gray sum.  Valid
+    // when the sum is multilinear in the (expanded) rows: square plain
+    // matrices, the repeated and leave-one-out sums; off for rectangular
+    // matrices and for the gradient, whose entries would need a per-row
+    // correction
+    int row_balance = 0;
+    // optional: the exponent without the double-float boost, for the FP64
+    // twin when it takes over from a double-float kernel that ran
+    int* exp_fp64_out = nullptr;
 };
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st);
 
@@ -60,7 +71,18 @@ struct PlainArgs {
     const int* df_info;    // {boost, ok} from the prepare kernel, or null (FP64 only)
     double* out2;          // complex128 result
     double* out4;          // optional: {re_hi, im_hi, re_lo, im_lo} of the scaled result
+    // double-float kernel only: per-block sums of |term|^2 (terms scaled by
+    // 2^40) and the relative rounding-error estimate of the result
+    double* block_s2 = nullptr;
+    double* err_out = nullptr;
+    int* df_ok = nullptr;  // writable df_info[1]: cleared to hand the result to the FP64 twin
 };
+
+// A double-float result whose estimated relative rounding error exceeds this
+// (the 1e-10 accuracy bar) is recomputed by the FP64 twin kernel.  The
+// estimate sat above the measured error in every case checked (2-8x
+// typically; Haar, rescaled, Gaussian and positive matrices, n = 16-36).
+constexpr double kDfEscalate = 1e-10;
 
 int plain_bucket(int cols);
 int plain_blocks_per_sm(int rows, int cols);
@@ -68,7 +90,7 @@ void df_shape(int cols, int group, int* cpl, int* grp);
 int plain_df_blocks_per_sm(int rows, int cpl, int grp);
 cudaError_t launch_plain_df(const longlong2* a1, const longlong2* a2, const int* exp_in, const int* df_info,
                             int rows, int cols, int cpl, int grp, int grid, int seg_log2, void* ws,
-                            double* out2, double* out4, cudaStream_t st);
+                            double* out2, double* out4, double* err_out, bool escalate, cudaStream_t st);
 size_t plain_workspace_bytes(int grid);
 cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* exp_in,
                          const int* df_info, int rows, int cols, int grid, int seg_log2, void* ws,
@@ -79,8 +101,9 @@ cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* ex
 // (prod of column 2-norms) near 2^-40 while keeping the largest possible
 // term (every |colsum| at its bound, times sqrt 2) below 2^118.  Returns
 // false when no o satisfies both (then the FP64 kernel must be used).
+// row_balance: the rows are scaled first as PrepArgs::row_balance does.
 bool df_boost(const double* A, int64_t rows, int64_t cols, int64_t ld, const int* row_w,
-              const int* col_w, int* boost);
+              const int* col_w, int* boost, bool row_balance = true);
 constexpr int kDfMaxCols = 48;
 
 // --------------------------------------------------------------- repeated
@@ -106,11 +129,15 @@ struct RepArgs {
     const int* df_info;       // {boost, ok} or null (FP64 only)
     double* out2;
     double* out4;
+    // double-float kernel only (as in PlainArgs)
+    double* block_s2 = nullptr;
+    double* err_out = nullptr;
+    int* df_ok = nullptr;
 };
 int repeated_blocks_per_sm(const RepArgs& a);
 void repeated_df_shape(int cols, int* cpl, int* grp);
 int repeated_df_blocks_per_sm(const RepArgs& a, int cpl, int grp);
-cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, cudaStream_t st);
+cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, bool escalate, cudaStream_t st);
 size_t repeated_workspace_bytes(int grid);
 cudaError_t launch_repeated(RepArgs a, int grid, void* ws, cudaStream_t st);
 
@@ -126,6 +153,78 @@ __device__ __forceinline__ void write_result(cdd v, int e, double* out2, double*
         out4[1] = ih;
         out4[2] = rl;
         out4[3] = il;
+    }
+}
+
+// End of a double-float Gray sweep, shared by the plain and repeated
+// double-float kernels.  Every block publishes its threads' double-double
+// sum and sum of |term 2^40|^2; the last block to arrive sums all blocks'
+// with every thread (strided, then a fixed butterfly and the warp order, so
+// the result is reproducible), writes the sum scaled by 2^exp_in and the
+// estimate
+//     sqrt(nfac) 2^-46 sqrt(sum |term|^2) / |sum|
+// of its relative rounding error (each term carries ~2^-46 sqrt(nfac)
+// relative error, independent between terms), and when that is above
+// kDfEscalate (or not finite) clears *df_ok so that the FP64 twin launched
+// next on the stream recomputes and overwrites the result.
+template <int THREADS>
+__device__ __forceinline__ void df_grid_finish(cdd acc, double s2, cdd* block_part, double* block_s2,
+                                               unsigned int* done, const int* exp_in, double* out2, double* out4,
+                                               double* err_out, int* df_ok, double nfac) {
+    __shared__ cdd s_warp[THREADS / 32];
+    __shared__ double s_wq[THREADS / 32];
+    __shared__ bool s_last;
+    acc = warp_sum_cdd(acc);
+    s2 = warp_sum_d(s2);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_warp[warp] = acc;
+        s_wq[warp] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd b = s_warp[0];
+        double q = s_wq[0];
+        for (int w = 1; w < THREADS / 32; ++w) {
+            b = cdd_add(b, s_warp[w]);
+            q += s_wq[w];
+        }
+        block_part[blockIdx.x] = b;
+        block_s2[blockIdx.x] = q;
+        __threadfence();
+        unsigned int t = atomicAdd(done, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;  // block-uniform
+    __threadfence();
+    cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+    double tq = 0.0;
+    for (unsigned int bk = threadIdx.x; bk < gridDim.x; bk += blockDim.x) {
+        const volatile double* qv = reinterpret_cast<const volatile double*>(&block_part[bk]);
+        cdd v{{qv[0], qv[1]}, {qv[2], qv[3]}};
+        tot = cdd_add(tot, v);
+        tq += *reinterpret_cast<const volatile double*>(&block_s2[bk]);
+    }
+    tot = warp_sum_cdd(tot);
+    tq = warp_sum_d(tq);
+    if (lane == 0) {
+        s_warp[warp] = tot;
+        s_wq[warp] = tq;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd all = s_warp[0];
+        double q2 = s_wq[0];
+        for (int w = 1; w < THREADS / 32; ++w) {
+            all = cdd_add(all, s_warp[w]);
+            q2 += s_wq[w];
+        }
+        write_result(all, *exp_in, out2, out4);
+        const double est = sqrt(nfac) * 0x1p-46 * sqrt(q2) * 0x1p-40 / hypot(all.re.hi, all.im.hi);
+        if (err_out) *err_out = est;
+        if (df_ok && !(est <= kDfEscalate)) *df_ok = 0;
+        *done = 0u;
     }
 }
 

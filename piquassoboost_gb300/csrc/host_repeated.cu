@@ -362,6 +362,8 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
     pa.exp_out = reinterpret_cast<int*>(base + w.exp);
     pa.df = df ? 1 : 0;
     pa.df_info = df ? reinterpret_cast<int*>(base + w.exp + 16) : nullptr;
+    pa.row_balance = 1;
+    pa.exp_fp64_out = pa.exp_out + 1;
     if (stats) cudaEventRecord(c.ev0, st);
     e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: prepare");
@@ -379,14 +381,21 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
     a.out2 = dout;
     a.out4 = dout + 2;
     if (df) {
-        e = launch_repeated_df(a, dcpl, dgrp, grid_df, base + w.kern, st);
+        // dout[6]: the double-float estimate (-1 when the range check fails)
+        a.err_out = dout + 6;
+        e = cudaMemsetAsync(a.err_out, 0, sizeof(double), st);
+        if (e == cudaSuccess)
+            e = launch_repeated_df(a, dcpl, dgrp, grid_df, base + w.kern, g_opt.df_escalate.load() != 0, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: df launch");
     }
+    // the FP64 twin scales by the exponent without the double-float boost
+    a.exp_in = pa.exp_fp64_out;
+    a.err_out = nullptr;
     e = launch_repeated(a, grid, base + w.kern, st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: launch");
     if (stats) cudaEventRecord(c.ev1, st);
-    double hres[6];
-    e = cudaMemcpyAsync(hres, dout, sizeof(hres), cudaMemcpyDeviceToHost, st);
+    double hres[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    e = cudaMemcpyAsync(hres, dout, (df ? 7 : 6) * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: kernel");
     out[0] = hres[0];
@@ -401,7 +410,10 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         stats->launches = df ? 3 : 2;
         stats->grid = df ? grid_df : grid;
         stats->seg_log2 = h.q;
-        stats->arith = df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        const bool ran_df = df && hres[6] >= 0.0;
+        const bool used_df = ran_df && (hres[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
+        stats->arith = used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->err_est = ran_df ? hres[6] : 0.0;
     }
     return GBPERM_OK;
 }

@@ -700,7 +700,7 @@ static int perm_grad_host(const double* A, int64_t n, int64_t count, int64_t ld,
         const double* Ab = A + 2 * b * stride;
         if (!all_finite(Ab, n, n, ld)) continue;  // NaN out, below
         int boost = 0;
-        if (!df_boost(Ab, n, n, ld, nullptr, nullptr, &boost))
+        if (!df_boost(Ab, n, n, ld, nullptr, nullptr, &boost, false))
             return fail(GBPERM_ERR_TOO_LARGE,
                         std::string(who) + ": matrix dynamic range beyond the double-float product");
     }

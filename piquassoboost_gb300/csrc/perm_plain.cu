@@ -212,8 +212,8 @@ int plain_blocks_per_sm(int rows, int cols) {
 }
 
 size_t plain_workspace_bytes(int grid) {
-    // block partials + completion counter
-    return align_up((size_t)grid * sizeof(cdd), 256) + 256;
+    // block partials + completion counter + per-block |term|^2 sums
+    return align_up((size_t)grid * sizeof(cdd), 256) + 256 + align_up((size_t)grid * sizeof(double), 256);
 }
 
 // Launch the plain kernel on device data that is already in fixed point

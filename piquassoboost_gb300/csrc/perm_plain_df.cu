@@ -30,13 +30,22 @@ __device__ __forceinline__ cf shfl_xor_cf(const cf& v, int m) {
 }
 
 template <int CPL, int GROUP>
-__global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
+// up to 18 columns per lane the kernel fits 128 registers (4 blocks per SM),
+// above that 168 (3 blocks); the allocator is held to those, which it
+// otherwise gives up for a few more live values
+#ifndef GBPERM_PLAIN_DF_MINB
+#define GBPERM_PLAIN_DF_MINB (CPL <= 18 ? 4 : 3)
+#endif
+__global__ void __launch_bounds__(kThreads, GBPERM_PLAIN_DF_MINB) plain_df_kernel(PlainArgs p) {
     constexpr int NP = CPL * GROUP;  // padded columns
     extern __shared__ __align__(16) unsigned char smem_raw[];
     longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);
     longlong2* s_a2 = s_a1 + p.rows * NP;
     const int rows = p.rows, cols = p.cols;
-    if (p.df_info[1] == 0) return;  // range check failed: the FP64 kernel runs instead
+    if (p.df_info[1] == 0) {  // range check failed: the FP64 kernel runs instead
+        if (blockIdx.x == 0 && threadIdx.x == 0 && p.err_out) *p.err_out = -1.0;
+        return;
+    }
     for (int e = threadIdx.x; e < rows * NP; e += blockDim.x) {
         int r = e / NP, j = e % NP;
         longlong2 z = make_longlong2(0, 0);
@@ -50,6 +59,11 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
     const int j0 = g * CPL;
     const bool leader = (g == 0);
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    // sum of |term 2^40|^2 (rounding-error estimate), per thread in shared
+    // memory: a register pair more would cost the 18-column shape a block
+    // per SM
+    __shared__ double s_s2t[kThreads];
+    s_s2t[threadIdx.x] = 0.0;
     const unsigned long long L = 1ull << p.seg_log2;
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
     long long cre[CPL], cim[CPL];
@@ -82,6 +96,7 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
         }
         unsigned int sbit = (unsigned int)(__popcll(g0) & 1) << 31;
         float brh = 0.f, brl = 0.f, bih = 0.f, bil = 0.f;
+        float s2f = 0.f;  // sum of |term 2^40|^2 since the last fold
         for (unsigned long long k = 0; k < L; ++k) {
             if (k != 0) {
                 const int b = __ffsll((long long)k) - 1;  // warp-uniform
@@ -121,6 +136,8 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
                     acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
                     acc.im = dd_add(acc.im, dd{(double)bih, (double)bil});
                     brh = brl = bih = bil = 0.f;
+                    s_s2t[threadIdx.x] += (double)s2f;
+                    s2f = 0.f;
                 }
             }
             // partial product of this lane's columns in kChains independent
@@ -151,49 +168,20 @@ __global__ void __launch_bounds__(kThreads) plain_df_kernel(PlainArgs p) {
                        __uint_as_float(__float_as_uint(pa.rl) ^ sbit));
                 df_acc(bih, bil, __uint_as_float(__float_as_uint(pa.ih) ^ sbit),
                        __uint_as_float(__float_as_uint(pa.il) ^ sbit));
+                // terms sit near 2^-40 (the range boost centres them there)
+#ifndef GBPERM_NO_S2
+                const float ur = pa.rh * 0x1p40f, ui = pa.ih * 0x1p40f;
+                s2f = fmaf(ur, ur, fmaf(ui, ui, s2f));
+#endif
             }
         }
         acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
         acc.im = dd_add(acc.im, dd{(double)bih, (double)bil});
+        s_s2t[threadIdx.x] += (double)s2f;
     }
 
-    __shared__ cdd s_warp[kThreads / 32];
-    __shared__ bool s_last;
-    acc = warp_sum_cdd(acc);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) s_warp[warp] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        cdd bsum = s_warp[0];
-        for (int w = 1; w < kThreads / 32; ++w) bsum = cdd_add(bsum, s_warp[w]);
-        p.block_part[blockIdx.x] = bsum;
-        __threadfence();
-        unsigned int t = atomicAdd(p.done, 1u);
-        s_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (s_last) {
-        // the last block sums the block partials: thread t takes partials
-        // t, t + blockDim, ... in order, then a fixed butterfly and the warp
-        // order -- deterministic, and not one thread's serial chain of L2
-        // loads and dependent double-double adds
-        __threadfence();
-        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (unsigned int bk = threadIdx.x; bk < gridDim.x; bk += blockDim.x) {
-            const volatile double* q = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
-            cdd v{{q[0], q[1]}, {q[2], q[3]}};
-            tot = cdd_add(tot, v);
-        }
-        tot = warp_sum_cdd(tot);
-        if (lane == 0) s_warp[warp] = tot;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            cdd all = s_warp[0];
-            for (int w = 1; w < kThreads / 32; ++w) all = cdd_add(all, s_warp[w]);
-            write_result(all, *p.exp_in, p.out2, p.out4);
-            *p.done = 0u;
-        }
-    }
+    df_grid_finish<kThreads>(acc, s_s2t[threadIdx.x], p.block_part, p.block_s2, p.done, p.exp_in, p.out2, p.out4, p.err_out,
+                             p.df_ok, (double)cols);
 }
 
 template <int CPL, int GROUP>
@@ -262,7 +250,7 @@ int plain_df_blocks_per_sm(int rows, int cpl, int grp) {
 
 cudaError_t launch_plain_df(const longlong2* a1, const longlong2* a2, const int* exp_in, const int* df_info,
                             int rows, int cols, int cpl, int grp, int grid, int seg_log2, void* ws,
-                            double* out2, double* out4, cudaStream_t st) {
+                            double* out2, double* out4, double* err_out, bool escalate, cudaStream_t st) {
     PlainArgs a;
     a.a1 = a1;
     a.a2 = a2;
@@ -277,6 +265,9 @@ cudaError_t launch_plain_df(const longlong2* a1, const longlong2* a2, const int*
     a.df_info = df_info;
     a.out2 = out2;
     a.out4 = out4;
+    a.block_s2 = reinterpret_cast<double*>(w + align_up((size_t)grid * sizeof(cdd), 256) + 256);
+    a.err_out = err_out;
+    a.df_ok = escalate ? const_cast<int*>(df_info) + 1 : nullptr;
     cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
 #define X(C, G) \

@@ -291,7 +291,10 @@ int repeated_blocks_per_sm(const RepArgs& a) {
     }
 }
 
-size_t repeated_workspace_bytes(int grid) { return align_up((size_t)grid * sizeof(cdd), 256) + 256; }
+size_t repeated_workspace_bytes(int grid) {
+    // block partials + completion counter + per-block |term|^2 sums (double-float kernel)
+    return align_up((size_t)grid * sizeof(cdd), 256) + 256 + align_up((size_t)grid * sizeof(double), 256);
+}
 
 cudaError_t launch_repeated(RepArgs a, int grid, void* ws, cudaStream_t st) {
     char* w = static_cast<char*>(ws);

@@ -51,7 +51,10 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
     __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
     __shared__ long long s_stride[kMaxDigits];
     const int R = p.R, C = p.C, nd = p.nd, q = p.q;
-    if (p.df_info[1] == 0) return;  // range check failed: the FP64 kernel runs instead
+    if (p.df_info[1] == 0) {  // range check failed: the FP64 kernel runs instead
+        if (blockIdx.x == 0 && threadIdx.x == 0 && p.err_out) *p.err_out = -1.0;
+        return;
+    }
     for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
         int r = e / NP, j = e % NP;
         s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
@@ -85,6 +88,7 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
     const int j0 = g * CPL;
     const bool leader = (g == 0);
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    double s2 = 0.0;  // sum of |term 2^40|^2 (rounding-error estimate)
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
     const unsigned long long lane_seg = (threadIdx.x & 31) / GROUP;
     constexpr unsigned long long S = 32 / GROUP;  // segments per warp
@@ -146,6 +150,7 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
         }
         unsigned int sbit = (unsigned int)(gsum & 1) << 31;
         float brh = 0.f, brl = 0.f, bih = 0.f, bil = 0.f;
+        float s2f = 0.f;  // sum of |term 2^40|^2 (low-digit weight in, high-digit weight out)
         for (unsigned long long k = 0; k < p.P; ++k) {
             if (k != 0) {
                 const int d = s_seq[k];  // warp-uniform
@@ -178,6 +183,8 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
                     acc.re = dd_add(acc.re, dd{(double)brh * whigh, (double)brl * whigh});
                     acc.im = dd_add(acc.im, dd{(double)bih * whigh, (double)bil * whigh});
                     brh = brl = bih = bil = 0.f;
+                    s2 += (double)s2f * whigh * whigh;
+                    s2f = 0.f;
                 }
             }
             // a lane's columns are contiguous, so padding (power 0) only ever
@@ -204,49 +211,17 @@ __global__ void __launch_bounds__(kThreads) repeated_df_kernel(RepArgs p) {
                        __uint_as_float(__float_as_uint(t.rl) ^ sbit));
                 df_acc(bih, bil, __uint_as_float(__float_as_uint(t.ih) ^ sbit),
                        __uint_as_float(__float_as_uint(t.il) ^ sbit));
+                const float ur = t.rh * 0x1p40f, ui = t.ih * 0x1p40f;
+                s2f = fmaf(ur, ur, fmaf(ui, ui, s2f));
             }
         }
         acc.re = dd_add(acc.re, dd{(double)brh * whigh, (double)brl * whigh});
         acc.im = dd_add(acc.im, dd{(double)bih * whigh, (double)bil * whigh});
+        s2 += (double)s2f * whigh * whigh;
     }
 
-    __shared__ cdd s_warp[kThreads / 32];
-    __shared__ bool s_last;
-    acc = warp_sum_cdd(acc);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) s_warp[warp] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        cdd b = s_warp[0];
-        for (int w = 1; w < kThreads / 32; ++w) b = cdd_add(b, s_warp[w]);
-        p.block_part[blockIdx.x] = b;
-        __threadfence();
-        unsigned int t = atomicAdd(p.done, 1u);
-        s_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (s_last) {
-        // the last block sums the block partials: thread t takes partials
-        // t, t + blockDim, ... in order, then a fixed butterfly and the warp
-        // order -- deterministic, and not one thread's serial chain of L2
-        // loads and dependent double-double adds
-        __threadfence();
-        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (unsigned int bk = threadIdx.x; bk < gridDim.x; bk += blockDim.x) {
-            const volatile double* qv = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
-            cdd v{{qv[0], qv[1]}, {qv[2], qv[3]}};
-            tot = cdd_add(tot, v);
-        }
-        tot = warp_sum_cdd(tot);
-        if (lane == 0) s_warp[warp] = tot;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            cdd all = s_warp[0];
-            for (int w = 1; w < kThreads / 32; ++w) all = cdd_add(all, s_warp[w]);
-            write_result(all, *p.exp_in, p.out2, p.out4);
-            *p.done = 0u;
-        }
-    }
+    df_grid_finish<kThreads>(acc, s2, p.block_part, p.block_s2, p.done, p.exp_in, p.out2, p.out4, p.err_out,
+                             p.df_ok, (double)C);
 }
 
 template <int CPL, int GROUP>
@@ -296,10 +271,12 @@ int repeated_df_blocks_per_sm(const RepArgs& a, int cpl, int grp) {
     return 1;
 }
 
-cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, cudaStream_t st) {
+cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, bool escalate, cudaStream_t st) {
     char* w = static_cast<char*>(ws);
     a.block_part = reinterpret_cast<cdd*>(w);
     a.done = reinterpret_cast<unsigned int*>(w + align_up((size_t)grid * sizeof(cdd), 256));
+    a.block_s2 = reinterpret_cast<double*>(w + align_up((size_t)grid * sizeof(cdd), 256) + 256);
+    a.df_ok = escalate ? const_cast<int*>(a.df_info) + 1 : nullptr;
     cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
 #define X(C, G) \

@@ -327,12 +327,13 @@ __device__ __forceinline__ void df_renorm2(float& h, float& l) {
 }
 
 template <int CPL>
-__global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_part) {
+__global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_part, double* col_s2) {
     constexpr int G = 4;
     constexpr int NP = CPL * G;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cdd* s_acc = reinterpret_cast<cdd*>(smem_raw);                           // CPL x kThreads
-    longlong2* s_a1 = reinterpret_cast<longlong2*>(s_acc + CPL * kThreads);  // R x NP (interleaved)
+    double* s_s2 = reinterpret_cast<double*>(s_acc + CPL * kThreads);        // CPL x kThreads: sum |LO|^2
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(s_s2 + CPL * kThreads);   // R x NP (interleaved)
     longlong2* s_a2 = s_a1 + p.R * NP;                                       // nd x NP (interleaved)
     float2* s_w = reinterpret_cast<float2*>(s_a2 + p.nd * NP);               // P: weights as float pairs
     unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);      // P
@@ -359,6 +360,7 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
     for (int e = threadIdx.x; e < nd; e += blockDim.x) s_D[e] = p.D[e];
     for (int e = threadIdx.x; e < R; e += blockDim.x) s_r[e] = p.rcoef[e];
     for (int e = threadIdx.x; e < CPL * kThreads; e += blockDim.x) s_acc[e] = cdd{{0.0, 0.0}, {0.0, 0.0}};
+    for (int e = threadIdx.x; e < CPL * kThreads; e += blockDim.x) s_s2[e] = 0.0;
     if (threadIdx.x == 0) {
         long long st = 1;
         for (int i = 0; i < q; ++i) {
@@ -382,6 +384,8 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
     const unsigned long long full = p.nseg / (2 * S) * (2 * S);
     long long cre[CPL], cim[CPL];
     cf Q[CPL];
+    float s2f[CPL];  // sum of |LO_c|^2 since the last fold (rounding-error estimate)
+    double* my_s2 = s_s2 + threadIdx.x;
 
     for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / G;
          hw < p.nseg; hw += T) {
@@ -410,6 +414,7 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
             cre[c] = 0;
             cim[c] = 0;
             Q[c] = cf{0.f, 0.f, 0.f, 0.f};
+            s2f[c] = 0.f;
         }
         int gsum = 0;
         double whigh = 1.0;
@@ -476,6 +481,8 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
                         t.im = dd_add(t.im, dd{(double)Q[c].ih * whigh, (double)Q[c].il * whigh});
                         my_acc[c * kThreads] = t;
                         Q[c] = cf{0.f, 0.f, 0.f, 0.f};
+                        my_s2[c * kThreads] += (double)s2f[c] * whigh * whigh;
+                        s2f[c] = 0.f;
                     }
                 }
             }
@@ -519,6 +526,7 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
                 if (cp[c] > 1) lo = cf_mul_pow(lo, x[c], cp[c] - 1);
                 df_add_lazy2(Q[c].rh, Q[c].rl, lo.rh, lo.rl);
                 df_add_lazy2(Q[c].ih, Q[c].il, lo.ih, lo.il);
+                s2f[c] = fmaf(lo.rh, lo.rh, fmaf(lo.ih, lo.ih, s2f[c]));
                 if (c > 0) suf = cf_mul(suf, P[c]);
             }
             if ((k & 7ull) == 7ull) {
@@ -535,6 +543,7 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
             t.re = dd_add(t.re, dd{(double)Q[c].rh * whigh, (double)Q[c].rl * whigh});
             t.im = dd_add(t.im, dd{(double)Q[c].ih * whigh, (double)Q[c].il * whigh});
             my_acc[c * kThreads] = t;
+            my_s2[c * kThreads] += (double)s2f[c] * whigh * whigh;
         }
     }
     __syncthreads();
@@ -543,18 +552,67 @@ __global__ void __launch_bounds__(kThreads) pmf_df_kernel(RepArgs p, cdd* col_pa
     for (int j = threadIdx.x; j < NP; j += blockDim.x) {
         const int gj = j / CPL, c = j % CPL;
         cdd b = s_acc[c * kThreads + gj];
-        for (int t = gj + G; t < kThreads; t += G) b = cdd_add(b, s_acc[c * kThreads + t]);
-        if (j < C) col_part[(size_t)blockIdx.x * C + j] = b;
+        double bq = s_s2[c * kThreads + gj];
+        for (int t = gj + G; t < kThreads; t += G) {
+            b = cdd_add(b, s_acc[c * kThreads + t]);
+            bq += s_s2[c * kThreads + t];
+        }
+        if (j < C) {
+            col_part[(size_t)blockIdx.x * C + j] = b;
+            col_s2[(size_t)blockIdx.x * C + j] = bq;
+        }
+    }
+}
+
+// Between the double-float kernel and its FP64 twin: sum each column's block
+// partials and |LO|^2 sums (a warp per column, fixed order), estimate each
+// leave-one-out permanent's relative rounding error as
+// sqrt(nfac) 2^-46 sqrt(sum |LO|^2) / |perm|, and when the largest is above
+// kDfEscalate (or not finite) clear df_info[1] so that the FP64 twin
+// recomputes the whole layer.  err_out receives the largest estimate (-1
+// when the range check had already sent the layer to the FP64 kernel).
+__global__ void __launch_bounds__(kFinThreads) pmf_check_kernel(const cdd* col_part, const double* col_s2,
+                                                                int nblocks, int C, double nfac, int* df_info,
+                                                                double* err_out, int escalate) {
+    __shared__ double s_max[kFinThreads / 32];
+    if (df_info[1] == 0) {  // block-uniform: the double-float kernel did not run
+        if (threadIdx.x == 0) *err_out = -1.0;
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double mx = 0.0;
+    for (int j = warp; j < C; j += nw) {
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        double q = 0.0;
+        for (int b = lane; b < nblocks; b += 32) {
+            tot = cdd_add(tot, col_part[(size_t)b * C + j]);
+            q += col_s2[(size_t)b * C + j];
+        }
+        tot = warp_sum_cdd(tot);
+        q = warp_sum_d(q);
+        double est = sqrt(nfac) * 0x1p-46 * sqrt(q) / hypot(tot.re.hi, tot.im.hi);
+        if (!(est == est)) est = INFINITY;
+        mx = fmax(mx, est);
+    }
+    if (lane == 0) s_max[warp] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = s_max[0];
+        for (int w = 1; w < nw; ++w) m = fmax(m, s_max[w]);
+        *err_out = m;
+        if (escalate && !(m <= kDfEscalate)) df_info[1] = 0;
     }
 }
 
 // Sum the block partials per column in a fixed order and scale: perm_l =
 // sum * 2^(exp - e_l + o) (column l lost one factor of its 2^-e_l scaling
-// and, in the double-float product, of the range boost 2^o).
+// and, in the double-float product, of the range boost 2^o; exp includes the
+// boost over all factors, exp_fp64 is the exponent without it).
 // Then the contraction with the interferometer and the normalisation, in the
 // reference's order (input modes ascending, total over modes ascending).
 __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* col_part, int nblocks, int C,
-                                                                   const int* exp_in, const int* col_e,
+                                                                   const int* exp_in, const int* exp_fp64,
+                                                                   const int* col_e,
                                                                    const int* df_info, const int* col_mode,
                                                                    const double* cin_w,
                                                                    const double2* U, long long ldu, int m,
@@ -571,8 +629,12 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
         tot = warp_sum_cdd(tot);
         if (lane == 0) {
             double o[2];
-            const int boost = df_info ? df_info[0] : 0;
-            write_result(tot, *exp_in - (col_e[j] - boost), o, nullptr);
+            // the double-float partials carry the range boost; the FP64
+            // twin's (it ran when the range check or the error estimate sent
+            // the layer to it) do not
+            const bool dfok = df_info && df_info[1];
+            const int ex = dfok ? *exp_in - (col_e[j] - df_info[0]) : *exp_fp64 - col_e[j];
+            write_result(tot, ex, o, nullptr);
             s_perm[j] = make_double2(o[0], o[1]);
         }
     }
@@ -656,20 +718,25 @@ cudaError_t pmf_launch(const RepArgs& a, int cpl, int grp, cdd* col_part, int gr
 }
 
 template <int CPL>
+size_t pmf_df_smem(const RepArgs& a) {
+    return pmf_smem<CPL, 4>(a) + (size_t)CPL * kThreads * sizeof(double);
+}
+
+template <int CPL>
 int pmf_df_bps_t(const RepArgs& a) {
     int nb = 0;
-    size_t smem = pmf_smem<CPL, 4>(a);
+    size_t smem = pmf_df_smem<CPL>(a);
     allow_max_dynamic_smem((const void*)pmf_df_kernel<CPL>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pmf_df_kernel<CPL>, kThreads, smem);
     return nb > 0 ? nb : 1;
 }
 
 template <int CPL>
-cudaError_t pmf_df_launch_t(const RepArgs& a, cdd* col_part, int grid, cudaStream_t st) {
-    size_t smem = pmf_smem<CPL, 4>(a);
+cudaError_t pmf_df_launch_t(const RepArgs& a, cdd* col_part, double* col_s2, int grid, cudaStream_t st) {
+    size_t smem = pmf_df_smem<CPL>(a);
     cudaError_t e = allow_max_dynamic_smem((const void*)pmf_df_kernel<CPL>);
     if (e != cudaSuccess) return e;
-    pmf_df_kernel<CPL><<<grid, kThreads, smem, st>>>(a, col_part);
+    pmf_df_kernel<CPL><<<grid, kThreads, smem, st>>>(a, col_part, col_s2);
     return cudaGetLastError();
 }
 
@@ -682,12 +749,12 @@ int pmf_df_bps(const RepArgs& a, int cpl) {
     }
 }
 
-cudaError_t pmf_df_launch(const RepArgs& a, int cpl, cdd* col_part, int grid, cudaStream_t st) {
+cudaError_t pmf_df_launch(const RepArgs& a, int cpl, cdd* col_part, double* col_s2, int grid, cudaStream_t st) {
     switch (cpl) {
-        case 1: return pmf_df_launch_t<1>(a, col_part, grid, st);
-        case 2: return pmf_df_launch_t<2>(a, col_part, grid, st);
-        case 4: return pmf_df_launch_t<4>(a, col_part, grid, st);
-        default: return pmf_df_launch_t<8>(a, col_part, grid, st);
+        case 1: return pmf_df_launch_t<1>(a, col_part, col_s2, grid, st);
+        case 2: return pmf_df_launch_t<2>(a, col_part, col_s2, grid, st);
+        case 4: return pmf_df_launch_t<4>(a, col_part, col_s2, grid, st);
+        default: return pmf_df_launch_t<8>(a, col_part, col_s2, grid, st);
     }
 }
 
@@ -809,6 +876,7 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     const size_t o_pmf = take((size_t)m * sizeof(double));
     const size_t o_add = take((size_t)m * sizeof(double2));  // 16-byte elements: own aligned region
     const size_t o_part = take((size_t)grid * C * sizeof(cdd));
+    const size_t o_s2 = take((size_t)grid * C * sizeof(double));
     rc = cx.ensure(off);
     if (rc) return rc;
     char* base = static_cast<char*>(cx.dbuf);
@@ -865,6 +933,8 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         pa.col_e_out = d_ints + i_cole;
         pa.df = df ? 1 : 0;
         pa.df_info = df ? d_exp + 4 : nullptr;
+        pa.row_balance = 1;
+        pa.exp_fp64_out = d_exp + 1;
         e = launch_prepare(pa, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: prepare");
         a.a1 = pa.a1;
@@ -877,24 +947,31 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         a.binom = reinterpret_cast<const double*>(base + o_binom);
         a.df_info = pa.df_info;
         if (df) {
-            e = pmf_df_launch(a, cpl, d_part, grid, st);
+            double* d_s2 = reinterpret_cast<double*>(base + o_s2);
+            e = pmf_df_launch(a, cpl, d_part, d_s2, grid, st);
             if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: df launch");
+            // error estimate before the FP64 twin, which runs when it fails
+            pmf_check_kernel<<<1, kFinThreads, 0, st>>>(d_part, d_s2, grid, C, (double)h.photons, d_exp + 4,
+                                                        reinterpret_cast<double*>(d_exp + 8),
+                                                        g_opt.df_escalate.load() != 0 ? 1 : 0);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: check launch");
         }
         e = pmf_launch(a, cpl, grp, d_part, grid, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: launch");
     } else {
         // no sample yet: every permanent is of an empty matrix, i.e. 1
         ones.assign(C, cdd{{1.0, 0.0}, {0.0, 0.0}});
-        zero.assign(1, 0);
+        zero.assign(2, 0);  // exponent with and without the boost
         e = cudaMemcpyAsync(d_part, ones.data(), C * sizeof(cdd), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_exp, zero.data(), sizeof(int), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_exp, zero.data(), 2 * sizeof(int), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: upload");
         nblocks = 1;
     }
     double* d_pmf = reinterpret_cast<double*>(base + o_pmf);
     double2* d_add = reinterpret_cast<double2*>(base + o_add);
     const size_t fsmem = (size_t)C * sizeof(double2);
-    pmf_finalize_kernel<<<1, kFinThreads, fsmem, st>>>(d_part, nblocks, C, d_exp, d_ints + i_cole,
+    pmf_finalize_kernel<<<1, kFinThreads, fsmem, st>>>(d_part, nblocks, C, d_exp, d_exp + 1, d_ints + i_cole,
                                                        df ? d_exp + 4 : nullptr, d_ints + i_mode,
                                                        reinterpret_cast<const double*>(base + o_cw),
                                                        reinterpret_cast<const double2*>(base + o_U), m, (int)m,
@@ -913,12 +990,18 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         stats->kernel_ms = ms;
         stats->steps = first_photon ? 0.0 : h.steps;
         stats->flops = first_photon ? 0.0 : pmf_step_flops(C, cpl, grp) * h.steps;
-        stats->launches = first_photon ? 1 : (df ? 4 : 3);
+        stats->launches = first_photon ? 1 : (df ? 5 : 3);
         stats->grid = grid;
         stats->seg_log2 = h.q;
         int info[2] = {0, 0};
-        if (df) cudaMemcpy(info, d_exp + 4, sizeof(info), cudaMemcpyDeviceToHost);
-        stats->arith = (df && info[1]) ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        double est = 0.0;
+        if (df && !first_photon) {
+            cudaMemcpy(info, d_exp + 4, sizeof(info), cudaMemcpyDeviceToHost);
+            cudaMemcpy(&est, d_exp + 8, sizeof(est), cudaMemcpyDeviceToHost);
+        }
+        const bool used_df = df && !first_photon && info[1];
+        stats->arith = used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->err_est = (df && !first_photon && est >= 0.0) ? est : 0.0;
     }
     return GBPERM_OK;
 }

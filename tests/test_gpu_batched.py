@@ -110,3 +110,16 @@ def test_batched_device_pointer_run_with_trivial_slots():
         assert abs(complex(re, im) - h) <= 1e-12 * max(abs(h), 1.0)
     assert complex(*dev[1]) == 1.0 and complex(*dev[-1]) == 0.0
     plan.close()
+
+
+def test_batched_fast_within_bar_of_fp64():
+    # the bench's uneven k = 8..28 instances (rows and columns drawn with
+    # repetition): every double-float result whose error estimate is above
+    # 1e-10 is recomputed with the FP64 product, so all are within the bar
+    from piquassoboost_gb300.workloads import batched_instances
+    mats = batched_instances(4096, seed=36)
+    st = nat.Stats()
+    f = np.array(nat.perm_batched(mats, mode="fast", stats=st))
+    d = np.array(nat.perm_batched(mats, mode="fp64"))
+    assert np.max(np.abs(f - d) / np.abs(d)) <= 1e-10
+    assert 0.0 < st.err_est <= 1e-10

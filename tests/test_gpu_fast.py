@@ -57,3 +57,52 @@ def test_fast_all_ones():
     for n in (8, 16, 24):
         v = nat.perm(np.ones((n, n)), mode="fast")
         assert abs(v - math.factorial(n)) <= TOL * math.factorial(n)
+
+
+def test_fast_escalates_to_fp64_when_estimate_exceeds_bar():
+    # a positive matrix: its Gray terms are huge next to the permanent, so the
+    # double-float estimate exceeds 1e-10 and the FP64 twin recomputes on the
+    # device; the result is then the FP64 kernel's, bit for bit
+    rng = np.random.default_rng(28)
+    G = np.abs(rng.standard_normal((28, 28))) + 0.1
+    st = nat.Stats()
+    v = nat.perm(G, mode="fast", stats=st)
+    assert st.arith == 0 and not (st.err_est <= 1e-10)
+    assert v == nat.perm(G, mode="fp64")
+    # with escalation off the double-float result stands, with its estimate
+    nat.set_option("df.escalate", 0)
+    try:
+        st2 = nat.Stats()
+        nat.perm(G, mode="fast", stats=st2)
+        assert st2.arith == 1 and st2.err_est == st.err_est
+    finally:
+        nat.set_option("df.escalate", 1)
+
+
+@pytest.mark.parametrize("n", [20, 24, 28])
+def test_fast_error_estimate_covers_the_error(n):
+    # well-conditioned inputs stay on the double-float product, and its
+    # error against the FP64 kernel is within a few times the estimate
+    for seed in range(3):
+        A = haar_block(n, seed=100 * n + seed)
+        st = nat.Stats()
+        v = nat.perm(A, mode="fast", stats=st)
+        r = nat.perm(A, mode="fp64")
+        if st.arith == 1:
+            assert 0.0 < st.err_est <= 1e-10
+            assert abs(v - r) <= 3.0 * st.err_est * abs(r) + 1e-14 * abs(r)
+        else:
+            assert v == r
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fast"])
+def test_row_scaled_matrix_meets_bar(mode):
+    # rows scaled by factors up to ~10: without the exact power-of-two row
+    # balancing the Gray sum cancels catastrophically (the double-float
+    # product was off by 1e-5 .. 1e-2 here)
+    for seed in range(4):
+        rng = np.random.default_rng(400 + seed)
+        A = np.exp(rng.uniform(-2.3, 2.3, 18))[:, None] * haar_block(18, seed=400 + seed)
+        v = nat.perm(A, mode=mode)
+        _, q = orc.bbfg(A, prec=1)
+        assert orc.rel_err(v, q) <= TOL
