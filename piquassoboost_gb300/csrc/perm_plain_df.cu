@@ -33,10 +33,7 @@ template <int CPL, int GROUP>
 // up to 18 columns per lane the kernel fits 128 registers (4 blocks per SM),
 // above that 168 (3 blocks); the allocator is held to those, which it
 // otherwise gives up for a few more live values
-#ifndef GBPERM_PLAIN_DF_MINB
-#define GBPERM_PLAIN_DF_MINB (CPL <= 18 ? 4 : 3)
-#endif
-__global__ void __launch_bounds__(kThreads, GBPERM_PLAIN_DF_MINB) plain_df_kernel(PlainArgs p) {
+__global__ void __launch_bounds__(kThreads, (CPL <= 18 ? 4 : 3)) plain_df_kernel(PlainArgs p) {
     constexpr int NP = CPL * GROUP;  // padded columns
     extern __shared__ __align__(16) unsigned char smem_raw[];
     longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);
@@ -169,10 +166,8 @@ __global__ void __launch_bounds__(kThreads, GBPERM_PLAIN_DF_MINB) plain_df_kerne
                 df_acc(bih, bil, __uint_as_float(__float_as_uint(pa.ih) ^ sbit),
                        __uint_as_float(__float_as_uint(pa.il) ^ sbit));
                 // terms sit near 2^-40 (the range boost centres them there)
-#ifndef GBPERM_NO_S2
                 const float ur = pa.rh * 0x1p40f, ui = pa.ih * 0x1p40f;
                 s2f = fmaf(ur, ur, fmaf(ui, ui, s2f));
-#endif
             }
         }
         acc.re = dd_add(acc.re, dd{(double)brh, (double)brl});
