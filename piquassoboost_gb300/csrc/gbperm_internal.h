@@ -48,13 +48,16 @@ struct PrepArgs {
     // component) and add sum_i w_i k_i to exp_out.  Exact, and it removes
     // the cancellation that unequal row norms cause in the Gray sum.  Valid
     // when the sum is multilinear in the (expanded) rows: square plain
-    // matrices, the repeated and leave-one-out sums; off for rectangular
-    // matrices and for the gradient, whose entries would need a per-row
-    // correction
+    // matrices, the repeated and leave-one-out sums, and the gradient (whose
+    // entry (k, l) then takes exponent exp - e_l - k_k: row_k_out); off for
+    // rectangular matrices
     int row_balance = 0;
     // optional: the exponent without the double-float boost, for the FP64
     // twin when it takes over from a double-float kernel that ran
     int* exp_fp64_out = nullptr;
+    // optional: the row scaling exponents k_i (rows ints per matrix), for
+    // results that lose a row (the gradient's minors)
+    int* row_k_out = nullptr;
 };
 cudaError_t launch_prepare(const PrepArgs& a, cudaStream_t st);
 

@@ -360,7 +360,7 @@ __global__ void grad_partial_kernel(const float4* warp_g, int nwarps, int n, flo
 // Second stage: sum the chunk partials in a fixed order in double-double,
 // scale, write the gradient (complex128, n x n row-major).
 __global__ void grad_finalize_kernel(const float4* part, int nchunks, int n, const int* exp_in, const int* col_e,
-                                     const int* df_info, double* grad) {
+                                     const int* row_k, const int* df_info, double* grad) {
     const int ne = n * n;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
@@ -368,6 +368,7 @@ __global__ void grad_finalize_kernel(const float4* part, int nchunks, int n, con
     part += inst * nchunks * ne;
     exp_in += inst;
     col_e += inst * n;
+    row_k += inst * n;
     df_info += 2 * inst;
     grad += inst * 2 * n * n;
     if (df_info[1] == 0) {
@@ -380,9 +381,11 @@ __global__ void grad_finalize_kernel(const float4* part, int nchunks, int n, con
         acc.re = dd_add(acc.re, dd{(double)v.x, (double)v.y});
         acc.im = dd_add(acc.im, dd{(double)v.z, (double)v.w});
     }
-    const int l = e % n;
-    // W_l omits column l: remove its factor from the permanent's scale
-    const int ex = *exp_in - (col_e[l] - df_info[0]);
+    const int l = e % n, k = e / n;
+    // the minor omits row k and column l: remove column l's factor (its
+    // 2^-e_l scaling and the range boost) and row k's 2^-k_k balancing
+    // from the permanent's scale
+    const int ex = *exp_in - (col_e[l] - df_info[0]) - row_k[k];
     double r2[2];
     write_result(acc, ex, r2, nullptr);
     grad[2 * e] = r2[0];
@@ -544,7 +547,7 @@ static GradPlan plan_grad(int n, int count) {
 }
 
 struct GradWs {
-    size_t a1, a2, exp, dfi, cole, warp_g, part, total;
+    size_t a1, a2, exp, dfi, cole, rowk, warp_g, part, total;
 };
 
 static GradWs grad_ws_layout(int n, const GradPlan& gp) {
@@ -561,6 +564,7 @@ static GradWs grad_ws_layout(int n, const GradPlan& gp) {
     w.exp = take(c * sizeof(int));
     w.dfi = take(c * 2 * sizeof(int));
     w.cole = take(c * n * sizeof(int));
+    w.rowk = take(c * n * sizeof(int));
     w.warp_g = take(c * gp.nwarps * n * n * sizeof(float4));
     w.part = take(c * gp.nchunks * n * n * sizeof(float4));
     w.total = off;
@@ -595,6 +599,7 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         int* exp_out = reinterpret_cast<int*>(base + w.exp);
         int* df_info = reinterpret_cast<int*>(base + w.dfi);
         int* col_e = reinterpret_cast<int*>(base + w.cole);
+        int* row_k = reinterpret_cast<int*>(base + w.rowk);
         float4* warp_g = reinterpret_cast<float4*>(base + w.warp_g);
         float4* fin_part = reinterpret_cast<float4*>(base + w.part);
         PrepArgs pa;
@@ -613,6 +618,8 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         pa.df_info = df_info;
         pa.count = c;
         pa.a_stride = stride;
+        pa.row_balance = 1;
+        pa.row_k_out = row_k;
         cudaError_t e = launch_prepare(pa, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: prepare");
         GradArgs g;
@@ -633,7 +640,7 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         grad_partial_kernel<<<dim3((ne + 127) / 128, gp.nchunks, c), 128, 0, st>>>(warp_g, gp.nwarps, n, fin_part);
         double* gout = d_grad + (size_t)done * 2 * n * n;
         grad_finalize_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(fin_part, gp.nchunks, n, exp_out, col_e,
-                                                                        df_info, gout);
+                                                                        row_k, df_info, gout);
         grad_perm_kernel<<<c, 32, 0, st>>>(dA + (long long)done * stride, ld, stride, n, gout, df_info,
                                            d_perm + (size_t)done * 2, d_perm4 ? d_perm4 + (size_t)done * 4 : nullptr);
         e = cudaGetLastError();
@@ -700,7 +707,7 @@ static int perm_grad_host(const double* A, int64_t n, int64_t count, int64_t ld,
         const double* Ab = A + 2 * b * stride;
         if (!all_finite(Ab, n, n, ld)) continue;  // NaN out, below
         int boost = 0;
-        if (!df_boost(Ab, n, n, ld, nullptr, nullptr, &boost, false))
+        if (!df_boost(Ab, n, n, ld, nullptr, nullptr, &boost, true))
             return fail(GBPERM_ERR_TOO_LARGE,
                         std::string(who) + ": matrix dynamic range beyond the double-float product");
     }

@@ -16,6 +16,7 @@ __global__ void prepare_kernel(PrepArgs p) {
         p.a2 += (size_t)bt * p.rows * p.cols;
         p.exp_out += bt;
         if (p.exp_fp64_out) p.exp_fp64_out += bt;
+        if (p.row_k_out) p.row_k_out += (size_t)bt * p.rows;
         if (p.col_e_out) p.col_e_out += (size_t)bt * p.cols;
         if (p.df_info) p.df_info += 2 * bt;
     }
@@ -33,6 +34,7 @@ __global__ void prepare_kernel(PrepArgs p) {
             if (mx > 0.0) frexp(mx, &k);
         }
         s_k[i] = k;
+        if (p.row_k_out) p.row_k_out[i] = k;
     }
     __syncthreads();
     for (int j = threadIdx.x; j < p.cols; j += blockDim.x) {

@@ -112,3 +112,18 @@ def test_grad_batched_minors():
             for l in range(9):
                 ref, _ = orc.bbfg(_minor(mats[b], k, l), prec=1)
                 assert abs(grads[b, k, l] - ref) <= 1e-10 * max(abs(ref), 1e-3 * gnorm)
+
+
+def test_grad_row_scaled_matrix():
+    # rows scaled by factors up to ~10: the rows are balanced by exact powers
+    # of two before the sweep, and each entry's exponent drops its row's
+    # factor; permanent and minors against the binary128 oracle
+    rng = np.random.default_rng(9)
+    n = 14
+    A = np.exp(rng.uniform(-2.3, 2.3, n))[:, None] * haar_block(n, seed=9)
+    p, G = nat.perm_grad(A)
+    _, ref = orc.bbfg(A, prec=1)
+    assert orc.rel_err(p, ref) <= 1e-10
+    for r, c in [(0, 0), (3, 7), (n - 1, 2), (5, n - 1), (9, 9)]:
+        _, m = orc.bbfg(np.delete(np.delete(A, r, 0), c, 1), prec=1)
+        assert orc.rel_err(G[r, c], m) <= 1e-10, (r, c)
