@@ -6,6 +6,7 @@
 * the drop-in classes keep the reference's lib-id table, messages and state
   coercion (Boson_Sampling_Utilities.py:30-335).
 """
+import ctypes
 import os
 import re
 
@@ -48,6 +49,15 @@ def test_version_and_errors(lib):
     assert nat.get_option("plain.seg_log2") == -1
     with pytest.raises(nat.GBPermError):
         nat.set_option("no.such.key", 1)
+    # double-float results above the error bar go to FP64 unless switched off
+    assert nat.get_option("df.escalate") == 1
+    nat.set_option("df.escalate", 0)
+    try:
+        assert nat.get_option("df.escalate") == 0
+    finally:
+        nat.set_option("df.escalate", 1)
+    # the stats record carries the error estimate after the four int32 fields
+    assert nat.Stats.err_est.offset == 40 and ctypes.sizeof(nat.Stats) == 48
 
 
 def test_trivial_shapes_need_no_gpu():
