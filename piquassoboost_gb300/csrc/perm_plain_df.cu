@@ -12,6 +12,11 @@
 // holds only CPL column sums (4 CPL registers) and the SM keeps more warps
 // in flight to hide the float-pair dependency chains.  The changed row is
 // still warp-uniform (aligned segments of equal length).
+//
+// Accuracy guard: the leaders also sum |term|^2, and the grid finish
+// (df_grid_finish) turns it into an estimate of the result's relative
+// rounding error; above 1e-10 it clears the range-check flag, so the FP64
+// twin (perm_plain.cu), launched next on the same stream, recomputes.
 #include "gbperm_internal.h"
 
 namespace gbperm {

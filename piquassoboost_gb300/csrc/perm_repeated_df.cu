@@ -7,7 +7,10 @@
 // [g*CPL, (g+1)*CPL) and a shuffle butterfly multiplies the partials.  Every
 // lane of a group tracks the same Gray digits (they are cheap integers), so
 // the weights and signs need no exchange.  Segment loops run over warp-sized
-// blocks of segments so all 32 lanes always reach the shuffles.
+// blocks of segments so all 32 lanes always reach the shuffles.  As in
+// perm_plain_df.cu the sweep ends with a rounding-error estimate that hands
+// the result to the FP64 twin when it is above 1e-10 (at 30 photons most
+// bunched outputs are).
 #include "gbperm_internal.h"
 
 namespace gbperm {

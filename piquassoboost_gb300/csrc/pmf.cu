@@ -23,7 +23,9 @@
 // are exact int64 fixed point and the digit walk is the one of
 // perm_repeated.cu; the product runs on the FP64 pipe.  A step costs about
 // 4 C complex multiplies for all C permanents, against C - 1 per permanent
-// (C^2 in all) in the per-mode form.
+// (C^2 in all) in the per-mode form.  The double-float twin (pmf_df_kernel)
+// is followed by a check kernel that estimates each permanent's rounding
+// error and hands the layer to the FP64 kernel when any is above 1e-10.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
