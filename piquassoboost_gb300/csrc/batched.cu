@@ -45,10 +45,12 @@ struct BInst {              // device instance descriptor
 };
 
 struct BInstOut {           // written by the batched prepare kernel
-    int exp;
+    int exp;                // result exponent of the double-float product (with the boost)
+    int exp64;              // result exponent of the FP64 product
     int boost;
-    int ok;                 // double-float range check
+    int ok;                 // double-float product in use (range check; cleared to redo in FP64)
     int finite;             // input finite
+    int redo;               // the FP64 pass recomputes this instance
 };
 
 struct BItem {
@@ -70,8 +72,10 @@ struct BArgs {
     cdd* item_part;
     double* item_s2;        // per item: sum of |term 2^40|^2 of its double-float terms
     double* out;            // 2 doubles per instance (device)
-    double* inst_est;       // per instance: relative error estimate (-1: FP64 product)
+    double* inst_est;       // per instance: relative error estimate (-1: FP64 product, -2: recomputed in FP64)
     int df;
+    int escalate;           // mark double-float instances above the error bar for the FP64 pass
+    int redo_only;          // the FP64 pass: only instances marked redo
 };
 
 // One block per instance (grid-stride): fixed point, exponent and
@@ -127,9 +131,11 @@ __global__ void batched_prepare_kernel(BArgs p) {
             }
             BInstOut r;
             r.exp = (int)(tot - (long long)o * in.cols - (in.rows - 1));
+            r.exp64 = (int)(tot - (in.rows - 1));
             r.boost = o;
             r.ok = ok;
             r.finite = s_bad ? 0 : 1;
+            r.redo = 0;
             p.iout[i] = r;
         }
         __syncthreads();
@@ -157,8 +163,9 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= p.nitems) break;
         const BItem item = p.items[it];
-        const BInst in = p.inst[item.inst];
         const BInstOut io = p.iout[item.inst];
+        if (p.redo_only && !io.redo) continue;  // warp-uniform
+        const BInst in = p.inst[item.inst];
         const int rows = in.rows, cols = in.cols;
         const unsigned long long s = item.seg0 + (unsigned long long)grp;
         const bool active = s < in.nseg && io.finite;
@@ -364,6 +371,7 @@ __global__ void batched_finalize_kernel(BArgs p) {
     for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.ninst; i += nw) {  // warp-uniform
         const BInst in = p.inst[i];
         const BInstOut io = p.iout[i];
+        if (p.redo_only && !io.redo) continue;
         if (!io.finite) {
             if (lane == 0) {
                 p.out[2 * i] = nan("");
@@ -381,12 +389,23 @@ __global__ void batched_finalize_kernel(BArgs p) {
         tot = warp_sum_cdd(tot);
         q = warp_sum_d(q);
         if (lane == 0) {
-            write_result(tot, io.exp, p.out + 2 * i, nullptr);
-            // relative rounding-error estimate of a double-float result, as
-            // in the single-permanent kernels (-1: the FP64 product ran)
-            p.inst_est[i] = (p.df && io.ok)
-                                ? sqrt((double)in.cols) * 0x1p-46 * sqrt(q) * 0x1p-40 / hypot(tot.re.hi, tot.im.hi)
-                                : -1.0;
+            write_result(tot, io.ok ? io.exp : io.exp64, p.out + 2 * i, nullptr);
+            if (p.redo_only) {
+                p.inst_est[i] = -2.0;
+            } else if (p.df && io.ok) {
+                // relative rounding-error estimate of a double-float result,
+                // as in the single-permanent kernels; above the bar the
+                // instance goes to the FP64 pass that follows
+                const double est =
+                    sqrt((double)in.cols) * 0x1p-46 * sqrt(q) * 0x1p-40 / hypot(tot.re.hi, tot.im.hi);
+                p.inst_est[i] = est;
+                if (p.escalate && !(est <= kDfEscalate)) {
+                    p.iout[i].ok = 0;
+                    p.iout[i].redo = 1;
+                }
+            } else {
+                p.inst_est[i] = -1.0;
+            }
         }
     }
 }
@@ -482,6 +501,7 @@ struct BatchPlan {
     int64_t count = 0;
     int arith = GBPERM_ARITH_FP64;
     bool df = false;
+    bool escalate = true;            // double-float instances above the error bar redone in FP64
     int cpl = 16, grp = 1;
     int grid = 1;
     int maxc = 1;                    // widest instance (columns)
@@ -549,6 +569,8 @@ static BArgs plan_args(BatchPlan* p) {
     a.out = p->dout;
     a.inst_est = p->dest;
     a.df = p->df ? 1 : 0;
+    a.escalate = p->escalate ? 1 : 0;
+    a.redo_only = 0;
     return a;
 }
 
@@ -562,6 +584,16 @@ static cudaError_t plan_enqueue(BatchPlan* p) {
     int pg = std::min(p->ninst, 4 * device_sms(p->device));
     batched_prepare_kernel<<<pg, 64, 0, p->stream>>>(a);
     e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = batch_launch(a, p->cpl, p->grp, p->df, p->grid, p->stream);
+    if (e != cudaSuccess) return e;
+    batched_finalize_kernel<<<(p->ninst + 3) / 4, 128, 0, p->stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !(p->df && p->escalate)) return e;
+    // the FP64 pass over the instances whose double-float estimate was above
+    // the bar (usually none: the warps fetch every item and skip the rest)
+    a.redo_only = 1;
+    e = cudaMemsetAsync(p->dcounter, 0, sizeof(unsigned int), p->stream);
     if (e != cudaSuccess) return e;
     e = batch_launch(a, p->cpl, p->grp, p->df, p->grid, p->stream);
     if (e != cudaSuccess) return e;
@@ -723,6 +755,7 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
         return cuda_fail(e, "gbperm_batch_plan_create");
     }
     p->df = arith == GBPERM_ARITH_DF32 && maxc <= kDfMaxCols;
+    p->escalate = g_opt.df_escalate.load() != 0;
     p->maxc = maxc;
     batch_shape(maxc, p->df, (int)g_opt.batched_threads.load(), &p->cpl, &p->grp);
     int bps = batch_bps(p->cpl, p->grp, p->df);
@@ -823,7 +856,6 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         e = cudaStreamSynchronize(p->stream);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_batch_plan_run: kernels");
     }
-    int escalated = 0;
     double worst = 0.0;  // largest estimate among the double-float results kept
     for (int64_t i = 0; i < p->count; ++i) {
         int d = p->dev_index[i];
@@ -833,17 +865,10 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         } else {
             out[2 * i] = p->hout[2 * d];
             out[2 * i + 1] = p->hout[2 * d + 1];
-            // a double-float result whose error estimate is above the bar
-            // is recomputed with the FP64 product (rare: one in thousands
-            // of the uneven k = 8..28 batches)
-            if (p->df && p->hest[d] >= 0.0 && !(p->hest[d] <= kDfEscalate) && g_opt.df_escalate.load() != 0) {
-                int rc = gbperm_perm(packed + 2 * p->off[i], p->rows[i], p->cols[i], p->cols[i], GBPERM_ARITH_FP64,
-                                     out + 2 * i, nullptr, nullptr);
-                if (rc) return rc;
-                ++escalated;
-            } else if (p->df && p->hest[d] >= 0.0) {
-                worst = std::max(worst, p->hest[d]);
-            }
+            // the estimate is -2 when the FP64 pass recomputed the instance
+            // (its double-float estimate was above the bar; rare: one in
+            // thousands of the k = 8..28 batches), -1 for the FP64 product
+            if (p->df && p->hest[d] >= 0.0) worst = std::max(worst, p->hest[d]);
         }
     }
     if (stats && p->ninst > 0) {
@@ -852,7 +877,7 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         stats->kernel_ms = ms;
         stats->steps = p->steps;
         stats->flops = p->flops;
-        stats->launches = 3 + 2 * escalated;  // + prepare and FP64 kernel per recomputed instance
+        stats->launches = (p->df && p->escalate) ? 5 : 3;  // + the FP64 pass and its finalize
         stats->err_est = worst;
         stats->grid = p->grid;
         stats->seg_log2 = (int)p->item_target_log2;
