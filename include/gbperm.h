@@ -62,8 +62,8 @@ typedef struct gbperm_stats {
                               estimated relative rounding error of its result,
                               sqrt(n) 2^-46 sqrt(sum |term|^2) / |perm| (pmf: the largest over the
                               layer's permanents; batched: the largest over the results kept in
-                              double-float).  Above 1e-10 the FP64 product recomputed the result (on
-                              the device; batched host calls: per instance on the host path) and
+                              double-float).  Above 1e-10 the FP64 product recomputed the result on
+                              the device (batched: per instance, in a second pass of the plan) and
                               arith reports FP64.  0 when only the FP64 product ran */
 } gbperm_stats;
 
