@@ -272,7 +272,8 @@ def run_ours(args, rank, world, local):
     d_out = torch.zeros(2, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     # prepare + permanent kernel (+ the FP64 twin of the double-float kernel,
-    # which returns at once when the range check passed)
+    # which returns at once unless the range check or the error estimate
+    # hands it the permanent)
     launches_per_step = 3 if args.mode == "fast" else 2
 
     def step(i):

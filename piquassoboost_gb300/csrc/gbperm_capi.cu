@@ -214,7 +214,8 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
     if (plan.df) {
         // the double-float kernel returns at once if the device range check
-        // failed; its FP64 twin below returns at once if it passed
+        // failed; its FP64 twin below returns at once unless that check
+        // failed or the double-float result's error estimate was above the bar
         double* err = d_err ? d_err : reinterpret_cast<double*>(base + w.scale + 8);
         e = cudaMemsetAsync(err, 0, sizeof(double), st);
         if (e != cudaSuccess) return cuda_fail(e, "plain df error slot");
