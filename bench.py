@@ -352,7 +352,8 @@ def run_ours(args, rank, world, local):
             "peak_source": "measured live by gbperm_probe_peak (DFMA probe), this run"}
     if args.mode == "fast":
         roof["note"] = ("double-float product on the FP32 pipe: frac is against the FP64 FMA peak "
-                        "(the north-star denominator); the FP32 FMA peak measured in the same run is "
+                        "(the FP64 roofline the target is stated against); the FP32 FMA peak measured "
+                        "in the same run is "
                         f"{peaks['fp32_tflops']:.1f} TFLOP/s")
         roof["fp32_peak_tflops"] = peaks["fp32_tflops"]
 
