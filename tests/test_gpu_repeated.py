@@ -45,7 +45,7 @@ def test_repeated_matches_expanded_plain():
 
 
 @pytest.mark.parametrize("mode", ["fp64", "fast"])
-def test_repeated_config3_small(mode):
+def test_repeated_24_modes_12_photons(mode):
     U, inp, out = repeated_instance(seed=11, modes=24, photons=12, max_mult=4)
     st = nat.Stats()
     v = nat.perm_repeated(U, inp, out, mode=mode, stats=st)
