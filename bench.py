@@ -52,15 +52,21 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain", choices=["plain", "repeated", "batched", "grad", "pmf", "mesh"],
                     help="plain: single n x n Haar block (default); repeated: 60-mode / 30-photon "
-                         "multiplicity permanent; batched: 4096 uneven k=8..28 permanents in one launch; "
+                         "multiplicity permanent; batched: 4096 uneven k=8..28 permanents in one launch "
+                         "(--batch-count, --batch-kmax); "
                          "grad: permanent + full gradient; pmf: one 60-mode / 30-photon boson-sampling "
                          "probability layer; mesh: 512-term Clements-mesh log-likelihood, forward + backward")
     ap.add_argument("--n", type=int, default=36)
     ap.add_argument("--mode", default="fast", choices=["fast", "fp64"])
     ap.add_argument("--seed", type=int, default=36)
+    ap.add_argument("--batch-count", type=int, default=4096, help="batched: permanents per batch")
+    ap.add_argument("--batch-kmax", type=int, default=28, help="batched: largest k (k uniform 8..kmax)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.batch_count < 1 or not 8 <= args.batch_kmax <= 32:
+        ap.error("--batch-count must be >= 1 and --batch-kmax in 8..32")
+    return args
 
 
 def dist_env():
@@ -75,6 +81,28 @@ def flops_plain(n: int) -> float:
 
 
 # ------------------------------------------------------------ CPU baseline
+def workload_desc(args) -> str:
+    """The workload line of `config`, the same for both arms."""
+    n = args.n
+    if args.workload == "repeated":
+        return ("repeated permanent: 60-mode Haar, one photon in modes 0-29, output occupation "
+                "from a seeded multinomial (multiplicities <= 4)")
+    if args.workload == "batched":
+        return (f"{args.batch_count} uneven k x k permanents, k uniform 8..{args.batch_kmax}, rows/cols drawn "
+                "with repetition from a seeded 100-mode Haar unitary; one persistent launch per step")
+    if args.workload == "grad":
+        n = min(n, 32)
+        return (f"permanent and full {n}x{n} complex gradient of the top-left block of a seeded "
+                f"Haar {2 * n}x{2 * n} unitary, one sweep")
+    if args.workload == "pmf":
+        return ("boson-sampling pmf layer: 60-mode Haar, one input photon in modes 0-29, a seeded "
+                "uniform-multinomial sample of 29 photons; 30 leave-one-out permanents per layer")
+    if args.workload == "mesh":
+        return ("512 terms log|perm(U_S)|^2, 12 photons in a 40-mode Clements mesh (seeded uniform "
+                "phases, seeded mode sets), forward + backward to the 1560 phases")
+    return f"plain permanent, top-left {n}x{n} block of a seeded Haar {2 * n}x{2 * n} unitary"
+
+
 def cpu_sample_rate(A: np.ndarray, seconds: float, threads: int = 0):
     """Gray steps/s of the oracle on all host cores, on a bounded contiguous
     sample of the permanent's Gray range (calibrated to ~`seconds`)."""
@@ -228,8 +256,7 @@ def run_reference(args, rank, world):
         "metric": METRIC, "value": perm_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"plain permanent, top-left {n}x{n} block of a seeded Haar {2 * n}x{2 * n} unitary",
-                   "n": n, "seed": args.seed},
+        "config": {"workload": workload_desc(args), "n": n, "seed": args.seed},
         "cpu_baseline": {"value": perm_s, "unit": UNIT, "cores": thr, "kind": "port",
                          "sample": f"per step a contiguous sample of ~{int(statistics.mean(spans))} of the "
                                    f"2^{n - 1} Gray steps (reference BBFG double algorithm, C restatement, "
@@ -370,8 +397,7 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"plain permanent, top-left {n}x{n} block of a seeded Haar {2 * n}x{2 * n} unitary",
-                   "n": n, "arith": args.mode, "seed": args.seed, "l2": "flushed (256 MiB write) between steps",
+        "config": {"workload": workload_desc(args), "n": n, "arith": args.mode, "seed": args.seed, "l2": "flushed (256 MiB write) between steps",
                    "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -493,8 +519,7 @@ def _repeated(args, rank, world, torch):
                          f"algorithm as the C oracle, {os.cpu_count()} threads)"}
     if rank == 0:
         _line(args, world, value, "perm/s", 1000 * wall / args.steps,
-              {"workload": "repeated permanent: 60-mode Haar, one photon in modes 0-29, output occupation "
-                           "from a seeded multinomial (multiplicities <= 4)", "arith": mode,
+              {"workload": workload_desc(args), "arith": mode,
                "l2": "inputs < 100 KB; compute-bound, no flush"},
               _roof(flops / args.steps, statistics.mean(kms), peak,
                     "repeated_df_kernel" if mode == "fast" else "repeated_kernel"),
@@ -509,8 +534,8 @@ def _batched(args, rank, world, torch):
     from piquassoboost_gb300.workloads import batched_instances, haar_block, repeated_instance
 
     mode = args.mode
-    count = 4096
-    mats = batched_instances(count, seed=4 + 1000 * rank, modes=100, kmin=8, kmax=28)
+    count, kmax = args.batch_count, args.batch_kmax
+    mats = batched_instances(count, seed=4 + 1000 * rank, modes=100, kmin=8, kmax=kmax)
     ks = np.array([m.shape[0] for m in mats])
     flops = float(np.sum(8.0 * ks * 2.0 ** (ks - 1)))
     peak = nat.probe_peak("fp64")
@@ -553,7 +578,7 @@ def _batched(args, rank, world, torch):
     e2e = world * count * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
     # sequential plain-GPU launches on the same device-resident inputs
     dm = [torch.from_numpy(m).to("cuda") for m in mats]
-    ws_b = int(lib.gbperm_perm_workspace_size(28, 28))
+    ws_b = int(lib.gbperm_perm_workspace_size(kmax, kmax))
     ws = torch.empty(ws_b, dtype=torch.uint8, device="cuda")
     sout = torch.zeros(2 * count, dtype=torch.float64, device="cuda")
     e0 = torch.cuda.Event(enable_timing=True)
@@ -589,13 +614,12 @@ def _batched(args, rank, world, torch):
                          f"double algorithm as the C oracle, scaled to the whole batch"}
     if rank == 0:
         _line(args, world, value, "perm/s", 1000 * wall / args.steps,
-              {"workload": "4096 uneven k x k permanents, k uniform 8..28, rows/cols drawn with repetition "
-                           "from a seeded 100-mode Haar unitary; one persistent launch per step", "arith": mode,
+              {"workload": workload_desc(args), "arith": mode,
                "item_log2": plan.item_log2(), "lanes_per_segment": plan.shape()[0],
                "autotune": {"default_shape": list(default_shape), "default_item_log2": default_item,
                             "chosen_shape": list(plan.shape()), "chosen_item_log2": plan.item_log2(),
                             "best_ms": tuned_ms, "tuning_s": t_tune},
-               "l2": "inputs 26 MB stay resident; compute-bound"},
+               "l2": f"inputs {packed.nbytes / 1e6:.3g} MB stay resident; compute-bound"},
               _roof(flops, statistics.mean(kms), peak, "batched_kernel"),
               cpu, {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": int(packed.nbytes),
                     "d2h_bytes_per_step": 16 * count},
@@ -655,8 +679,7 @@ def _grad(args, rank, world, torch):
     e2e = world * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
     if rank == 0:
         _line(args, world, world * args.steps / wall, "(perm+grad)/s", 1000 * wall / args.steps,
-              {"workload": f"permanent and full {n}x{n} complex gradient of the top-left block of a seeded "
-                           f"Haar {2 * n}x{2 * n} unitary, one sweep", "n": n, "arith": "fast"},
+              {"workload": workload_desc(args), "n": n, "arith": "fast"},
               _roof(flops, statistics.mean(gms), peak, "grad_kernel (forward flops only)"),
               None, {"value": e2e, "unit": "(perm+grad)/s", "h2d_bytes_per_step": n * n * 16,
                      "d2h_bytes_per_step": n * n * 16 + 16}, 5 * args.steps,
@@ -709,9 +732,7 @@ def _pmf(args, rank, world, torch):
                          f"per occupied input mode as in the reference, C oracle, {os.cpu_count()} threads"}
     if rank == 0:
         _line(args, world, value, "layers/s", 1000 * wall / args.steps,
-              {"workload": "boson-sampling pmf layer: 60-mode Haar, one input photon in modes 0-29, a seeded "
-                           "uniform-multinomial sample of 29 photons; 30 leave-one-out permanents per layer",
-               "arith": args.mode, "l2": "inputs < 100 KB; compute-bound, no flush"},
+              {"workload": workload_desc(args), "arith": args.mode, "l2": "inputs < 100 KB; compute-bound, no flush"},
               _roof(flops / args.steps, statistics.mean(kms), peak,
                     "pmf_df_kernel (FP64-equivalent flops of the FP64 form)" if args.mode == "fast"
                     else "pmf_kernel (executed FP64 flops)"),
@@ -856,8 +877,7 @@ def _mesh(args, rank, world, torch):
                          f"term on {os.cpu_count()} threads), scaled to the whole batch; the mesh itself not counted"}
     if rank == 0:
         _line(args, world, value, "(loss+grad)/s", 1000 * wall / args.steps,
-              {"workload": "512 terms log|perm(U_S)|^2, 12 photons in a 40-mode Clements mesh (seeded uniform "
-                           "phases, seeded mode sets), forward + backward to the 1560 phases", "arith": "fast",
+              {"workload": workload_desc(args), "arith": "fast",
                "launch": "forward + backward captured once as a CUDA graph, one replay per step (checked equal "
                          "to the eager step); eager timing in eager_step_ms",
                "l2": "inputs < 1 MB; launch- and compute-bound, no flush"},
@@ -885,10 +905,11 @@ def _reference_secondary(args, world):
         v = args.steps / sum(ts)
         unit, sample = "perm/s", "full permanents of one 60-mode / 30-photon instance"
     elif args.workload == "batched":
-        mats = batched_instances(4096, seed=4, modes=100, kmin=8, kmax=28)
+        count = args.batch_count
+        mats = batched_instances(count, seed=4, modes=100, kmin=8, kmax=args.batch_kmax)
         ks = np.array([m.shape[0] for m in mats])
         flops = float(np.sum(8.0 * ks * 2.0 ** (ks - 1)))
-        order = np.argsort(-ks)[::256]
+        order = np.argsort(-ks)[::max(1, count // 16)]
         ts, fl = [], []
         for _ in range(args.steps):
             t = time.perf_counter()
@@ -898,8 +919,9 @@ def _reference_secondary(args, world):
                 f += 8.0 * ks[i] * 2.0 ** (ks[i] - 1)
             ts.append(time.perf_counter() - t)
             fl.append(f)
-        v = 4096 / (sum(ts) / len(ts) * flops / fl[0])
-        unit, sample = "perm/s", "16 size-stratified instances per step, scaled to the 4096-instance batch"
+        v = count / (sum(ts) / len(ts) * flops / fl[0])
+        unit, sample = "perm/s", (f"{len(order)} size-stratified instances per step, scaled to the "
+                                  f"{count}-instance batch")
     elif args.workload == "mesh":
         from concurrent.futures import ThreadPoolExecutor
 
@@ -948,7 +970,7 @@ def _reference_secondary(args, world):
             ts.append(time.perf_counter() - t)
         v = args.steps / sum(ts) / 2.0 ** (n - 24) / n
         unit, sample = "(perm+grad)/s", "forward-only 24x24 oracle time scaled by 2^(n-24) and n minors"
-    _line(args, world, v, unit, 1000.0 / v if v else None, {"workload": args.workload}, None,
+    _line(args, world, v, unit, 1000.0 / v if v else None, {"workload": workload_desc(args)}, None,
           {"value": v, "unit": unit, "cores": os.cpu_count(), "kind": "port", "sample": sample},
           {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}, 0)
     return 0
