@@ -623,7 +623,9 @@ def _batched(args, rank, world, torch):
               _roof(flops, statistics.mean(kms), peak, "batched_kernel"),
               cpu, {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": int(packed.nbytes),
                     "d2h_bytes_per_step": 16 * count},
-              3 * args.steps,
+              # per step: prepare, worker, finalize, the FP64 redo worker and its
+              # finalize (double-float plans), the slot-order scatter
+              (6 if mode == "fast" else 4) * args.steps,
               {"sequential_plain_gpu": {"ms": seq_ms, "perm_per_s": count / (seq_ms * 1e-3),
                                         "batched_speedup": seq_ms / statistics.mean(kms),
                                         "max_rel_diff_vs_batched": diff}}, clocks=clocks)
