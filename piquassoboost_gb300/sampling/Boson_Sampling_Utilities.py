@@ -17,6 +17,12 @@ without MPFR or FPGA support fail the same way the reference does ("Wrong
 value set for permanent library.").  Two ids are added: 20 (GB300 FP64) and
 21 (GB300 fast: FP32-pipe double-float product).
 
+Every class also takes a keyword-only ``backend``: None (default) keeps the
+arithmetic of its library id, "fp64" selects the FP64 product and "fast" the
+double-float product (whose results above a 1e-10 error estimate are
+recomputed in FP64 on the device).  The reference has no such argument; an
+unknown value raises ValueError.
+
 Deliberate deviations: arrays are converted to complex128 / int64 (the
 reference reinterprets a C-contiguous array's memory whatever its dtype), and
 states longer than the matrix raise instead of reading past it.
@@ -36,9 +42,17 @@ PLAIN_LIBS = {0: "fp64", 6: "fp64", 7: "fp64", 8: "fp64", 10: "fp64", 11: "fp64"
 # repeated ids served on the GPU (lib 9 constructs but cannot calculate)
 REPEATED_LIBS = {0: "fp64", 1: "fp64", 6: "fp64", 7: "fp64", 8: "fp64", 20: "fp64", 21: "fast"}
 REPEATED_CONSTRUCT_ONLY = {9}
+BACKENDS = ("fp64", "fast")
+
 # lib 0 (ChinHuhPermanentCalculator) evaluates the Chin-Huh form of the sum
 # (CChinHuhPermanentCalculator.cpp:48-201) on the same kernels
 REPEATED_FORM = {0: "chinhuh"}
+
+
+def _check_backend(backend):
+    if backend is not None and backend not in BACKENDS:
+        raise ValueError(f"unknown backend {backend!r}: expected None, 'fp64' or 'fast'")
+    return backend
 
 
 def _coerce_matrix(m):
@@ -51,12 +65,13 @@ def _coerce_matrix(m):
 class GlynnPermanentCalculator_wrapper:
     """Plain permanent calculator (the reference's CPython type of that name)."""
 
-    def __init__(self, matrix=None, lib: int = 7):
+    def __init__(self, matrix=None, lib: int = 7, *, backend=None):
         if matrix is None:
             raise TypeError("GlynnPermanentCalculator_wrapper: matrix is required")
         if lib not in PLAIN_LIBS:
             raise Exception(WRONG_LIB)
         self.lib = int(lib)
+        self.backend = _check_backend(backend)
         self._matrix = _coerce_matrix(matrix)
 
     @property
@@ -68,7 +83,7 @@ class GlynnPermanentCalculator_wrapper:
         self._matrix = _coerce_matrix(value)
 
     def calculate(self):
-        mode = PLAIN_LIBS[self.lib]
+        mode = self.backend or PLAIN_LIBS[self.lib]
         if isinstance(self._matrix, list):
             return nat.perm_batched([nat.as_matrix(m) for m in self._matrix], mode=mode)
         if self.lib in (10, 11):
@@ -83,12 +98,13 @@ class ChinHuhPermanentCalculator_wrapper:
     """Repeated-multiplicity calculator (the reference's CPython type of that
     name, which dispatches on ``lib``)."""
 
-    def __init__(self, lib: int = 7, matrix=None, input_state=None, output_state=None):
+    def __init__(self, lib: int = 7, matrix=None, input_state=None, output_state=None, *, backend=None):
         if matrix is None or input_state is None or output_state is None:
             raise TypeError("ChinHuhPermanentCalculator_wrapper: matrix, input_state and output_state are required")
         if lib not in REPEATED_LIBS and lib not in REPEATED_CONSTRUCT_ONLY:
             raise Exception(WRONG_LIB)
         self.lib = int(lib)
+        self.backend = _check_backend(backend)
         self._matrix = _coerce_matrix(matrix)
         self.input_state = input_state
         self.output_state = output_state
@@ -104,7 +120,7 @@ class ChinHuhPermanentCalculator_wrapper:
     def calculate(self):
         if self.lib not in REPEATED_LIBS:
             raise Exception(WRONG_LIB)
-        mode = REPEATED_LIBS[self.lib]
+        mode = self.backend or REPEATED_LIBS[self.lib]
         ins, outs = self.input_state, self.output_state
         if isinstance(ins, list) and isinstance(outs, list):
             # ChinHuhPermanentCalculator_Wrapper.hpp:233-323
@@ -136,7 +152,7 @@ class RepeatedPermanentCalculator(ChinHuhPermanentCalculator_wrapper):
     instance (Boson_Sampling_Utilities.py:30-78): states that are neither numpy
     arrays nor lists are converted to int64 arrays; lists must hold arrays."""
 
-    def __init__(self, lib, matrix, input_state, output_state):
+    def __init__(self, lib, matrix, input_state, output_state, *, backend=None):
         if not isinstance(input_state, np.ndarray):
             if not isinstance(input_state, list):
                 input_state = np.array(input_state, dtype=np.int64)
@@ -151,133 +167,134 @@ class RepeatedPermanentCalculator(ChinHuhPermanentCalculator_wrapper):
                 for item in output_state:
                     if not isinstance(item, np.ndarray):
                         raise Exception('The output state should be a numpy array, or a list of numpy arrays')
-        super().__init__(lib=lib, matrix=matrix, input_state=input_state, output_state=output_state)
+        super().__init__(lib=lib, matrix=matrix, input_state=input_state, output_state=output_state,
+                         backend=backend)
 
     def calculate(self):
         return super().calculate()
 
 
 class ChinHuhPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(0, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(0, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(1, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(1, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedInfPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(9, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(9, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedSingleDFEPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(2, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(2, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedDualDFEPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(3, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(3, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedMultiSingleDFEPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(4, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(4, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedMultiDualDFEPermanentCalculator(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(5, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(5, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnRepeatedPermanentCalculatorDouble(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(6, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(6, matrix, input_state, output_state, backend=backend)
 
 
 class BBFGRepeatedPermanentCalculatorDouble(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(7, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(7, matrix, input_state, output_state, backend=backend)
 
 
 class BBFGRepeatedPermanentCalculatorLongDouble(RepeatedPermanentCalculator):
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(8, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(8, matrix, input_state, output_state, backend=backend)
 
 
 class GB300RepeatedPermanentCalculator(RepeatedPermanentCalculator):
     """New id 20: GB300 FP64 product (exact integer column sums)."""
 
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(20, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(20, matrix, input_state, output_state, backend=backend)
 
 
 class GB300FastRepeatedPermanentCalculator(RepeatedPermanentCalculator):
     """New id 21: GB300 FP32-pipe double-float product."""
 
-    def __init__(self, matrix, input_state, output_state):
-        super().__init__(21, matrix, input_state, output_state)
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(21, matrix, input_state, output_state, backend=backend)
 
 
 class GlynnPermanent(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 0)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 0, backend=backend)
 
 
 class GlynnPermanentInf(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 1)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 1, backend=backend)
 
 
 class GlynnPermanentSingleDFE(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 2)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 2, backend=backend)
 
 
 class GlynnPermanentDualDFE(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 3)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 3, backend=backend)
 
 
 class GlynnPermanentDouble(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 6)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 6, backend=backend)
 
 
 class BBFGPermanentDouble(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 7)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 7, backend=backend)
 
 
 class BBFGPermanentLongDouble(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 8)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 8, backend=backend)
 
 
 class GlynnPermanentSimpleDouble(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 10)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 10, backend=backend)
 
 
 class GlynnPermanentSimpleLongDouble(GlynnPermanentCalculator_wrapper):
-    def __init__(self, matrix):
-        super().__init__(matrix, 11)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 11, backend=backend)
 
 
 class GB300Permanent(GlynnPermanentCalculator_wrapper):
     """New id 20: GB300 FP64 product (exact integer column sums)."""
 
-    def __init__(self, matrix):
-        super().__init__(matrix, 20)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 20, backend=backend)
 
 
 class GB300FastPermanent(GlynnPermanentCalculator_wrapper):
     """New id 21: GB300 FP32-pipe double-float product."""
 
-    def __init__(self, matrix):
-        super().__init__(matrix, 21)
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 21, backend=backend)
 
 
 __all__: List[str] = [n for n in dir() if n[0].isupper()]

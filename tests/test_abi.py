@@ -119,6 +119,32 @@ def test_dropin_lib_ids_and_messages():
         bsu.BBFGRepeatedPermanentCalculatorDouble(A, [1, 1, 1], (1, 1, 1))
 
 
+def test_dropin_backend_keyword():
+    from piquassoboost_gb300.sampling import Boson_Sampling_Utilities as bsu
+
+    A = np.eye(3)
+    assert bsu.BBFGPermanentDouble(A).backend is None
+    assert bsu.GlynnPermanent(A, backend="fast").backend == "fast"
+    assert bsu.GB300FastRepeatedPermanentCalculator(A, (1, 1, 1), (1, 1, 1), backend="fp64").backend == "fp64"
+    assert bsu.ChinHuhPermanentCalculator_wrapper(7, A, np.ones(3, np.int64), np.ones(3, np.int64),
+                                                  backend="fast").backend == "fast"
+    for bad in ("cpu", "FP64", 1):
+        with pytest.raises(ValueError, match="unknown backend"):
+            bsu.BBFGPermanentDouble(A, backend=bad)
+        with pytest.raises(ValueError, match="unknown backend"):
+            bsu.BBFGRepeatedPermanentCalculatorDouble(A, (1, 1, 1), (1, 1, 1), backend=bad)
+    # the library id is still checked first, with the reference's message
+    with pytest.raises(Exception, match="Wrong value set for permanent library."):
+        bsu.GlynnPermanentInf(A, backend="fast")
+    # keyword only: a third positional argument is not taken as the backend
+    with pytest.raises(TypeError):
+        bsu.BBFGPermanentDouble(A, "fast")
+    # trivial shapes are answered without a device under either arithmetic
+    assert bsu.BBFGPermanentDouble(np.zeros((0, 0)), backend="fast").calculate() == 1
+    assert bsu.GB300Permanent(np.ones((5, 3)), backend="fast").calculate() == 0
+    assert bsu.BBFGRepeatedPermanentCalculatorDouble(A, (0, 0, 0), (0, 0, 0), backend="fast").calculate() == 1
+
+
 def test_dropin_state_coercion_and_lists():
     from piquassoboost_gb300.sampling import Boson_Sampling_Utilities as bsu
 

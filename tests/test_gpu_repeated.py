@@ -136,6 +136,22 @@ def test_repeated_list_branch_uses_batch():
         assert abs(v - ref) <= TOL * abs(ref)
 
 
+def test_dropin_backend_keyword_selects_the_arithmetic():
+    from piquassoboost_gb300.sampling import Boson_Sampling_Utilities as bsu
+    U = haar_unitary(10, 6)
+    cin = np.array([1, 1, 0, 2, 0, 1, 0, 0, 1, 0])
+    rout = np.array([0, 2, 1, 0, 1, 0, 1, 1, 0, 0])
+    # the keyword gives the same call as the library id of that arithmetic (both deterministic)
+    assert bsu.BBFGRepeatedPermanentCalculatorDouble(U, cin, rout, backend="fast").calculate() == \
+        bsu.GB300FastRepeatedPermanentCalculator(U, cin, rout).calculate()
+    assert bsu.GB300FastRepeatedPermanentCalculator(U, cin, rout, backend="fp64").calculate() == \
+        nat.perm_repeated(U, cin, rout, mode="fp64")
+    A = U[:7, :7]
+    assert bsu.BBFGPermanentDouble(A, backend="fast").calculate() == bsu.GB300FastPermanent(A).calculate()
+    ref, _ = orc.bbfg(A, prec=1)
+    assert abs(bsu.GlynnPermanent(A, backend="fast").calculate() - ref) <= TOL * abs(ref)
+
+
 @pytest.mark.parametrize("mode", ["fp64", "fast"])
 def test_chinhuh_form_vs_reference_build(mode):
     import json
