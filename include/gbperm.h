@@ -76,7 +76,11 @@ int gbperm_device_count(void);
  *   "plain.seg_log2"      force log2 segment length of the plain kernel (-1 = auto)
  *   "plain.grid"          force the plain grid size (0 = auto)
  *   "repeated.low_digits" force the digits handled inside a repeated segment (-1 = auto)
- *   "batched.threads"     force threads per instance of the batched kernel (0 = autotuned)
+ *   "batched.threads"     lanes sharing one Gray segment in a double-float batch plan
+ *                         (2 or 4; 0 = 2), read when a plan is created; the autotuner
+ *                         tries both
+ *   "batched.item_log2"   force the log2 work-item target of new batch plans (0 = by
+ *                         the batch's total work)
  *   "plain.df_group"      lanes sharing one Gray segment in the double-float kernel
  *                         (1, 2, 4 or 8; 0 = by column count)
  *   "df.escalate"         1 (default): a double-float result whose error estimate exceeds
