@@ -103,30 +103,35 @@ def workload_desc(args) -> str:
     return f"plain permanent, top-left {n}x{n} block of a seeded Haar {2 * n}x{2 * n} unitary"
 
 
-def cpu_sample_rate(A: np.ndarray, seconds: float, threads: int = 0):
+def cpu_sample_rate(A: np.ndarray, seconds: float, threads: int = 0, prec: int = 0):
     """Gray steps/s of the oracle on all host cores, on a bounded contiguous
-    sample of the permanent's Gray range (calibrated to ~`seconds`)."""
+    sample of the permanent's Gray range (calibrated to ~`seconds`).
+    prec 0: double (the reference's lib 7); 1: binary128 (its lib 8 on
+    AArch64, where long double is binary128)."""
     from tests import oracle_bind as orc
 
     lib = orc.lib()
     P = ctypes.c_void_p
-    lib.orc_bbfg_range.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
-                                   ctypes.c_uint64, ctypes.c_uint64, P]
+    fn = lib.orc_bbfg_range_prec
+    fn.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_uint64, ctypes.c_uint64, P]
     a = np.ascontiguousarray(A, dtype=np.complex128)
     n = a.shape[0]
     total = 1 << (n - 1)
     out = np.zeros(4)
     # calibrate on a small sample, then run the measured sample
-    span = min(total, 1 << 22)
+    span = min(total, 1 << (22 if prec == 0 else 16))
     t0 = time.perf_counter()
-    lib.orc_bbfg_range(a.ctypes.data_as(P), n, n, n, threads, 0, span, out.ctypes.data_as(P))
+    rc = fn(a.ctypes.data_as(P), n, n, n, prec, threads, 0, span, out.ctypes.data_as(P))
     dt = time.perf_counter() - t0
     rate = span / max(dt, 1e-9)
-    span = int(min(total, max(1 << 20, rate * seconds)))
+    span = int(min(total, max(1 << (20 if prec == 0 else 14), rate * seconds)))
     start = (total - span) // 2
     t0 = time.perf_counter()
-    lib.orc_bbfg_range(a.ctypes.data_as(P), n, n, n, threads, start, start + span, out.ctypes.data_as(P))
+    rc |= fn(a.ctypes.data_as(P), n, n, n, prec, threads, start, start + span, out.ctypes.data_as(P))
     dt = time.perf_counter() - t0
+    if rc != 0:
+        raise RuntimeError("orc_bbfg_range_prec failed")
     return span / dt, span, dt
 
 
@@ -392,6 +397,13 @@ def run_ours(args, rank, world, local):
                "sample": f"{span} contiguous Gray steps of the same {n}x{n} permanent ({dt:.1f} s, "
                          f"{thr} threads, reference BBFG double algorithm as the C oracle); "
                          f"perm/s = steps/s / 2^{n - 1}"}
+        # the reference's lib 8 ("long double", binary128 on this Arm host), a short sample
+        try:
+            rate8, span8, dt8 = cpu_sample_rate(mats[args.warmup], min(3.0, args.cpu_seconds / 4), thr, prec=1)
+            cpu["lib8_long_double"] = {"value": rate8 / 2.0 ** (n - 1), "unit": UNIT,
+                                       "sample": f"{span8} Gray steps in binary128 ({dt8:.1f} s, {thr} threads)"}
+        except Exception as exc:  # the lib 7 baseline above stands on its own
+            cpu["lib8_long_double"] = {"value": None, "error": str(exc)[:200]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

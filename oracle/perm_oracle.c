@@ -216,29 +216,48 @@ int orc_bbfg(const double* A, int64_t rows, int64_t cols, int64_t ld, int prec, 
 
 /* Partial plain BBFG sum over the Gray indices [idx_begin, idx_end) (no
  * 2^-(rows-1) normalisation), with the same 4 x threads segmentation.  Used
- * to time a bounded sample of a large permanent. */
-int orc_bbfg_range(const double* A, int64_t rows, int64_t cols, int64_t ld, int nthreads,
-                   uint64_t idx_begin, uint64_t idx_end, double* out) {
+ * to time a bounded sample of a large permanent.  prec: 0 double (lib 7),
+ * 1 binary128 (lib 8 where long double is binary128, as on AArch64). */
+int orc_bbfg_range_prec(const double* A, int64_t rows, int64_t cols, int64_t ld, int prec, int nthreads,
+                        uint64_t idx_begin, uint64_t idx_end, double* out) {
     if (rows < 1 || cols < 1 || rows > 63) return set_err(3, "orc_bbfg_range: bad shape");
     if (idx_end > (1ULL << (rows - 1)) || idx_begin >= idx_end) return set_err(1, "orc_bbfg_range: bad range");
+    if (prec != 0 && prec != 1) return set_err(1, "orc_bbfg_range: prec must be 0 or 1");
     int nt = hw_threads(nthreads);
     job_t J;
     memset(&J, 0, sizeof(J));
-    J.kind = 0; J.prec = 0; J.A = A; J.rows = rows; J.cols = cols; J.ld = ld;
+    J.kind = 0; J.prec = prec; J.A = A; J.rows = rows; J.cols = cols; J.ld = ld;
     J.total = idx_end - idx_begin;
     J.base = idx_begin;
     int64_t conc = 4 * (int64_t)nt;
     J.njobs = conc < (int64_t)J.total ? conc : (int64_t)J.total;
-    cx_d *A1, *A2;
-    make_a12_d(A, rows, cols, ld, &A1, &A2);
-    J.A1 = A1; J.A2 = A2;
-    J.part_d = (cx_d*)calloc((size_t)J.njobs, sizeof(cx_d));
-    run_pool(&J, nt);
-    acc_t_d acc = {0, 0, 0, 0};
-    for (int64_t j = 0; j < J.njobs; ++j) acc_add_d(&acc, J.part_d[j]);
-    put_d(acc_get_d(&acc), out);
-    free(A1); free(A2); free(J.part_d);
+    if (prec == 0) {
+        cx_d *A1, *A2;
+        make_a12_d(A, rows, cols, ld, &A1, &A2);
+        J.A1 = A1; J.A2 = A2;
+        J.part_d = (cx_d*)calloc((size_t)J.njobs, sizeof(cx_d));
+        run_pool(&J, nt);
+        acc_t_d acc = {0, 0, 0, 0};
+        for (int64_t j = 0; j < J.njobs; ++j) acc_add_d(&acc, J.part_d[j]);
+        put_d(acc_get_d(&acc), out);
+        free(A1); free(A2); free(J.part_d);
+    } else {
+        cx_q *A1, *A2;
+        make_a12_q(A, rows, cols, ld, &A1, &A2);
+        J.A1 = A1; J.A2 = A2;
+        J.part_q = (cx_q*)calloc((size_t)J.njobs, sizeof(cx_q));
+        run_pool(&J, nt);
+        acc_t_q acc = {0, 0, 0, 0};
+        for (int64_t j = 0; j < J.njobs; ++j) acc_add_q(&acc, J.part_q[j]);
+        put_q(acc_get_q(&acc), out);
+        free(A1); free(A2); free(J.part_q);
+    }
     return 0;
+}
+
+int orc_bbfg_range(const double* A, int64_t rows, int64_t cols, int64_t ld, int nthreads,
+                   uint64_t idx_begin, uint64_t idx_end, double* out) {
+    return orc_bbfg_range_prec(A, rows, cols, ld, 0, nthreads, idx_begin, idx_end, out);
 }
 
 /* --------------------------------------------------------- repeated BBFG */
