@@ -3,8 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
  * calculators (piquassoboost, sampling/source/ permanent calculators), used by
- * the tests as the checker and by bench.py as the CPU baseline.  The product
- * library never links or calls it.
+ * the tests as the expected values and by bench.py as the CPU baseline.  The
+ * product library never links or calls it.
  *
  * Parity pin: tests/test_oracle.py checks every entry point against the golden
  * values of the reference's unittests/test_permanent.py:47-251 and against

@@ -1,6 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/perm_oracle.c) for the tests.
 
-Test infrastructure only: the oracle is the checker, never the thing tested.
+Test infrastructure only: the oracle gives the expected values, and is never
+the thing tested.
 Results come back as (value, dd) where dd = [re_hi, im_hi, re_lo, im_lo].
 """
 from __future__ import annotations
