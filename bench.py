@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=36)
     ap.add_argument("--batch-count", type=int, default=4096, help="batched: permanents per batch")
     ap.add_argument("--batch-kmax", type=int, default=28, help="batched: largest k (k uniform 8..kmax)")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="length of the CPU baseline sample, seconds")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.batch_count < 1 or not 8 <= args.batch_kmax <= 32:
