@@ -148,3 +148,31 @@ def test_oracle_chinhuh_vs_reference_build(i):
     for prec in (0, 1):
         v, _ = orc.chinhuh(A, case["input_state"], case["output_state"], prec=prec)
         assert _close(v, ref[0], 1e-10), (prec, v, ref[0])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_range_sums_add_up_to_the_permanent(prec):
+    """orc_bbfg_range_prec (the bench's CPU-baseline sampler) over a split of
+    the whole Gray range gives the full sum, in double and in binary128."""
+    import ctypes
+
+    lib = orc.lib()
+    P = ctypes.c_void_p
+    fn = lib.orc_bbfg_range_prec
+    fn.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_uint64, ctypes.c_uint64, P]
+    rng = np.random.default_rng(7)
+    n = 12
+    A = np.ascontiguousarray(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    total = 1 << (n - 1)
+    cuts = [0, 1, 333, 1024, total]
+    acc = 0j
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        out = np.zeros(4)
+        assert fn(A.ctypes.data_as(P), n, n, n, prec, 3, a, b, out.ctypes.data_as(P)) == 0
+        acc += complex(out[0] + out[2], out[1] + out[3])
+    ref, _ = orc.bbfg(A, prec=1)
+    assert abs(acc / total - ref) <= 1e-12 * abs(ref)
+    out = np.zeros(4)
+    assert fn(A.ctypes.data_as(P), n, n, n, 2, 1, 0, total, out.ctypes.data_as(P)) != 0  # bad prec
+    assert fn(A.ctypes.data_as(P), n, n, n, 0, 1, 5, 5, out.ctypes.data_as(P)) != 0  # empty range
