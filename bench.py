@@ -57,7 +57,13 @@ def parse():
                          "grad: permanent + full gradient; pmf: one 60-mode / 30-photon boson-sampling "
                          "probability layer; mesh: 512-term Clements-mesh log-likelihood, forward + backward")
     ap.add_argument("--n", type=int, default=36)
-    ap.add_argument("--mode", default="fast", choices=["fast", "fp64"])
+    ap.add_argument("--mode", default=None, choices=["fx", "fast", "fp64"],
+                    help="arithmetic of the product: fx (integer mantissas, at least FP64 accuracy; the "
+                         "plain default), fp64 (FP64 pipe; the default of the other workloads), fast "
+                         "(double-float on the FP32 pipe, recomputed in FP64 above its error bar)")
+    ap.add_argument("--check-steps", type=int, default=3,
+                    help="plain: timed matrices recomputed by the other two products for the accuracy "
+                         "check and their own rates")
     ap.add_argument("--seed", type=int, default=36)
     ap.add_argument("--batch-count", type=int, default=4096, help="batched: permanents per batch")
     ap.add_argument("--batch-kmax", type=int, default=28, help="batched: largest k (k uniform 8..kmax)")
@@ -66,6 +72,10 @@ def parse():
     args = ap.parse_args()
     if args.batch_count < 1 or not 8 <= args.batch_kmax <= 32:
         ap.error("--batch-count must be >= 1 and --batch-kmax in 8..32")
+    if args.mode is None:
+        args.mode = "fx" if args.workload == "plain" else "fp64"
+    if args.mode == "fx" and args.workload != "plain":
+        ap.error("--mode fx: the integer-mantissa product serves the plain workload")
     return args
 
 
@@ -273,6 +283,13 @@ def run_reference(args, rank, world):
 
 
 # ----------------------------------------------------------------- our arm
+def _imad_ops_plain(n: int) -> float:
+    """Algorithmic 32x32->64 multiply-adds of one plain permanent on the
+    integer-mantissa product: 12 per complex multiply, n - 1 multiplies per
+    Gray step, 2^(n-1) steps."""
+    return 12.0 * (n - 1) * 2.0 ** (n - 1)
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -303,13 +320,13 @@ def run_ours(args, rank, world, local):
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     d_out = torch.zeros(2, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
-    # prepare + permanent kernel (+ the FP64 twin of the double-float kernel,
-    # which returns at once unless the range check or the error estimate
-    # hands it the permanent)
-    launches_per_step = 3 if args.mode == "fast" else 2
+    # prepare + permanent kernel; the double-float kernel also queues its
+    # FP64 twin (it returns at once unless the range check or the error
+    # estimate hands it the permanent)
+    launches_per_step = {"fast": 3}.get(args.mode, 2)
 
-    def step(i):
-        rc = lib.gbperm_perm_dev(ctypes.c_void_p(d_mats[i].data_ptr()), n, n, n, arith,
+    def step(i, a=arith):
+        rc = lib.gbperm_perm_dev(ctypes.c_void_p(d_mats[i].data_ptr()), n, n, n, a,
                                  ctypes.c_void_p(d_out.data_ptr()), None, ctypes.c_void_p(ws.data_ptr()),
                                  ws_bytes, sptr)
         nat.check(rc)
@@ -317,7 +334,7 @@ def run_ours(args, rank, world, local):
     for i in range(args.warmup):
         step(i)
     torch.cuda.synchronize()
-    peaks = {"fp64_tflops": nat.probe_peak("fp64"), "fp32_tflops": nat.probe_peak("fp32")}
+    peaks = {k: nat.probe_peak(k) for k in ("fp64", "fp32", "imad_wide")}
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -340,21 +357,11 @@ def run_ours(args, rank, world, local):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     kern_ms = [a.elapsed_time(b) for a, b in ev]
+    got = [complex(r[0].item(), r[1].item()) for r in results]
     from piquassoboost_gb300.replicas import replica_throughput
 
     # replicas: every rank computed its own `steps` permanents
     value, t_max = replica_throughput(args.steps, wall, device=dev)
-
-    # correctness spot check of the timed results against the FP64 kernel
-    # (one FP64 permanent: ~10 s at n = 36; skipped for larger n); the error
-    # is stated relative to |perm| and to the product of the row 2-norms
-    check = None
-    check_rows = None
-    if n <= 36 and args.mode == "fast":
-        ref = nat.perm(mats[args.warmup], mode="fp64")
-        got = complex(results[0][0].item(), results[0][1].item())
-        check = abs(got - ref) / abs(ref)
-        check_rows = abs(got - ref) / float(np.prod(np.linalg.norm(mats[args.warmup], axis=1)))
 
     # e2e through the public host-buffer entry point, pinned input, every step
     pinned = [torch.from_numpy(m).pin_memory() for m in mats[args.warmup:]]
@@ -370,24 +377,83 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     e2e, _ = replica_throughput(args.steps, time.perf_counter() - t1, device=dev)
 
+    # the same first `check_steps` timed matrices through the other products:
+    # each one's own rate and roofline, and the headline results checked
+    # against the FP64 kernel (relative to |perm| and to the product of the
+    # row 2-norms); the double-float path runs as users get it, with its
+    # on-device recomputation in FP64 when its error estimate is above 1e-10
+    nchk = max(0, min(args.check_steps, args.steps))
+    idx = [args.warmup + k for k in range(nchk)]
+    flops = flops_plain(n)
+    products = {}
+    ref64 = {}
+    for mode in ("fp64", "fx", "fast"):
+        if mode == args.mode and mode != "fp64":
+            continue
+        st = nat.Stats()
+        ms, vals, esc, ests = [], [], 0, []
+        for i in idx:
+            v = nat.perm(mats[i], mode=mode, stats=st)
+            ms.append(st.kernel_ms)
+            vals.append(v)
+            if mode == "fast":
+                ests.append(st.err_est)
+                esc += int(st.arith == nat.ARITH_FP64)
+        if mode == "fp64":
+            ref64 = dict(zip(idx, vals))
+            if args.mode == "fp64":
+                continue
+        if not ms:
+            continue
+        d = {"kernel_ms": ms, "perm_per_s": len(ms) / (sum(ms) * 1e-3),
+             "fp64_equivalent_tflops": flops / (statistics.mean(ms) * 1e-3) / 1e12}
+        if mode == "fp64":
+            d.update({"dtype": "f64", "kernel": "plain_kernel",
+                      "frac_of_fp64_peak": d["fp64_equivalent_tflops"] / peaks["fp64"]})
+        elif mode == "fx":
+            d.update({"dtype": "int64 mantissas (>= f64 accuracy)", "kernel": "plain_fx_kernel"})
+        else:
+            d.update({"dtype": "f32 pairs (double-float product)", "kernel": "plain_df_kernel",
+                      "escalated_steps": esc, "err_est": ests,
+                      "note": "an escalated step reruns the permanent on the FP64 kernel: kernel_ms includes "
+                              "the double-float pass it discards"})
+        products[mode] = d
+        if mode != "fp64":
+            products[mode]["rel_err_vs_fp64_kernel"] = [abs(v - ref64[i]) / abs(ref64[i]) for i, v in zip(idx, vals)]
+
+    check = {}
+    if ref64 and args.mode != "fp64":
+        rel = [abs(got[k] - ref64[i]) / abs(ref64[i]) for k, i in enumerate(idx)]
+        rown = [abs(got[k] - ref64[i]) / float(np.prod(np.linalg.norm(mats[i], axis=1))) for k, i in enumerate(idx)]
+        check = {"timed_results_checked": nchk, "rel_err_vs_fp64_kernel": rel, "max_rel_err": max(rel),
+                 "err_by_row_norm_product": rown}
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return 0
 
     avg_ms = statistics.mean(kern_ms)
-    achieved = flops_plain(n) / (avg_ms * 1e-3) / 1e12
-    roof = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / peaks["fp64_tflops"], "traffic": traffic_from_profile(n, args.mode),
-            "kernel": ("plain_df_kernel" if args.mode == "fast" else "plain_kernel"),
-            "work_per_launch": f"8 n 2^(n-1) = {flops_plain(n):.4g} algorithmic FP64-equivalent flops",
-            "peak_source": "measured live by gbperm_probe_peak (DFMA probe), this run"}
-    if args.mode == "fast":
-        roof["note"] = ("double-float product on the FP32 pipe: frac is against the FP64 FMA peak "
-                        "(the FP64 roofline the target is stated against); the FP32 FMA peak measured "
-                        "in the same run is "
-                        f"{peaks['fp32_tflops']:.1f} TFLOP/s")
-        roof["fp32_peak_tflops"] = peaks["fp32_tflops"]
+    ach_flops = flops / (avg_ms * 1e-3) / 1e12
+    if args.mode == "fx":
+        ach = _imad_ops_plain(n) / (avg_ms * 1e-3) / 1e12
+        roof = {"bound": "int", "achieved": ach, "peak": peaks["imad_wide"], "unit": "Tops/s",
+                "frac": ach / peaks["imad_wide"], "traffic": traffic_from_profile(n, args.mode),
+                "kernel": "plain_fx_kernel",
+                "work_per_launch": f"12 (n-1) 2^(n-1) = {_imad_ops_plain(n):.4g} 32x32->64 multiply-adds "
+                                   f"(12 per complex multiply of 31-bit limbs)",
+                "peak_source": "mad.wide.s32 probe (gbperm_probe_peak kind 3), measured in this run",
+                "fp64_equivalent_tflops": ach_flops, "fp64_peak_tflops": peaks["fp64"],
+                "x_fp64_peak": ach_flops / peaks["fp64"]}
+    else:
+        roof = {"bound": "fp64", "achieved": ach_flops, "peak": peaks["fp64"], "unit": "TFLOP/s",
+                "frac": ach_flops / peaks["fp64"], "traffic": traffic_from_profile(n, args.mode),
+                "kernel": ("plain_df_kernel" if args.mode == "fast" else "plain_kernel"),
+                "work_per_launch": f"8 n 2^(n-1) = {flops:.4g} algorithmic FP64-equivalent flops",
+                "peak_source": "DFMA probe (gbperm_probe_peak kind 0), measured in this run"}
+        if args.mode == "fast":
+            roof["note"] = ("double-float product on the FP32 pipe: frac is FP64-equivalent flops against "
+                            f"the FP64 FMA peak; the FP32 FMA peak measured in this run is {peaks['fp32']:.1f} TFLOP/s")
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -405,20 +471,22 @@ def run_ours(args, rank, world, local):
         except Exception as exc:  # the lib 7 baseline above stands on its own
             cpu["lib8_long_double"] = {"value": None, "error": str(exc)[:200]}
 
+    dtype = {"fx": "int64", "fp64": "f64", "fast": "f32x2"}[args.mode]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_desc(args), "n": n, "arith": args.mode, "seed": args.seed, "l2": "flushed (256 MiB write) between steps",
-                   "parallelism": f"replicas x{world}"},
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "config": {"workload": workload_desc(args), "n": n, "arith": args.mode, "seed": args.seed,
+                   "l2": "flushed (256 MiB write) between steps", "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * n * 16, "d2h_bytes_per_step": 16},
         "clocks": clk,
         "gpu_launches": launches_per_step * args.steps,
         "kernel_ms": kern_ms,
-        "rel_err_vs_fp64_kernel": check,
-        "err_vs_fp64_by_row_norm_product": check_rows,
+        "accuracy": check,
+        "products": products,
+        "peaks": peaks,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

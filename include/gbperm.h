@@ -45,6 +45,11 @@ extern "C" {
 #define GBPERM_ARITH_DF32 1  /* double-float product on the FP32 pipe (~2^-46 per
                                 complex multiply); used for up to 48 columns when
                                 the matrix's dynamic range allows, else FP64 */
+#define GBPERM_ARITH_FX64 2  /* integer-mantissa product on the integer pipes: 64-bit
+                                mantissas in 31-bit limbs, 55-57 significant bits per
+                                complex multiply (the FP64 product keeps 53); any
+                                dynamic range, no FP64 fallback needed.  Plain
+                                permanents (gbperm_perm, gbperm_perm_dev) */
 
 /* Largest supported matrix side (columns of the product, rows of the Gray code). */
 #define GBPERM_MAX_DIM 64
@@ -259,15 +264,21 @@ int gbperm_mesh_unitary_backward_dev(const void* d_phases, int64_t m, const void
  * (256 KiB) that every GPU loading the library keeps until exit; sizes whose
  * scratch would not fit return GBPERM_ERR_TOO_LARGE.  The first call on a
  * device looks the array's device address up (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race, so serialise them. */
+ * device current; make that first call before any stream capture, and do
+ * not cudaDeviceReset() a device while the library is in use (the looked-up
+ * address would go stale).  Trivial shapes are written by a small kernel on
+ * the stream, without a host copy or a synchronisation.  All calls share
+ * the array: calls that overlap on the GPU race, so serialise them. */
 int gbperm_perm_noalloc(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
                         void* d_out_dd, void* stream);
 size_t gbperm_perm_noalloc_scratch_bytes(void);
 
 /* ------------------------------------------------------------- probes */
-/* Measured pipe peak of the current device in TFLOP/s (FMA = 2 flops):
- * kind 0 = FP64 FMA, kind 1 = FP32 FMA.  Runs ~0.1 s of probe kernels. */
+/* Measured pipe peak of the current device: kind 0 = FP64 FMA, kind 1 =
+ * FP32 FMA, kind 2 = FP64 tensor MMA (mma.sync m8n8k4), all in TFLOP/s
+ * (FMA = 2 flops); kind 3 = 32x32->64-bit integer multiply-add
+ * (mad.wide.s32), kind 4 = 32-bit integer multiply-add (mad.lo.s32), both
+ * in tera lane-operations/s.  Runs ~0.1 s of probe kernels. */
 int gbperm_probe_peak(int kind, double* tflops);
 
 #ifdef __cplusplus

@@ -24,7 +24,9 @@ GBPERM_ERR_NO_DEVICE = 6
 
 ARITH_FP64 = 0
 ARITH_DF32 = 1
-_MODES = {"fp64": ARITH_FP64, "fast": ARITH_DF32, "df32": ARITH_DF32}
+ARITH_FX64 = 2
+# "fx": integer-mantissa product (at least FP64 accuracy, integer pipes)
+_MODES = {"fp64": ARITH_FP64, "fast": ARITH_DF32, "df32": ARITH_DF32, "fx": ARITH_FX64}
 
 
 def arith_of(mode) -> int:
@@ -350,10 +352,15 @@ def compute_pmf(interferometer, sample, current_input, mode="fp64", stats: Stats
     return pmf, add
 
 
+_PROBES = {"fp64": 0, "fp32": 1, "dmma": 2, "imad_wide": 3, "imad": 4}
+
+
 def probe_peak(kind: str) -> float:
-    """Measured FP64 ("fp64") or FP32 ("fp32") FMA peak in TFLOP/s."""
+    """Measured pipe peak: "fp64" / "fp32" FMA and "dmma" (FP64 tensor MMA)
+    in TFLOP/s; "imad_wide" (mad.wide.s32) and "imad" (mad.lo.s32) in tera
+    lane-operations/s."""
     v = ctypes.c_double()
-    check(load().gbperm_probe_peak({"fp64": 0, "fp32": 1}[kind], ctypes.byref(v)))
+    check(load().gbperm_probe_peak(_PROBES[kind], ctypes.byref(v)))
     return v.value
 
 

@@ -156,14 +156,22 @@ static void plain_geometry(int rows, int grid_full, int seg_threads, int* grid, 
     *seg_log2 = l;
 }
 
-PlainPlan plan_plain(int rows, int cols, bool df) {
+PlainPlan plan_plain(int rows, int cols, int arith) {
     PlainPlan p;
-    p.df = df;
+    p.df = arith == GBPERM_ARITH_DF32;
+    p.fx = arith == GBPERM_ARITH_FX64;
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = device_sms(dev);
+    if (p.fx) {
+        // the integer-mantissa kernel runs alone: no FP64 twin to plan
+        fx_shape(cols, &p.cpl_fx, &p.grp_fx);
+        plain_geometry(rows, sms * plain_fx_blocks_per_sm(rows, p.cpl_fx, p.grp_fx), p.grp_fx, &p.grid_fx,
+                       &p.seg_log2_fx);
+        return p;
+    }
     plain_geometry(rows, sms * plain_blocks_per_sm(rows, cols), 1, &p.grid, &p.seg_log2);
-    if (df) {
+    if (p.df) {
         df_shape(cols, (int)g_opt.plain_df_group.load(), &p.cpl, &p.grp);
         plain_geometry(rows, sms * plain_df_blocks_per_sm(rows, p.cpl, p.grp), p.grp, &p.grid_df, &p.seg_log2_df);
     }
@@ -212,6 +220,16 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     pa.exp_fp64_out = pa.exp_out + 1;
     cudaError_t e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
+    if (plan.fx) {
+        e = launch_plain_fx(pa.a1, pa.a2, pa.exp_out, rows, cols, plan.cpl_fx, plan.grp_fx, plan.grid_fx,
+                            plan.seg_log2_fx, base + w.kern, d_out2, d_out4, st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain fx launch");
+        if (d_err) {
+            e = cudaMemsetAsync(d_err, 0, sizeof(double), st);
+            if (e != cudaSuccess) return cuda_fail(e, "plain fx error slot");
+        }
+        return GBPERM_OK;
+    }
     if (plan.df) {
         // the double-float kernel returns at once if the device range check
         // failed; its FP64 twin below returns at once unless that check
@@ -280,14 +298,16 @@ int64_t gbperm_get_option(const char* key) {
 
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols) {
     if (rows <= 0 || cols <= 0 || rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM) return 256;
-    // the larger of the two arithmetics' needs (grids may differ)
-    PlainPlan plan = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols);
-    return plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
+    // the largest of the arithmetics' needs (grids may differ)
+    PlainPlan plan = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
+    PlainPlan pfx = plan_plain((int)rows, (int)cols, GBPERM_ARITH_FX64);
+    const int g = plan.max_grid() > pfx.max_grid() ? plan.max_grid() : pfx.max_grid();
+    return plain_ws_layout((int)rows, (int)cols, g, nullptr);
 }
 
 int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
                     void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream) {
-    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: unknown arithmetic");
     if (rows < 0 || cols < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: negative shape");
     if (!d_out) return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: null output");
@@ -308,7 +328,8 @@ int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int 
         return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_dev: matrix larger than 64 x 64");
     if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: workspace must be 256-byte aligned");
-    PlainPlan plan = plan_plain((int)rows, (int)cols, arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols);
+    const int a = (arith == GBPERM_ARITH_DF32 && cols > kDfMaxCols) ? GBPERM_ARITH_FP64 : arith;
+    PlainPlan plan = plan_plain((int)rows, (int)cols, a);
     return run_plain_dev(static_cast<const double2*>(dA), ld, (int)rows, (int)cols, workspace,
                          workspace_bytes, static_cast<double*>(d_out), static_cast<double*>(d_out_dd), st,
                          plan);
@@ -329,13 +350,15 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         if (out_dd) out_dd[0] = out_dd[1] = out_dd[2] = out_dd[3] = NAN;
         return GBPERM_OK;
     }
-    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_perm: unknown arithmetic");
     bool df = false;
     int boost = 0;
     if (arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols)
         df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost, rows == cols);
-    PlainPlan plan = plan_plain((int)rows, (int)cols, df);
+    const bool fx = arith == GBPERM_ARITH_FX64;
+    PlainPlan plan = plan_plain((int)rows, (int)cols,
+                                fx ? GBPERM_ARITH_FX64 : (df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64));
     size_t mat_bytes = align_up((size_t)rows * cols * sizeof(double2), 256);
     size_t ws = plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
     ThreadCtx& c = thread_ctx();
@@ -367,13 +390,13 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         stats->steps = std::ldexp(1.0, (int)rows - 1);
         stats->flops = 8.0 * (double)cols * stats->steps;
         stats->launches = df ? 3 : 2;
-        stats->grid = df ? plan.grid_df : plan.grid;
-        stats->seg_log2 = df ? plan.seg_log2_df : plan.seg_log2;
+        stats->grid = fx ? plan.grid_fx : (df ? plan.grid_df : plan.grid);
+        stats->seg_log2 = fx ? plan.seg_log2_fx : (df ? plan.seg_log2_df : plan.seg_log2);
         // h[6]: the double-float estimate, -1 when the range check sent the
         // matrix to the FP64 kernel; above the bar the FP64 twin recomputed
         const bool ran_df = df && h[6] >= 0.0;
         const bool used_df = ran_df && (h[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
-        stats->arith = used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->arith = fx ? GBPERM_ARITH_FX64 : (used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
         stats->err_est = ran_df ? h[6] : 0.0;
     }
     return GBPERM_OK;

@@ -58,12 +58,23 @@ struct PlainPlan {
     int grid_df = 1;
     int seg_log2_df = 0;
     int cpl = 8, grp = 1;  // double-float lane-group shape
-    int max_grid() const { return df && grid_df > grid ? grid_df : grid; }
+    bool fx = false;       // integer-mantissa kernel (runs alone, no FP64 twin)
+    int grid_fx = 1;
+    int seg_log2_fx = 0;
+    int cpl_fx = 8, grp_fx = 1;
+    int max_grid() const {
+        int g = grid;
+        if (df && grid_df > g) g = grid_df;
+        if (fx && grid_fx > g) g = grid_fx;
+        return g;
+    }
 };
 struct PlainWs {
     size_t a1 = 0, a2 = 0, exp = 0, scale = 0, kern = 0;
 };
-PlainPlan plan_plain(int rows, int cols, bool df);
+// arith: GBPERM_ARITH_*; the caller maps DF32 to FP64 beyond kDfMaxCols or
+// when the host range check fails
+PlainPlan plan_plain(int rows, int cols, int arith);
 size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w);
 // d_err: optional device double that receives the double-float product's
 // relative rounding-error estimate (0 when the FP64 product runs)

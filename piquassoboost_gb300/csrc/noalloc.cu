@@ -14,7 +14,14 @@
 // holds it until the process exits.  Host code cannot use the array's name
 // as a device address, so the first call on each device, with that device
 // current, looks the address up with cudaGetSymbolAddress and caches it.
-// That first call should therefore come before any stream capture.
+// That first call should therefore come before any stream capture.  The
+// cached address belongs to the device's primary context: a
+// cudaDeviceReset() while the library is in use leaves it stale, so do not
+// reset a device between calls.
+//
+// Trivial shapes (0 x 0, rows >= cols + 2) are answered by a one-thread
+// kernel that writes the constant on the stream: no host copy and no
+// synchronisation, like every other call of this entry point.
 //
 // All calls share the one array and it keeps the last call's contents: the
 // kernels overwrite every value they read before reading it, and the
@@ -57,6 +64,16 @@ int scratch_for_current_device(void** out) {
     return GBPERM_OK;
 }
 
+// The constant result of a trivial shape (no scratch, no host copy).
+__global__ void noalloc_const_kernel(double v, double* out2, double* out4) {
+    out2[0] = v;
+    out2[1] = 0.0;
+    if (out4) {
+        out4[0] = v;
+        out4[1] = out4[2] = out4[3] = 0.0;
+    }
+}
+
 }  // namespace
 
 }  // namespace gbperm
@@ -74,20 +91,16 @@ extern "C" int gbperm_perm_noalloc(const void* dA, int64_t rows, int64_t cols, i
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double hv[4];
     if (plain_trivial(rows, cols, hv, hv)) {
-        // trivial shapes: write the constant result (a pageable-host copy,
-        // not an allocation)
-        double h2[2] = {hv[0], 0.0};
-        double h4[4] = {hv[0], 0.0, 0.0, 0.0};
-        cudaError_t e = cudaMemcpyAsync(d_out, h2, sizeof(h2), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess && d_out_dd) e = cudaMemcpyAsync(d_out_dd, h4, sizeof(h4), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        noalloc_const_kernel<<<1, 1, 0, st>>>(hv[0], static_cast<double*>(d_out), static_cast<double*>(d_out_dd));
+        cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? GBPERM_OK : cuda_fail(e, "gbperm_perm_noalloc");
     }
     if (!dA) return fail(GBPERM_ERR_ARG, "gbperm_perm_noalloc: null matrix");
     if (ld < cols) return fail(GBPERM_ERR_ARG, "gbperm_perm_noalloc: ld < cols");
     if (rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM)
         return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_noalloc: matrix larger than 64 x 64");
-    PlainPlan plan = plan_plain((int)rows, (int)cols, arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols);
+    PlainPlan plan = plan_plain((int)rows, (int)cols,
+                                arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
     size_t need = plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
     if (need > kNoAllocScratchBytes)
         return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_noalloc: needs " + std::to_string(need) +

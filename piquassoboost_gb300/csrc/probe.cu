@@ -1,10 +1,16 @@
 // Pipe-throughput probes used as roofline denominators.
 //
 // The measured peaks cover HBM copy bandwidth and bf16 tensor rates
-// only; the permanent kernels are bound by the FP64 pipe (FP64 product) or
-// by FP32/ALU issue (double-float product), so the library measures those
-// two peaks itself: a grid of independent FMA chains, 8 per thread, timed
-// with CUDA events after a warm-up launch.
+// only; the permanent kernels are bound by the FP64 pipe (FP64 product), by
+// FP32/ALU issue (double-float product) or by the integer multiply-add pipe
+// (integer-mantissa product), so the library measures those peaks itself:
+// a grid of independent chains, 8 per thread, timed with CUDA events after
+// a warm-up launch.  Kinds:
+//   0  FP64 FMA (DFMA)                    TFLOP/s, 2 flops per FMA
+//   1  FP32 FMA (FFMA)                    TFLOP/s, 2 flops per FMA
+//   2  FP64 tensor MMA (mma.sync m8n8k4)  TFLOP/s, 2*8*8*4 flops per warp MMA
+//   3  32x32->64 multiply-add (mad.wide.s32, IMAD.WIDE)   tera-ops/s (lane ops)
+//   4  32-bit multiply-add (mad.lo.s32, IMAD)             tera-ops/s (lane ops)
 #include "gbperm.h"
 #include "gbperm_capi_internal.h"
 
@@ -42,6 +48,58 @@ __global__ void probe_ffma(float* out, float a, float b) {
     if (s == 123.456f) out[0] = s;
 }
 
+// FP64 tensor core: each warp keeps kChains independent 8x8 accumulators
+// and feeds them the same A/B fragments (one f64 each per lane).
+__global__ void probe_dmma(double* out, double a, double b) {
+    double acc[kChains][2];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) acc[i][0] = acc[i][1] = threadIdx.x * 1e-3 + i;
+    const double fa = a + threadIdx.x * 1e-6, fb = b;
+    for (int it = 0; it < kProbeIters / 4; ++it) {
+#pragma unroll
+        for (int i = 0; i < kChains; ++i)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                         : "+d"(acc[i][0]), "+d"(acc[i][1])
+                         : "d"(fa), "d"(fb));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) s += acc[i][0] + acc[i][1];
+    if (s == 123.456) out[0] = s;
+}
+
+__global__ void probe_imad_wide(long long* out, int a, int b) {
+    long long x[kChains];
+    int m[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) {
+        x[i] = threadIdx.x + i;
+        m[i] = a + (int)threadIdx.x + i;
+    }
+    for (int it = 0; it < 4 * kProbeIters; ++it) {
+#pragma unroll
+        for (int i = 0; i < kChains; ++i) asm volatile("mad.wide.s32 %0, %1, %2, %0;" : "+l"(x[i]) : "r"(m[i]), "r"(b));
+    }
+    long long s = 0;
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) s += x[i];
+    if (s == 123456789) out[0] = s;
+}
+
+__global__ void probe_imad(int* out, int a, int b) {
+    int x[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) x[i] = threadIdx.x + i;
+    for (int it = 0; it < 4 * kProbeIters; ++it) {
+#pragma unroll
+        for (int i = 0; i < kChains; ++i) asm volatile("mad.lo.s32 %0, %0, %1, %2;" : "+r"(x[i]) : "r"(a), "r"(b));
+    }
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) s += x[i];
+    if (s == 123456789) out[0] = s;
+}
+
 }  // namespace
 }  // namespace gbperm
 
@@ -49,7 +107,9 @@ using namespace gbperm;
 
 extern "C" int gbperm_probe_peak(int kind, double* tflops) {
     if (!tflops) return fail(GBPERM_ERR_ARG, "gbperm_probe_peak: null output");
-    if (kind != 0 && kind != 1) return fail(GBPERM_ERR_ARG, "gbperm_probe_peak: kind must be 0 (FP64) or 1 (FP32)");
+    if (kind < 0 || kind > 4)
+        return fail(GBPERM_ERR_ARG,
+                    "gbperm_probe_peak: kind must be 0 (FP64), 1 (FP32), 2 (FP64 MMA), 3 (IMAD.WIDE) or 4 (IMAD)");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_probe_peak");
@@ -65,7 +125,10 @@ extern "C" int gbperm_probe_peak(int kind, double* tflops) {
     for (int rep = 0; rep < 3; ++rep) {
         cudaEventRecord(e0);
         if (kind == 0) probe_dfma<<<blocks, threads>>>((double*)buf, 1.0000001, 1e-9);
-        else probe_ffma<<<blocks, threads>>>((float*)buf, 1.0000001f, 1e-9f);
+        else if (kind == 1) probe_ffma<<<blocks, threads>>>((float*)buf, 1.0000001f, 1e-9f);
+        else if (kind == 2) probe_dmma<<<blocks, threads>>>((double*)buf, 1.0000001, 1e-9);
+        else if (kind == 3) probe_imad_wide<<<blocks, threads>>>((long long*)buf, 3, 5);
+        else probe_imad<<<blocks, threads>>>((int*)buf, 3, 5);
         cudaEventRecord(e1);
         e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) break;
@@ -77,7 +140,11 @@ extern "C" int gbperm_probe_peak(int kind, double* tflops) {
     cudaEventDestroy(e1);
     cudaFree(buf);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_probe_peak: kernel");
-    double fmas = (double)blocks * threads * kChains * (kind == 0 ? kProbeIters : 4.0 * kProbeIters);
-    *tflops = 2.0 * fmas / (best * 1e-3) / 1e12;
+    double ops;
+    if (kind == 0) ops = 2.0 * blocks * threads * kChains * (double)kProbeIters;
+    else if (kind == 1) ops = 2.0 * blocks * threads * kChains * 4.0 * kProbeIters;
+    else if (kind == 2) ops = 2.0 * 8 * 8 * 4 * (blocks * threads / 32.0) * kChains * (kProbeIters / 4);
+    else ops = (double)blocks * threads * kChains * 4.0 * kProbeIters;
+    *tflops = ops / (best * 1e-3) / 1e12;
     return GBPERM_OK;
 }

@@ -40,6 +40,34 @@ def test_grad_sampled_minors(n):
         assert abs(G[k, l] - ref) <= 1e-10 * max(abs(ref), 1e-3 * gnorm)
 
 
+@pytest.mark.parametrize("n", [28, 32])
+def test_grad_large_sampled_minors_and_differences(n):
+    # the gradient sizes of the differentiable-permanent configuration:
+    # 16 seeded entries against their minors (n - 1 permanents on the FP64
+    # kernel, itself pinned to the oracle) and 3 against FP64 central
+    # differences (the permanent is linear in each entry, so the difference
+    # quotient is exact up to rounding)
+    A = haar_block(n, seed=900 + n)
+    p, G = nat.perm_grad(A)
+    ref = nat.perm(A, mode="fp64")
+    assert abs(p - ref) <= 1e-10 * abs(ref)
+    gnorm = np.abs(G).max()
+    rng = np.random.default_rng(n)
+    for _ in range(16):
+        k, l = (int(x) for x in rng.integers(0, n, size=2))
+        m = nat.perm(_minor(A, k, l), mode="fp64")
+        assert abs(G[k, l] - m) <= 1e-10 * max(abs(m), 1e-3 * gnorm), (k, l, G[k, l], m)
+    for _ in range(3):
+        k, l = (int(x) for x in rng.integers(0, n, size=2))
+        h = 1e-2
+        Ap = A.copy()
+        Ap[k, l] += h
+        Am = A.copy()
+        Am[k, l] -= h
+        fd = (nat.perm(Ap, mode="fp64") - nat.perm(Am, mode="fp64")) / (2 * h)
+        assert abs(fd - G[k, l]) <= 1e-8 * max(abs(G[k, l]), 1e-3 * gnorm), (k, l, fd, G[k, l])
+
+
 def test_grad_finite_differences():
     n = 10
     A = haar_block(n, seed=31)
