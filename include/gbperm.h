@@ -88,6 +88,8 @@ int gbperm_device_count(void);
  *                         the batch's total work)
  *   "plain.df_group"      lanes sharing one Gray segment in the double-float kernel
  *                         (1, 2, 4 or 8; 0 = by column count)
+ *   "plain.fx_group"      lanes sharing one Gray segment in the integer-mantissa kernel
+ *                         (0 = by column count: pairs up to 40 columns; 4 = quads from 22)
  *   "df.escalate"         1 (default): a double-float result whose error estimate exceeds
  *                         1e-10 is recomputed by the FP64 kernel; 0: keep it (stats.err_est
  *                         still reports the estimate)
@@ -209,6 +211,30 @@ int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t
  * GBPERM_ERR_STATE_SUM. */
 int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample, const int64_t* current_input,
                        int arith, double* pmf, double* addends, gbperm_stats* stats);
+
+/* ------------------------------------------------ boson sampler (B form) */
+/* The generalised Clifford & Clifford sampler over gbperm_compute_pmf
+ * layers.  Replaces CGeneralizedCliffordsBSimulationStrategy::simulate and
+ * fill_r_sample (piquassoboost/sampling/simulation_strategies/source/
+ * CGeneralizedCliffordsBSimulationStrategy.cpp:137-316, the branch without
+ * MPI) with the reference's random stream: std::mt19937 seeded with the low
+ * 32 bits of `seed` (samplingHelperFunctions.cpp:58-74), so a given seed
+ * yields the reference's samples.  After gbperm_sampler_set_uniform_losses
+ * it is CGeneralizedCliffordsBUniformLossesSimulationStrategy
+ * (CGeneralizedCliffordsBUniformLossesSimulationStrategy.cpp:110-322): each
+ * sample first draws its surviving photon count from the binomial law with
+ * eta = transmissivity^2.  The sampler keeps its own copy of U (m x m,
+ * leading dimension ld) and its own generator (the reference shares one
+ * generator across all strategy objects).  simulate writes nsamples rows of
+ * m occupations (int64) into out; the input state has m entries. */
+typedef struct gbperm_sampler gbperm_sampler;
+int gbperm_sampler_create(const double* U, int64_t m, int64_t ld, uint64_t seed, int arith, gbperm_sampler** out);
+int gbperm_sampler_set_matrix(gbperm_sampler* s, const double* U, int64_t m, int64_t ld);
+int gbperm_sampler_seed(gbperm_sampler* s, uint64_t seed);
+int gbperm_sampler_set_uniform_losses(gbperm_sampler* s, double transmissivity);
+int gbperm_sampler_simulate(gbperm_sampler* s, const int64_t* input_state, int64_t m, int64_t nsamples,
+                            int64_t* out, gbperm_stats* stats);
+void gbperm_sampler_destroy(gbperm_sampler* s);
 
 /* ----------------------------------------------- permanent + gradient */
 /* Permanent of an n x n matrix and its full gradient G[k][l] = dperm/da_kl

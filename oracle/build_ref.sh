@@ -22,6 +22,8 @@ SRCS=(
   "$S/GlynnPermanentCalculators_implementation.cpp" "$S/GlynnPermanentCalculatorSimple.cpp"
   "$S/CChinHuhPermanentCalculator.cpp" "$S/BatchedPermanentCalculator.cpp"
   "$REF/sampling/simulation_strategies/source/samplingHelperFunctions.cpp"
+  "$REF/sampling/simulation_strategies/source/CGeneralizedCliffordsBSimulationStrategy.cpp"
+  "$REF/sampling/simulation_strategies/source/CGeneralizedCliffordsBUniformLossesSimulationStrategy.cpp"
   "$HERE/ref_capi.cpp"
 )
 OBJS=()

@@ -655,3 +655,120 @@ int orc_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sampl
     free(sub);
     return rc;
 }
+
+/* ------------------------------------------------- Clifford & Clifford B */
+/* MT19937 (Matsumoto & Nishimura, ACM TOMACS 8(1), 1998; the generator that
+ * std::mt19937 specifies), restated from the published algorithm: 624-word
+ * state, initialised by x_i = 1812433253 (x_{i-1} xor (x_{i-1} >> 30)) + i,
+ * twisted 624 words at a time and tempered on output. */
+typedef struct {
+    uint32_t x[624];
+    int i;
+} orc_mt_t;
+
+static void orc_mt_seed(orc_mt_t* g, uint32_t s) {
+    g->x[0] = s;
+    for (int i = 1; i < 624; ++i) g->x[i] = 1812433253u * (g->x[i - 1] ^ (g->x[i - 1] >> 30)) + (uint32_t)i;
+    g->i = 624;
+}
+
+static uint32_t orc_mt_next(orc_mt_t* g) {
+    if (g->i >= 624) {
+        for (int k = 0; k < 624; ++k) {
+            const uint32_t y = (g->x[k] & 0x80000000u) | (g->x[(k + 1) % 624] & 0x7fffffffu);
+            g->x[k] = g->x[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        g->i = 0;
+    }
+    uint32_t y = g->x[g->i++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+/* CGeneralizedCliffordsBSimulationStrategy::simulate without MPI
+ * (simulation_strategies/source/CGeneralizedCliffordsBSimulationStrategy.cpp
+ * :137-283) and fill_r_sample (:287-316), with the helpers of
+ * samplingHelperFunctions.cpp: the generator seeded with the low 32 bits of
+ * `seed` (:60-62), a photon of the working input list picked by
+ * generator() % size (:68-74, update_input_by_single_photon :378-405), one
+ * compute_pmf layer per photon, and the output mode drawn as the first index
+ * whose running pmf sum reaches generator() / (2^32 - 1) (sample_from_pmf
+ * :351-375; index 0 when no sum reaches it).  out: nsamples x m occupations.
+ * transmissivity >= 0: the uniform-losses strategy
+ * (CGeneralizedCliffordsBUniformLossesSimulationStrategy.cpp:110-322): each
+ * sample first draws its photon count k, the first k whose running sum of
+ * binom(n, k) eta^k (1 - eta)^(n - k), eta = transmissivity^2, reaches
+ * generator() / (2^32 - 1) (or 1), and places k photons; < 0: lossless. */
+int orc_sample_b(const double* U, int64_t m, int64_t ld, const int64_t* input_state, int64_t nsamples,
+                 uint64_t seed, double transmissivity, int prec, int nthreads, int64_t* out) {
+    orc_mt_t g;
+    orc_mt_seed(&g, (uint32_t)seed);
+    int64_t np = 0;
+    for (int64_t i = 0; i < m; ++i) {
+        if (input_state[i] < 0) return set_err(1, "orc_sample_b: negative occupation");
+        np += input_state[i];
+    }
+    int64_t* particles = (int64_t*)malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
+    int64_t* working = (int64_t*)malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));
+    int64_t* current = (int64_t*)malloc(sizeof(int64_t) * (size_t)m);
+    double* pmf = (double*)malloc(sizeof(double) * (size_t)m);
+    int64_t k = 0;
+    for (int64_t i = 0; i < m; ++i)
+        for (int64_t c = 0; c < input_state[i]; ++c) particles[k++] = i;
+    double* law = (double*)malloc(sizeof(double) * (size_t)(np + 1));
+    if (transmissivity >= 0.0) {
+        const double eta = transmissivity * transmissivity;
+        for (int64_t i = 0; i <= np; ++i) {
+            int64_t b = 1;
+            for (int64_t q = 1; q <= i; ++q) b = b * (np - i + q) / q;
+            law[i] = (double)b * pow(eta, (double)i) * pow(1.0 - eta, (double)(np - i));
+        }
+    }
+    int rc = 0;
+    for (int64_t s = 0; s < nsamples && rc == 0; ++s) {
+        int64_t* sample = out + s * m;
+        memset(sample, 0, sizeof(int64_t) * (size_t)m);
+        memset(current, 0, sizeof(int64_t) * (size_t)m);
+        memcpy(working, particles, sizeof(int64_t) * (size_t)np);
+        int64_t nw = np, ns = 0, target = np;
+        if (transmissivity >= 0.0) {
+            const double u = (double)orc_mt_next(&g) / 4294967295.0;
+            int64_t q = 0;
+            double w = law[0];
+            while (w < u && w < 1.0 && q < np) {
+                ++q;
+                w += law[q];
+            }
+            target = q;
+        }
+        while (target > ns && rc == 0) {
+            const int64_t r = (int64_t)(orc_mt_next(&g) % (uint32_t)nw);
+            current[working[r]]++;
+            memmove(working + r, working + r + 1, sizeof(int64_t) * (size_t)(nw - r - 1));
+            nw--;
+            rc = orc_compute_pmf(U, m, ld, sample, current, prec, nthreads, pmf, NULL);
+            if (rc) break;
+            const double u = (double)orc_mt_next(&g) / 4294967295.0;
+            int64_t pick = 0;
+            double acc = 0.0;
+            for (int64_t i = 0; i < m; ++i) {
+                acc = acc + pmf[i];
+                if (acc >= u) {
+                    pick = i;
+                    break;
+                }
+            }
+            sample[pick]++;
+            ns++;
+        }
+    }
+    free(particles);
+    free(working);
+    free(current);
+    free(pmf);
+    free(law);
+    return rc;
+}

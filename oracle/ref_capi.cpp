@@ -24,6 +24,8 @@
 #include "GlynnPermanentCalculator.h"
 #include "GlynnPermanentCalculatorRepeated.h"
 #include "GlynnPermanentCalculatorSimple.h"
+#include "CGeneralizedCliffordsBSimulationStrategy.h"
+#include "CGeneralizedCliffordsBUniformLossesSimulationStrategy.h"
 #include "samplingHelperFunctions.h"
 
 static thread_local std::string g_err;
@@ -126,6 +128,60 @@ int ref_compute_pmf(const double* U, int64_t m, const int64_t* sample, const int
         inp.number_of_photons = ni;
         pic::matrix_real r = pic::compute_pmf(u, smp, inp);
         std::memcpy(pmf, r.get_data(), (size_t)m * sizeof(double));
+        return 0;
+    } catch (std::string& e) {
+        g_err = e;
+        return 2;
+    }
+}
+
+// The reference's Clifford & Clifford B sampler
+// (CGeneralizedCliffordsBSimulationStrategy.cpp:137-316, without MPI):
+// seeded with `seed`, `nsamples` samples of the input occupation
+// `input_state` (m modes) written row by row into out (nsamples x m).
+int ref_sample_b(const double* U, int64_t m, const int64_t* input_state, int64_t nsamples, uint64_t seed,
+                 int64_t* out) {
+    try {
+        pic::matrix u((pic::Complex16*)U, (size_t)m, (size_t)m);
+        pic::CGeneralizedCliffordsBSimulationStrategy strategy(u, 0);
+        strategy.seed(seed);
+        pic::PicState_int64 inp((int64_t*)input_state, (size_t)m);
+        int64_t np = 0;
+        for (int64_t i = 0; i < m; ++i) np += input_state[i];
+        inp.number_of_photons = np;
+        std::vector<pic::PicState_int64> samples = strategy.simulate(inp, (int)nsamples);
+        if ((int64_t)samples.size() != nsamples) {
+            g_err = "ref_sample_b: fewer samples than asked";
+            return 3;
+        }
+        for (int64_t s = 0; s < nsamples; ++s)
+            std::memcpy(out + s * m, samples[s].get_data(), (size_t)m * sizeof(int64_t));
+        return 0;
+    } catch (std::string& e) {
+        g_err = e;
+        return 2;
+    }
+}
+
+// The reference's uniform-losses sampler
+// (CGeneralizedCliffordsBUniformLossesSimulationStrategy.cpp:110-322).
+int ref_sample_b_uniform_losses(const double* U, int64_t m, double transmissivity, const int64_t* input_state,
+                                int64_t nsamples, uint64_t seed, int64_t* out) {
+    try {
+        pic::matrix u((pic::Complex16*)U, (size_t)m, (size_t)m);
+        pic::CGeneralizedCliffordsBUniformLossesSimulationStrategy strategy(u, transmissivity, 0);
+        strategy.seed(seed);
+        pic::PicState_int64 inp((int64_t*)input_state, (size_t)m);
+        int64_t np = 0;
+        for (int64_t i = 0; i < m; ++i) np += input_state[i];
+        inp.number_of_photons = np;
+        std::vector<pic::PicState_int64> samples = strategy.simulate(inp, (int)nsamples);
+        if ((int64_t)samples.size() != nsamples) {
+            g_err = "ref_sample_b_uniform_losses: fewer samples than asked";
+            return 3;
+        }
+        for (int64_t s = 0; s < nsamples; ++s)
+            std::memcpy(out + s * m, samples[s].get_data(), (size_t)m * sizeof(int64_t));
         return 0;
     } catch (std::string& e) {
         g_err = e;

@@ -103,6 +103,13 @@ _SIGNATURES = [
     ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, ctypes.c_int, _P, _P, _P]),
     ("gbperm_perm_repeated_batched", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _I64, ctypes.c_int, _P, _P]),
+    ("gbperm_sampler_create", ctypes.c_int, [_P, _I64, _I64, ctypes.c_uint64, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbperm_sampler_set_matrix", ctypes.c_int, [_P, _P, _I64, _I64]),
+    ("gbperm_sampler_seed", ctypes.c_int, [_P, ctypes.c_uint64]),
+    ("gbperm_sampler_set_uniform_losses", ctypes.c_int, [_P, ctypes.c_double]),
+    ("gbperm_sampler_simulate", ctypes.c_int, [_P, _P, _I64, _I64, _P, _P]),
+    ("gbperm_sampler_destroy", None, [_P]),
     ("gbperm_mesh_workspace_size", ctypes.c_size_t, [_I64]),
     ("gbperm_mesh_unitary_dev", ctypes.c_int, [_P, _I64, _P, _P, ctypes.c_size_t, _P]),
     ("gbperm_mesh_unitary_backward_dev", ctypes.c_int, [_P, _I64, _P, _P, _P, ctypes.c_size_t, _P]),
@@ -350,6 +357,54 @@ def compute_pmf(interferometer, sample, current_input, mode="fp64", stats: Stats
                                  arith_of(mode), pmf.ctypes.data_as(_P), add.ctypes.data_as(_P),
                                  ctypes.byref(stats) if stats is not None else None))
     return pmf, add
+
+
+class Sampler:
+    """Handle of a native boson sampler (gbperm_sampler_*): the generalised
+    Clifford & Clifford B form over GPU pmf layers, with the reference's
+    std::mt19937 random stream.  transmissivity=None: lossless; a value in
+    [0, 1]: uniform losses (each sample first draws its surviving photon
+    count)."""
+
+    def __init__(self, interferometer, seed: int, mode="fp64", transmissivity=None):
+        lib = load()
+        U = np.ascontiguousarray(interferometer, dtype=np.complex128)
+        if U.ndim != 2 or U.shape[0] != U.shape[1]:
+            raise ValueError("the interferometer must be a square matrix")
+        self._h = ctypes.c_void_p()
+        check(lib.gbperm_sampler_create(U.ctypes.data_as(_P), U.shape[0], U.shape[0], int(seed) & (2 ** 64 - 1),
+                                        arith_of(mode), ctypes.byref(self._h)))
+        self.modes = U.shape[0]
+        if transmissivity is not None:
+            check(lib.gbperm_sampler_set_uniform_losses(self._h, float(transmissivity)))
+
+    def set_matrix(self, interferometer):
+        U = np.ascontiguousarray(interferometer, dtype=np.complex128)
+        if U.ndim != 2 or U.shape[0] != U.shape[1]:
+            raise ValueError("the interferometer must be a square matrix")
+        check(load().gbperm_sampler_set_matrix(self._h, U.ctypes.data_as(_P), U.shape[0], U.shape[0]))
+        self.modes = U.shape[0]
+
+    def seed(self, value: int):
+        check(load().gbperm_sampler_seed(self._h, int(value) & (2 ** 64 - 1)))
+
+    def simulate(self, input_state, samples_number: int, stats: Stats | None = None) -> np.ndarray:
+        inp = np.ascontiguousarray(np.asarray(input_state).reshape(-1), dtype=np.int64)
+        out = np.zeros((max(int(samples_number), 0), inp.shape[0]), dtype=np.int64)
+        check(load().gbperm_sampler_simulate(self._h, inp.ctypes.data_as(_P), inp.shape[0], int(samples_number),
+                                             out.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
+        return out
+
+    def close(self):
+        if self._h:
+            load().gbperm_sampler_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _PROBES = {"fp64": 0, "fp32": 1, "dmma": 2, "imad_wide": 3, "imad": 4}

@@ -101,13 +101,14 @@ def build_oracle(verbose: bool = False) -> str:
 
 
 def build_reference_oracle(verbose: bool = False) -> str | None:
-    """Build oracle/_ref from the reference sources when the reference tree exists."""
+    """Build oracle/_ref (the reference's own calculators, test
+    infrastructure) with oracle/build_ref.sh.  The script locates the
+    reference tree (PQB_REFERENCE_ROOT, or its default) and exits with status
+    3 where there is none, as on the GPU machine; then this returns None."""
     script = os.path.join(REPO_DIR, "oracle", "build_ref.sh")
+    shim = os.path.join(REPO_DIR, "oracle", "ref_capi.cpp")
     out = os.path.join(REPO_DIR, "oracle", "_ref", "libpqbref.so")
-    root = os.environ.get("PQB_REFERENCE_ROOT", "/root/reference")
-    if not os.path.isdir(os.path.join(root, "piquassoboost", "sampling", "source")):
-        return None
-    if os.path.exists(out):
+    if not _stale(out, [script, shim]):
         return out
     r = subprocess.run(["bash", script], capture_output=True, text=True)
     if verbose:

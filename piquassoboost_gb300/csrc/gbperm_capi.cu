@@ -165,7 +165,7 @@ PlainPlan plan_plain(int rows, int cols, int arith) {
     int sms = device_sms(dev);
     if (p.fx) {
         // the integer-mantissa kernel runs alone: no FP64 twin to plan
-        fx_shape(cols, &p.cpl_fx, &p.grp_fx);
+        fx_shape(cols, (int)g_opt.plain_fx_group.load(), &p.cpl_fx, &p.grp_fx);
         plain_geometry(rows, sms * plain_fx_blocks_per_sm(rows, p.cpl_fx, p.grp_fx), p.grp_fx, &p.grid_fx,
                        &p.seg_log2_fx);
         return p;

@@ -101,7 +101,9 @@ cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* ex
 
 // Integer-mantissa product (perm_plain_fx.cu): lane-group shape for a column
 // count, occupancy and launch.  No range check and no FP64 twin.
-void fx_shape(int cols, int* cpl, int* grp);
+// group: 0 = by column count (lane pairs up to 40 columns), 4 = lane quads
+// from 22 columns on
+void fx_shape(int cols, int group, int* cpl, int* grp);
 int plain_fx_blocks_per_sm(int rows, int cpl, int grp);
 cudaError_t launch_plain_fx(const longlong2* a1, const longlong2* a2, const int* exp_in, int rows, int cols,
                             int cpl, int grp, int grid, int seg_log2, void* ws, double* out2, double* out4,
@@ -150,6 +152,10 @@ void repeated_df_shape(int cols, int* cpl, int* grp);
 int repeated_df_blocks_per_sm(const RepArgs& a, int cpl, int grp);
 cudaError_t launch_repeated_df(RepArgs a, int cpl, int grp, int grid, void* ws, bool escalate, cudaStream_t st);
 size_t repeated_workspace_bytes(int grid);
+// integer-mantissa product (perm_repeated_fx.cu): no range check, no twin
+void repeated_fx_shape(int cols, int* cpl, int* grp);
+int repeated_fx_blocks_per_sm(const RepArgs& a, int cpl, int grp);
+cudaError_t launch_repeated_fx(RepArgs a, int cpl, int grp, int grid, void* ws, cudaStream_t st);
 cudaError_t launch_repeated(RepArgs a, int grid, void* ws, cudaStream_t st);
 
 // Scale a double-double complex sum by 2^e and store it: out2 = {re, im}

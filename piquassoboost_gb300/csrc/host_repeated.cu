@@ -264,7 +264,7 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
                         int64_t ncol, const int64_t* row_mult, int64_t nrow, int arith, double* out, double* out_dd,
                         gbperm_stats* stats, bool chinhuh) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
-    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: unknown arithmetic");
     if (!out) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: null output");
     if (rows < 0 || cols < 0 || nrow < 0 || ncol < 0) return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated: negative size");
@@ -297,6 +297,10 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), cw.data(), &boost);
     }
     if (df) repeated_df_shape(h.C, &dcpl, &dgrp);
+    // integer-mantissa product: runs alone (no FP64 twin)
+    const bool fx = arith == GBPERM_ARITH_FX64;
+    int xcpl = 0, xgrp = 0, grid_fx = 1;
+    if (fx) repeated_fx_shape(h.C, &xcpl, &xgrp);
     int dev = 0;
     cudaGetDevice(&dev);
     const unsigned long long sms = (unsigned long long)device_sms(dev);
@@ -312,10 +316,11 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         [&](unsigned long long P) {
             RepArgs t = a;
             t.P = P;
+            if (fx) return sms * (unsigned long long)repeated_fx_blocks_per_sm(t, xcpl, xgrp) * (128ull / xgrp);
             if (df) return sms * (unsigned long long)repeated_df_blocks_per_sm(t, dcpl, dgrp) * (128ull / dgrp);
             return sms * (unsigned long long)repeated_blocks_per_sm(t) * 128ull;
         },
-        df ? 6.5 : 2.0);
+        fx ? 4.0 : (df ? 6.5 : 2.0));
     a.q = h.q;
     a.P = h.P;
     a.nseg = h.nseg;
@@ -329,8 +334,14 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         unsigned long long need_df = (h.nseg + per_block - 1) / per_block;
         grid_df = (int)std::max(1ull, std::min(gfull, need_df));
     }
+    if (fx) {
+        unsigned long long gfull = sms * repeated_fx_blocks_per_sm(a, xcpl, xgrp);
+        unsigned long long per_block = 128ull / (unsigned long long)xgrp;
+        unsigned long long need_fx = (h.nseg + per_block - 1) / per_block;
+        grid_fx = (int)std::max(1ull, std::min(gfull, need_fx));
+    }
     RepWs w;
-    size_t bytes = repeated_ws_layout(h, std::max(grid, grid_df), &w);
+    size_t bytes = repeated_ws_layout(h, std::max(std::max(grid, grid_df), grid_fx), &w);
     ThreadCtx& c = thread_ctx();
     rc = c.ensure(bytes);
     if (rc) return rc;
@@ -388,11 +399,16 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
             e = launch_repeated_df(a, dcpl, dgrp, grid_df, base + w.kern, g_opt.df_escalate.load() != 0, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: df launch");
     }
-    // the FP64 twin scales by the exponent without the double-float boost
-    a.exp_in = pa.exp_fp64_out;
-    a.err_out = nullptr;
-    e = launch_repeated(a, grid, base + w.kern, st);
-    if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: launch");
+    if (fx) {
+        e = launch_repeated_fx(a, xcpl, xgrp, grid_fx, base + w.kern, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: fx launch");
+    } else {
+        // the FP64 twin scales by the exponent without the double-float boost
+        a.exp_in = pa.exp_fp64_out;
+        a.err_out = nullptr;
+        e = launch_repeated(a, grid, base + w.kern, st);
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: launch");
+    }
     if (stats) cudaEventRecord(c.ev1, st);
     double hres[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     e = cudaMemcpyAsync(hres, dout, (df ? 7 : 6) * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -408,11 +424,11 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         stats->steps = h.steps;
         stats->flops = h.flops;
         stats->launches = df ? 3 : 2;
-        stats->grid = df ? grid_df : grid;
+        stats->grid = fx ? grid_fx : (df ? grid_df : grid);
         stats->seg_log2 = h.q;
         const bool ran_df = df && hres[6] >= 0.0;
         const bool used_df = ran_df && (hres[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
-        stats->arith = used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->arith = fx ? GBPERM_ARITH_FX64 : (used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
         stats->err_est = ran_df ? hres[6] : 0.0;
     }
     return GBPERM_OK;

@@ -227,19 +227,20 @@ int fx_bps_t(int rows) {
 }
 
 // (CPL, GROUP) shapes compiled: one lane up to 8 columns, lane pairs up to
-// 40, lane quads up to 64; fx_shape() picks CPL = ceil(cols / GROUP), which
-// leaves every lane at least one real column
+// 40, lane quads above (and from 22 columns on request); fx_shape() picks
+// CPL = ceil(cols / GROUP), which leaves every lane at least one real column
 #define GBPERM_FX_SHAPES(X)                                                                                   \
     X(8, 1) X(5, 2) X(6, 2) X(7, 2) X(8, 2) X(9, 2) X(10, 2) X(11, 2) X(12, 2) X(13, 2) X(14, 2) X(15, 2)    \
-    X(16, 2) X(17, 2) X(18, 2) X(19, 2) X(20, 2) X(11, 4) X(12, 4) X(13, 4) X(14, 4) X(15, 4) X(16, 4)
+    X(16, 2) X(17, 2) X(18, 2) X(19, 2) X(20, 2) X(6, 4) X(7, 4) X(8, 4) X(9, 4) X(10, 4) X(11, 4) X(12, 4)  \
+    X(13, 4) X(14, 4) X(15, 4) X(16, 4)
 
 }  // namespace
 
-void fx_shape(int cols, int* cpl, int* grp) {
+void fx_shape(int cols, int group, int* cpl, int* grp) {
     if (cols <= 8) {
         *cpl = 8;
         *grp = 1;
-    } else if (cols <= 40) {
+    } else if (cols <= 40 && !(group == 4 && cols > 21)) {
         *grp = 2;
         *cpl = (cols + 1) / 2;
     } else {

@@ -1,0 +1,348 @@
+// Repeated-multiplicity permanent with the integer-mantissa product (GB300
+// integer pipes).
+//
+// Same sum, digit plan and exact int64 column sums as perm_repeated.cu
+// (BBFGPermanentCalculatorRepeated.hpp:116-307); the product
+// prod_j colsum_j^(c_j) runs on 64-bit integer mantissas in 31-bit limbs
+// (gbperm_fx.cuh), with lane groups as in perm_repeated_df.cu: GROUP lanes
+// walk one segment, lane g owns columns [g*CPL, (g+1)*CPL), forms their
+// partial product in two interleaved chains, and a shuffle butterfly
+// multiplies the GROUP partials.  Every lane of a group tracks the same Gray
+// digits, so the weights and signs need no exchange.  The leader converts the
+// term to double with integer instructions and accumulates weight x term
+// with one FP64 FMA per component.  No range check, error estimate or FP64
+// twin: each multiply keeps 55-57 significant bits.
+#include "gbperm_fx.cuh"
+#include "gbperm_internal.h"
+
+namespace gbperm {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+// x^e of a column sum (e >= 2) as normalised limbs; returns the shift count
+// sigma of the result.  Out of line: reached only for columns of
+// multiplicity above 1.
+__device__ __noinline__ int fx_pow_col(long long cr, long long ci, int e, fxl* out) {
+    fxl z;
+    const int sz = fx_norm_col(cr, ci, z);
+    fxl r = z;
+    int sig = sz;
+    for (int k = 1; k < e; ++k) {
+        long long pr, pi;
+        fx_mul(r, z, pr, pi);
+        sig += sz - 1 + fx_norm(pr, pi, r);
+    }
+    *out = r;
+    return sig;
+}
+
+template <int CPL, int GROUP>
+__global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
+    constexpr int NP = CPL * GROUP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);            // R x NP
+    longlong2* s_a2 = s_a1 + p.R * NP;                                   // nd x NP
+    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);           // P
+    unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);  // P
+    __shared__ int s_cpow[NP];
+    __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
+    __shared__ long long s_stride[kMaxDigits];
+    const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
+    }
+    for (int e = threadIdx.x; e < nd * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
+    }
+    for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
+        s_w[e] = p.wlow[e];
+        s_seq[e] = p.seq[e];
+    }
+    for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
+    for (int e = threadIdx.x; e < nd; e += blockDim.x) s_D[e] = p.D[e];
+    for (int e = threadIdx.x; e < R; e += blockDim.x) s_r[e] = p.rcoef[e];
+    if (threadIdx.x == 0) {
+        long long s = 1;
+        for (int i = 0; i < q; ++i) {
+            s_stride[i] = s;
+            s *= (long long)(p.D[i] + 1);
+        }
+    }
+    __syncthreads();
+
+    const int g = threadIdx.x % GROUP;
+    const int j0 = g * CPL;
+    // real columns of this lane: contiguous from its first column (>= 1, the
+    // host picks shapes with C > (GROUP - 1) * CPL)
+    const int nr = C - j0 < CPL ? C - j0 : CPL;
+    const bool leader = (g == 0);
+    cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
+    const unsigned long long lane_seg = (threadIdx.x & 31) / GROUP;
+    constexpr unsigned long long S = 32 / GROUP;  // segments per warp
+    const unsigned long long full = p.nseg / (2 * S) * (2 * S);
+    long long cre[CPL], cim[CPL];
+
+    for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / GROUP;
+         hw < p.nseg; hw += T) {
+        const unsigned long long h_raw = parity_slot(hw + lane_seg, S, full);
+        const bool active = h_raw < p.nseg;
+        const unsigned long long h = active ? h_raw : 0ull;
+        int gdig[kMaxDigits];
+        {
+            unsigned long long rem = h;
+            int cnt[kMaxDigits];
+            for (int i = q; i < nd; ++i) {
+                unsigned long long L = (unsigned long long)(s_D[i] + 1);
+                cnt[i] = (int)(rem % L);
+                rem /= L;
+            }
+            int par = 0;
+            for (int i = nd - 1; i >= 0; --i) {
+                int c = i >= q ? cnt[i] : 0;
+                int gg = par ? s_D[i] - c : c;
+                gdig[i] = gg;
+                par ^= gg & 1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cre[c] = 0;
+            cim[c] = 0;
+        }
+        int gsum = 0;
+        double whigh = 1.0;
+        unsigned long long Gd = 0ull;
+        unsigned int dir = 0u;
+        long long widx = 0;
+        for (int i = 0; i < R; ++i) {
+            int gi = i < nd ? gdig[i] : 0;
+            long long coef = (long long)(s_r[i] - 2 * gi);
+            const longlong2* a = s_a1 + i * NP + j0;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                longlong2 v = a[c];
+                cre[c] += coef * v.x;
+                cim[c] += coef * v.y;
+            }
+            if (i < nd) {
+                gsum += gi;
+                if (i < q) {
+                    Gd |= (unsigned long long)gi << (4 * i);
+                    if (gi == 0) dir |= 1u << i;
+                    widx += (long long)gi * s_stride[i];
+                } else {
+                    whigh *= p.binom[s_D[i] * kBinomStride + gi];
+                }
+            }
+        }
+        unsigned long long sbit = (unsigned long long)(gsum & 1) << 63;
+        double bre = 0.0, bim = 0.0;
+        for (unsigned long long k = 0; k < p.P; ++k) {
+            if (k != 0) {
+                const int d = s_seq[k];  // warp-uniform
+                const bool up = (dir >> d) & 1u;
+                const int sh = 4 * d;
+                int gv = (int)((Gd >> sh) & 15ull);
+                gv += up ? 1 : -1;
+                Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
+                if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
+                widx += up ? s_stride[d] : -s_stride[d];
+                // warp-uniform: a warp's segments share their parity
+                const longlong2* a = s_a2 + d * NP + j0;
+                if (up) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] -= v.x;
+                        cim[c] -= v.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] += v.x;
+                        cim[c] += v.y;
+                    }
+                }
+                sbit ^= 0x8000000000000000ull;
+                if ((k & 255ull) == 0) {
+                    acc.re = dd_add_d(acc.re, bre * whigh);
+                    acc.im = dd_add_d(acc.im, bim * whigh);
+                    bre = 0.0;
+                    bim = 0.0;
+                }
+            }
+            // prod_c colsum_c^(power_c) of this lane's real columns, in two
+            // chains; sig: shift count (shifts minus multiplies)
+            fxl ch[2];
+            int sig = 0;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (c < nr) {
+                    const int e = s_cpow[j0 + c];
+                    if (e == 1) {
+                        if (c < 2) {
+                            sig += fx_norm_col(cre[c], cim[c], ch[c]);
+                        } else {
+                            long long rr, ri;
+                            fx_mul(ch[c & 1], fx_col(cre[c], cim[c]), rr, ri);
+                            sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                        }
+                    } else if (e > 1) {
+                        fxl x;
+                        const int sx = fx_pow_col(cre[c], cim[c], e, &x);
+                        if (c < 2) {
+                            ch[c] = x;
+                            sig += sx;
+                        } else {
+                            long long rr, ri;
+                            fx_mul(ch[c & 1], x, rr, ri);
+                            sig += sx + fx_norm(rr, ri, ch[c & 1]) - 1;
+                        }
+                    } else if (c < 2) {
+                        // a column of power 0 among the real ones cannot
+                        // occur (the host drops empty columns); keep the
+                        // chain defined as the value 1 = 2^58 2^-58
+                        ch[c] = fxl{1 << 27, 0, 0, 0};
+                        sig += -3;
+                    }
+                }
+            }
+            long long pr, pi;
+            if (nr >= 2) {
+                fx_mul(ch[0], ch[1], pr, pi);
+                sig -= 1;
+            } else {
+                pr = fx_join(ch[0].rh, ch[0].rl);
+                pi = fx_join(ch[0].ih, ch[0].il);
+            }
+#pragma unroll
+            for (int m = 1; m < GROUP; m <<= 1) {
+                fxl x;
+                sig += fx_norm(pr, pi, x);
+                const fxl y = shfl_xor_fxl(x, m);
+                sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
+                fx_mul(x, y, pr, pi);
+            }
+            if (leader && active) {
+                const int ex = -61 - sig;
+                const double w = s_w[widx];
+                const double tr = __longlong_as_double(__double_as_longlong(fx_to_double(pr, ex)) ^ (long long)sbit);
+                const double ti = __longlong_as_double(__double_as_longlong(fx_to_double(pi, ex)) ^ (long long)sbit);
+                bre = fma(w, tr, bre);
+                bim = fma(w, ti, bim);
+            }
+        }
+        acc.re = dd_add_d(acc.re, bre * whigh);
+        acc.im = dd_add_d(acc.im, bim * whigh);
+    }
+
+    // block reduction (double-double, fixed order); the last block sums the
+    // block partials with all its threads
+    __shared__ cdd s_warp[kThreads / 32];
+    __shared__ bool s_last;
+    acc = warp_sum_cdd(acc);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd b = s_warp[0];
+        for (int w = 1; w < kThreads / 32; ++w) b = cdd_add(b, s_warp[w]);
+        p.block_part[blockIdx.x] = b;
+        __threadfence();
+        unsigned int t = atomicAdd(p.done, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        for (unsigned int bk = threadIdx.x; bk < gridDim.x; bk += blockDim.x) {
+            const volatile double* qv = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
+            cdd v{{qv[0], qv[1]}, {qv[2], qv[3]}};
+            tot = cdd_add(tot, v);
+        }
+        tot = warp_sum_cdd(tot);
+        if (lane == 0) s_warp[warp] = tot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cdd all = s_warp[0];
+            for (int w = 1; w < kThreads / 32; ++w) all = cdd_add(all, s_warp[w]);
+            write_result(all, *p.exp_in, p.out2, p.out4);
+            *p.done = 0u;
+        }
+    }
+}
+
+template <int CPL, int GROUP>
+size_t rep_fx_smem(const RepArgs& a) {
+    return (size_t)(a.R + a.nd) * CPL * GROUP * sizeof(longlong2) + (size_t)a.P * (sizeof(double) + 1) + 16;
+}
+
+template <int CPL, int GROUP>
+cudaError_t launch_rep_fx_t(const RepArgs& a, int grid, cudaStream_t st) {
+    cudaError_t e = allow_max_dynamic_smem((const void*)repeated_fx_kernel<CPL, GROUP>);
+    if (e != cudaSuccess) return e;
+    repeated_fx_kernel<CPL, GROUP><<<grid, kThreads, rep_fx_smem<CPL, GROUP>(a), st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int CPL, int GROUP>
+int rep_fx_bps_t(const RepArgs& a) {
+    int nb = 0;
+    allow_max_dynamic_smem((const void*)repeated_fx_kernel<CPL, GROUP>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, repeated_fx_kernel<CPL, GROUP>, kThreads,
+                                                  rep_fx_smem<CPL, GROUP>(a));
+    return nb > 0 ? nb : 1;
+}
+
+// one lane up to 8 columns; lane pairs with an even column count per lane up
+// to 40; lane quads up to 64.  Every lane keeps at least one real column.
+#define GBPERM_REP_FX_SHAPES(X) \
+    X(8, 1) X(6, 2) X(8, 2) X(10, 2) X(12, 2) X(14, 2) X(16, 2) X(18, 2) X(20, 2) X(12, 4) X(16, 4)
+
+}  // namespace
+
+void repeated_fx_shape(int cols, int* cpl, int* grp) {
+    if (cols <= 8) {
+        *cpl = 8;
+        *grp = 1;
+        return;
+    }
+    if (cols <= 40) {
+        *grp = 2;
+        const int half = (cols + 1) / 2;
+        *cpl = half < 6 ? 6 : (half + 1) / 2 * 2;
+        return;
+    }
+    *grp = 4;
+    *cpl = cols <= 48 ? 12 : 16;
+}
+
+int repeated_fx_blocks_per_sm(const RepArgs& a, int cpl, int grp) {
+#define X(C, G) \
+    if (cpl == C && grp == G) return rep_fx_bps_t<C, G>(a);
+    GBPERM_REP_FX_SHAPES(X)
+#undef X
+    return 1;
+}
+
+cudaError_t launch_repeated_fx(RepArgs a, int cpl, int grp, int grid, void* ws, cudaStream_t st) {
+    char* w = static_cast<char*>(ws);
+    a.block_part = reinterpret_cast<cdd*>(w);
+    a.done = reinterpret_cast<unsigned int*>(w + align_up((size_t)grid * sizeof(cdd), 256));
+    cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+#define X(C, G) \
+    if (cpl == C && grp == G) return launch_rep_fx_t<C, G>(a, grid, st);
+    GBPERM_REP_FX_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace gbperm

@@ -12,7 +12,14 @@ It writes
                              is parsed, never executed);
   reference_calculators.json outputs of the reference's own C++ calculators
                              (plain lib 0/6/7/8/10/11, repeated lib 0/1/6/7/8,
-                             adaptInterferometer) on seeded inputs.
+                             adaptInterferometer) on seeded inputs;
+  reference_sampler.json     the seeded boson samples of the reference's
+                             unittests/test_seeding.py (the lossless and the
+                             uniform-losses cases; literals read with the AST
+                             as above), and sample sequences of the
+                             reference's own C++ samplers
+                             (CGeneralizedCliffordsB[UniformLosses]
+                             SimulationStrategy) on seeded inputs.
 The fixtures are committed; tests read them without the reference.
 """
 from __future__ import annotations
@@ -240,6 +247,118 @@ def reference_calculators(ref):
     return cases
 
 
+# ------------------------------------------------------------ sampler side
+def _literal(node):
+    """Python literals, unary minus and complex sums like -0.1 - 0.2j."""
+    if isinstance(node, ast.Constant):
+        return node.value
+    if isinstance(node, (ast.List, ast.Tuple)):
+        return [_literal(e) for e in node.elts]
+    if isinstance(node, ast.UnaryOp) and isinstance(node.op, (ast.USub, ast.UAdd)):
+        v = _literal(node.operand)
+        return -v if isinstance(node.op, ast.USub) else v
+    if isinstance(node, ast.BinOp) and isinstance(node.op, (ast.Add, ast.Sub)):
+        a, b = _literal(node.left), _literal(node.right)
+        return a + b if isinstance(node.op, ast.Add) else a - b
+    if isinstance(node, ast.BinOp) and isinstance(node.op, ast.Mult):
+        a, b = _literal(node.left), _literal(node.right)
+        return a * b  # list repetition, as Python evaluates it
+    raise ValueError(f"not a literal: {ast.dump(node)[:80]}")
+
+
+def extract_seeding(path):
+    """The lossless and uniform-losses boson-sampling cases of
+    unittests/test_seeding.py: interferometer, input occupation, seed,
+    shots, singular values and the expected samples (a multiset: piquasso
+    lists the samples grouped from its outcome counts, not in drawing
+    order)."""
+    tree = ast.parse(open(path).read())
+    U = None
+    for st in tree.body:
+        if isinstance(st, ast.Assign) and st.targets[0].id == "_U":
+            U = np.array(_literal(st.value.args[0]), dtype=np.complex128)
+    cases = []
+    for fn in tree.body:
+        if not isinstance(fn, ast.FunctionDef) or fn.name not in (
+                "test_boson_sampling_seeded", "test_LossyInterferometer_boson_sampling_uniform_losses"):
+            continue
+        vals = {}
+        for node in ast.walk(fn):
+            if isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Name):
+                name = node.targets[0].id
+                if name in ("seed_sequence", "expected_samples"):
+                    vals[name] = _literal(node.value)
+                if name == "singular_values":
+                    vals[name] = _literal(node.value.args[0])
+            if isinstance(node, ast.Call) and getattr(node.func, "attr", "") == "StateVector":
+                vals["input_state"] = _literal(node.args[0])
+            if isinstance(node, ast.Call) and getattr(node.func, "attr", "") == "execute":
+                for kw in node.keywords:
+                    if kw.arg == "shots":
+                        vals["shots"] = _literal(kw.value)
+        case = {"name": fn.name, "source": f"unittests/test_seeding.py:{fn.lineno}", "seed": vals["seed_sequence"],
+                "input_state": vals["input_state"], "shots": vals["shots"],
+                "expected_multiset": sorted(list(map(list, vals["expected_samples"])))}
+        if "singular_values" in vals:
+            # the test's lossy matrix _U diag(s) _U _U^T; its singular values are
+            # uniform, so the reference's boosted path divides it by the first
+            # one and runs the uniform-losses strategy with that transmissivity
+            M = U @ np.diag(np.array(vals["singular_values"])) @ U @ U.T
+            sv = np.linalg.svd(M)[1]
+            case["transmissivity"] = float(sv[0])
+            case["interferometer"] = _cplx_list(M / sv[0])
+        else:
+            case["interferometer"] = _cplx_list(U)
+        case["modes"] = len(vals["input_state"])
+        cases.append(case)
+    return cases
+
+
+def reference_sampler(ref_so, seeding_cases):
+    lib = ctypes.CDLL(ref_so)
+    lib.ref_sample_b.argtypes = [_P, _I, _P, _I, ctypes.c_uint64, _P]
+    lib.ref_sample_b_uniform_losses.argtypes = [_P, _I, ctypes.c_double, _P, _I, ctypes.c_uint64, _P]
+
+    def run(U, inp, seed, n, t=None):
+        U = np.ascontiguousarray(U, dtype=np.complex128)
+        m = U.shape[0]
+        inp = np.ascontiguousarray(inp, dtype=np.int64)
+        out = np.zeros((n, m), dtype=np.int64)
+        if t is None:
+            rc = lib.ref_sample_b(U.ctypes.data_as(_P), m, inp.ctypes.data_as(_P), n, seed, out.ctypes.data_as(_P))
+        else:
+            rc = lib.ref_sample_b_uniform_losses(U.ctypes.data_as(_P), m, t, inp.ctypes.data_as(_P), n, seed,
+                                                 out.ctypes.data_as(_P))
+        if rc != 0:
+            raise RuntimeError("reference sampler failed")
+        return out.tolist()
+
+    seqs = []
+    for c in seeding_cases:
+        U = np.array([complex(a, b) for a, b in c["interferometer"]]).reshape(c["modes"], c["modes"])
+        got = run(U, c["input_state"], c["seed"], c["shots"], c.get("transmissivity"))
+        if sorted(got) != c["expected_multiset"]:
+            raise RuntimeError(f"the reference build does not reproduce {c['name']}")
+        seqs.append({"name": c["name"], "interferometer": c["interferometer"], "modes": c["modes"],
+                     "input_state": c["input_state"], "seed": c["seed"], "transmissivity": c.get("transmissivity"),
+                     "samples": got})
+    # seeded Haar interferometers: (modes, unitary seed, input occupation,
+    # sampler seed, samples, transmissivity or None)
+    plan = [
+        (8, 3, [1, 1, 1, 1, 0, 0, 0, 0], 5, 12, None),
+        (12, 4, [1, 0, 1, 0, 2, 0, 1, 0, 0, 0, 0, 0], 77, 10, None),
+        (16, 5, [1] * 8 + [0] * 8, 2024, 6, None),
+        (20, 6, [1] * 10 + [0] * 10, 9, 4, None),
+        (10, 7, [1] * 5 + [0] * 5, 11, 15, 0.8),
+        (14, 8, [2, 0, 1, 1, 0, 1, 0, 0, 1, 0, 0, 0, 0, 0], 123, 10, 0.6),
+    ]
+    for m, useed, inp, seed, n, t in plan:
+        U = haar_unitary(m, useed)
+        seqs.append({"name": f"haar{m}_seed{seed}", "interferometer": _cplx_list(U), "modes": m,
+                     "input_state": inp, "seed": seed, "transmissivity": t, "samples": run(U, inp, seed, n, t)})
+    return seqs
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference-root", default=os.environ.get("PQB_REFERENCE_ROOT", "/root/reference"))
@@ -258,6 +377,12 @@ def main():
     with open(os.path.join(HERE, "reference_calculators.json"), "w") as f:
         json.dump({"source": "reference C++ calculators built by oracle/build_ref.sh", **calc}, f)
     print({k: len(v) for k, v in calc.items()})
+    seeding = extract_seeding(os.path.join(args.reference_root, "unittests", "test_seeding.py"))
+    seqs = reference_sampler(so, seeding)
+    with open(os.path.join(HERE, "reference_sampler.json"), "w") as f:
+        json.dump({"source": "unittests/test_seeding.py and the reference C++ samplers built by oracle/build_ref.sh",
+                   "seeding_cases": seeding, "sequences": seqs}, f)
+    print(f"{len(seeding)} seeding cases, {len(seqs)} sampler sequences")
 
 
 if __name__ == "__main__":

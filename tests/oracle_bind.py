@@ -148,3 +148,19 @@ def compute_pmf(U, sample, current_input, prec=0, threads=0):
     if rc != 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return pmf, add
+
+
+def sample_b(U, input_state, nsamples, seed, transmissivity=None, prec=0, threads=1):
+    """The oracle's Clifford & Clifford B sampler (orc_sample_b): nsamples
+    rows of output occupations; transmissivity None = lossless."""
+    u = _mat(U)
+    m = u.shape[0]
+    inp = np.ascontiguousarray(input_state, dtype=np.int64)
+    out = np.zeros((nsamples, m), dtype=np.int64)
+    f = lib().orc_sample_b
+    f.argtypes = [_P, _I, _I, _P, _I, ctypes.c_uint64, ctypes.c_double, ctypes.c_int, ctypes.c_int, _P]
+    rc = f(u.ctypes.data_as(_P), m, m, inp.ctypes.data_as(_P), nsamples, seed,
+           -1.0 if transmissivity is None else float(transmissivity), prec, threads, out.ctypes.data_as(_P))
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return out

@@ -20,7 +20,7 @@ def _random_case(seed):
     return A, cin, rout
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fast"])
+@pytest.mark.parametrize("mode", ["fp64", "fast", "fx"])
 @pytest.mark.parametrize("seed", range(60))
 def test_repeated_random(seed, mode):
     A, cin, rout = _random_case(seed)
@@ -44,7 +44,7 @@ def test_repeated_matches_expanded_plain():
     assert orc.rel_err(v, dref) <= TOL
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fast"])
+@pytest.mark.parametrize("mode", ["fp64", "fast", "fx"])
 def test_repeated_24_modes_12_photons(mode):
     U, inp, out = repeated_instance(seed=11, modes=24, photons=12, max_mult=4)
     st = nat.Stats()
@@ -53,6 +53,37 @@ def test_repeated_24_modes_12_photons(mode):
     assert orc.rel_err(v, dref) <= TOL
     if mode == "fast":
         assert st.arith == nat.ARITH_DF32
+    if mode == "fx":
+        assert st.arith == nat.ARITH_FX64
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_repeated_fx_vs_fp64_60_modes_30_photons(seed):
+    # the repeated configuration (60-mode Haar, 30 photons, multiplicities up
+    # to 4): the integer-mantissa product against the FP64 kernel, where the
+    # double-float product misses the bar on most instances
+    U, inp, out = repeated_instance(seed=seed, modes=60, photons=30, max_mult=4)
+    a = nat.perm_repeated(U, inp, out, mode="fx")
+    b = nat.perm_repeated(U, inp, out, mode="fp64")
+    assert abs(a - b) <= TOL * abs(b), (a, b)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_repeated_fx_column_powers(seed):
+    # input multiplicities above 1 on the column side (powers by repeated
+    # normalised multiplies), several lane shapes
+    rng = np.random.default_rng(500 + seed)
+    m = int(rng.integers(6, 26))
+    U = haar_unitary(m, 500 + seed)
+    k = int(rng.integers(4, 12))
+    cin = rng.multinomial(k, np.ones(m) / m).astype(np.int64)
+    rout = rng.multinomial(k, np.ones(m) / m).astype(np.int64)
+    v = nat.perm_repeated(U, cin, rout, mode="fx")
+    _, dref = orc.bbfg_repeated(U, cin, rout, prec=1)
+    if abs(complex(dref[0], dref[1])) < 1e-300:
+        assert abs(v) < 1e-12
+    else:
+        assert orc.rel_err(v, dref) <= TOL
 
 
 def test_repeated_fast_vs_fp64_boson_sampling_shape():
