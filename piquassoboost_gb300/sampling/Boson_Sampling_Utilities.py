@@ -14,14 +14,19 @@ Library ids (the reference's tables, GlynnPermanentCalculator_Wrapper.hpp
 :34-44 and ChinHuhPermanentCalculator_Wrapper.hpp:36-47) all select the same
 GPU Glynn/BBFG sum; the ids whose reference backend is absent from a build
 without MPFR or FPGA support fail the same way the reference does ("Wrong
-value set for permanent library.").  Two ids are added: 20 (GB300 FP64) and
-21 (GB300 fast: FP32-pipe double-float product).
+value set for permanent library.").  Three ids are added: 20 (GB300 FP64),
+21 (GB300 fast: FP32-pipe double-float product) and 22 (GB300 integer-mantissa
+product).  The reference's "long double" ids (plain 0, 8, 11; repeated 1, 8)
+run the integer-mantissa product: 55-57 significant bits per complex
+multiply, more than the FP64 product's 53 (it does not reach the x87
+extended type's 64).  Lists of matrices or of states run through the batched
+launches, which have no integer-mantissa product: there "fx" uses FP64.
 
 Every class also takes a keyword-only ``backend``: None (default) keeps the
-arithmetic of its library id, "fp64" selects the FP64 product and "fast" the
-double-float product (whose results above a 1e-10 error estimate are
-recomputed in FP64 on the device).  The reference has no such argument; an
-unknown value raises ValueError.
+arithmetic of its library id, "fp64" selects the FP64 product, "fx" the
+integer-mantissa product and "fast" the double-float product (whose results
+above a 1e-10 error estimate are recomputed in FP64 on the device).  The
+reference has no such argument; an unknown value raises ValueError.
 
 Deliberate deviations: arrays are converted to complex128 / int64 (the
 reference reinterprets a C-contiguous array's memory whatever its dtype), and
@@ -38,11 +43,16 @@ from .. import _native as nat
 WRONG_LIB = "Wrong value set for permanent library."
 
 # plain ids served on the GPU; value = arithmetic mode passed to libgbperm
-PLAIN_LIBS = {0: "fp64", 6: "fp64", 7: "fp64", 8: "fp64", 10: "fp64", 11: "fp64", 20: "fp64", 21: "fast"}
+PLAIN_LIBS = {0: "fx", 6: "fp64", 7: "fp64", 8: "fx", 10: "fp64", 11: "fx", 20: "fp64", 21: "fast", 22: "fx"}
 # repeated ids served on the GPU (lib 9 constructs but cannot calculate)
-REPEATED_LIBS = {0: "fp64", 1: "fp64", 6: "fp64", 7: "fp64", 8: "fp64", 20: "fp64", 21: "fast"}
+REPEATED_LIBS = {0: "fp64", 1: "fx", 6: "fp64", 7: "fp64", 8: "fx", 20: "fp64", 21: "fast", 22: "fx"}
 REPEATED_CONSTRUCT_ONLY = {9}
-BACKENDS = ("fp64", "fast")
+BACKENDS = ("fp64", "fast", "fx")
+
+
+def _batched_mode(mode):
+    # the batched launches have no integer-mantissa product
+    return "fp64" if mode == "fx" else mode
 
 # lib 0 (ChinHuhPermanentCalculator) evaluates the Chin-Huh form of the sum
 # (CChinHuhPermanentCalculator.cpp:48-201) on the same kernels
@@ -51,7 +61,7 @@ REPEATED_FORM = {0: "chinhuh"}
 
 def _check_backend(backend):
     if backend is not None and backend not in BACKENDS:
-        raise ValueError(f"unknown backend {backend!r}: expected None, 'fp64' or 'fast'")
+        raise ValueError(f"unknown backend {backend!r}: expected None, 'fp64', 'fx' or 'fast'")
     return backend
 
 
@@ -85,7 +95,7 @@ class GlynnPermanentCalculator_wrapper:
     def calculate(self):
         mode = self.backend or PLAIN_LIBS[self.lib]
         if isinstance(self._matrix, list):
-            return nat.perm_batched([nat.as_matrix(m) for m in self._matrix], mode=mode)
+            return nat.perm_batched([nat.as_matrix(m) for m in self._matrix], mode=_batched_mode(mode))
         if self.lib in (10, 11):
             a = nat.as_matrix(self._matrix)
             if a.shape[0] != a.shape[1] and a.size > 0:
@@ -136,7 +146,7 @@ class ChinHuhPermanentCalculator_wrapper:
                     row = [(fixed_in, out) for out in outs[i]]
                 shape.append(len(row))
                 pairs.extend(row)
-            vals = nat.perm_repeated_many(self._matrix, pairs, mode=mode)
+            vals = nat.perm_repeated_many(self._matrix, pairs, mode=_batched_mode(mode))
             res, k = [], 0
             for n in shape:
                 res.append(vals[k:k + n])
@@ -238,6 +248,13 @@ class GB300FastRepeatedPermanentCalculator(RepeatedPermanentCalculator):
         super().__init__(21, matrix, input_state, output_state, backend=backend)
 
 
+class GB300FxRepeatedPermanentCalculator(RepeatedPermanentCalculator):
+    """New id 22: GB300 integer-mantissa product (at least FP64 accuracy)."""
+
+    def __init__(self, matrix, input_state, output_state, *, backend=None):
+        super().__init__(22, matrix, input_state, output_state, backend=backend)
+
+
 class GlynnPermanent(GlynnPermanentCalculator_wrapper):
     def __init__(self, matrix, *, backend=None):
         super().__init__(matrix, 0, backend=backend)
@@ -295,6 +312,13 @@ class GB300FastPermanent(GlynnPermanentCalculator_wrapper):
 
     def __init__(self, matrix, *, backend=None):
         super().__init__(matrix, 21, backend=backend)
+
+
+class GB300FxPermanent(GlynnPermanentCalculator_wrapper):
+    """New id 22: GB300 integer-mantissa product (at least FP64 accuracy)."""
+
+    def __init__(self, matrix, *, backend=None):
+        super().__init__(matrix, 22, backend=backend)
 
 
 __all__: List[str] = [n for n in dir() if n[0].isupper()]

@@ -125,3 +125,28 @@ def test_fx_at_least_as_accurate_as_fp64():
             errs[mode].append(orc.rel_err(nat.perm(A, mode=mode), q))
     rms = {m: float(np.sqrt(np.mean(np.square(e)))) for m, e in errs.items()}
     assert rms["fx"] <= rms["fp64"], rms
+
+
+def test_dropin_ids_route_to_fx():
+    # id 22 and the reference's long-double ids (plain 0, 8, 11; repeated
+    # 1, 8) run the integer-mantissa product; lists under "fx" run the
+    # batched launches in FP64
+    from piquassoboost_gb300.sampling import Boson_Sampling_Utilities as bsu
+    from piquassoboost_gb300.workloads import haar_unitary, repeated_instance
+
+    A = haar_block(14, seed=14)
+    v = nat.perm(A, mode="fx")
+    for cls in (bsu.GB300FxPermanent, bsu.GlynnPermanent, bsu.BBFGPermanentLongDouble,
+                bsu.GlynnPermanentSimpleLongDouble):
+        assert cls(A).calculate() == v, cls.__name__
+    assert bsu.BBFGPermanentDouble(A, backend="fx").calculate() == v
+    U, cin, rout = repeated_instance(seed=5, modes=16, photons=8, max_mult=3)
+    r = nat.perm_repeated(U, cin, rout, mode="fx")
+    for cls in (bsu.GB300FxRepeatedPermanentCalculator, bsu.GlynnRepeatedPermanentCalculator,
+                bsu.BBFGRepeatedPermanentCalculatorLongDouble):
+        assert cls(U, cin, rout).calculate() == r, cls.__name__
+    mats = [haar_block(k, seed=k) for k in (6, 9, 12)]
+    got = bsu.GB300FxPermanent(mats).calculate()
+    for m, g in zip(mats, got):
+        ref = nat.perm(m, mode="fp64")
+        assert abs(g - ref) <= TOL * abs(ref)
