@@ -50,12 +50,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "repeated", "batched", "grad", "pmf", "mesh"],
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "repeated", "batched", "grad", "pmf", "mesh", "sampler"],
                     help="plain: single n x n Haar block (default); repeated: 60-mode / 30-photon "
                          "multiplicity permanent; batched: 4096 uneven k=8..28 permanents in one launch "
                          "(--batch-count, --batch-kmax); "
                          "grad: permanent + full gradient; pmf: one 60-mode / 30-photon boson-sampling "
-                         "probability layer; mesh: 512-term Clements-mesh log-likelihood, forward + backward")
+                         "probability layer; mesh: 512-term Clements-mesh log-likelihood, forward + backward; "
+                         "sampler: seeded boson samples, 40 modes / 20 photons")
     ap.add_argument("--n", type=int, default=36)
     ap.add_argument("--mode", default=None, choices=["fx", "fast", "fp64"],
                     help="arithmetic of the product: fx (integer mantissas, at least FP64 accuracy; the "
@@ -73,9 +75,9 @@ def parse():
     if args.batch_count < 1 or not 8 <= args.batch_kmax <= 32:
         ap.error("--batch-count must be >= 1 and --batch-kmax in 8..32")
     if args.mode is None:
-        args.mode = "fx" if args.workload == "plain" else "fp64"
-    if args.mode == "fx" and args.workload != "plain":
-        ap.error("--mode fx: the integer-mantissa product serves the plain workload")
+        args.mode = "fx" if args.workload in ("plain", "repeated", "batched") else "fp64"
+    if args.mode == "fx" and args.workload not in ("plain", "repeated", "batched"):
+        ap.error("--mode fx: the integer-mantissa product serves the plain, repeated and batched workloads")
     return args
 
 
@@ -107,6 +109,9 @@ def workload_desc(args) -> str:
     if args.workload == "pmf":
         return ("boson-sampling pmf layer: 60-mode Haar, one input photon in modes 0-29, a seeded "
                 "uniform-multinomial sample of 29 photons; 30 leave-one-out permanents per layer")
+    if args.workload == "sampler":
+        return ("boson samples: 40-mode Haar, one photon in each of modes 0-19, generalised Clifford & Clifford B "
+                "sampler with the reference's mt19937 stream (seeded); one sample per step")
     if args.workload == "mesh":
         return ("512 terms log|perm(U_S)|^2, 12 photons in a 40-mode Clements mesh (seeded uniform "
                 "phases, seeded mode sets), forward + backward to the 1560 phases")
@@ -541,7 +546,8 @@ def run_secondary(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    fn = {"repeated": _repeated, "batched": _batched, "grad": _grad, "pmf": _pmf, "mesh": _mesh}[args.workload]
+    fn = {"repeated": _repeated, "batched": _batched, "grad": _grad, "pmf": _pmf, "mesh": _mesh,
+          "sampler": _sampler}[args.workload]
     rc = fn(args, rank, world, torch)
     if world > 1:
         import torch.distributed as dist
@@ -602,14 +608,131 @@ def _repeated(args, rank, world, torch):
               {"workload": workload_desc(args), "arith": mode,
                "l2": "inputs < 100 KB; compute-bound, no flush"},
               _roof(flops / args.steps, statistics.mean(kms), peak,
-                    "repeated_df_kernel" if mode == "fast" else "repeated_kernel"),
+                    {"fast": "repeated_df_kernel", "fx": "repeated_fx_kernel"}.get(mode, "repeated_kernel")),
               cpu, {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": 60 * 60 * 16 + 2 * 60 * 8,
                     "d2h_bytes_per_step": 48}, (3 if mode == "fast" else 2) * args.steps, clocks=clocks)
     return 0
 
 
 # ---------------------------------------------------------------- batched
+def _batched_multiplicity(args, rank, world, torch):
+    """The batched configuration through the multiplicity plan
+    (gbperm_rep_batch_*): the instances' row and column draws as (input,
+    output) state pairs of the 100-mode unitary, the form the reference's
+    batched calculator takes, each walked as a repeated permanent in one
+    persistent launch; against sequential plain-GPU launches of the same
+    k x k submatrices in the same (integer-mantissa) arithmetic."""
+    from piquassoboost_gb300 import _native as nat
+    from piquassoboost_gb300.workloads import batched_index_sets, index_sets_to_states
+
+    count, kmax, modes = args.batch_count, args.batch_kmax, 100
+    U, rows, cols = batched_index_sets(count, seed=4 + 1000 * rank, modes=modes, kmin=8, kmax=kmax)
+    pairs = index_sets_to_states(rows, cols, modes)
+    mats = [np.ascontiguousarray(U[np.ix_(r, c)]) for r, c in zip(rows, cols)]
+    ks = np.array([len(r) for r in rows])
+    flops_plain = float(np.sum(8.0 * ks * 2.0 ** (ks - 1)))
+    peaks = {k: nat.probe_peak(k) for k in ("fp64", "imad_wide")}
+    lib = nat.load()
+    t_plan = time.perf_counter()
+    plan = nat.RepBatchPlan(U, pairs)
+    t_plan = time.perf_counter() - t_plan
+    info = plan.info()
+    stream = torch.cuda.current_stream()
+    d_out = torch.zeros(2 * count, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
+    clocks = clk.stop()
+    kms = [a.elapsed_time(b) for a, b in ev]
+    value = world * count * args.steps / wall
+    got = d_out.cpu().numpy().reshape(-1, 2)
+    got = got[:, 0] + 1j * got[:, 1]
+    # e2e: the public host call a user makes for a list of state pairs
+    # (planning, upload, the persistent launch and the copy back), every step
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        nat.perm_repeated_many(U, pairs, mode="fx")
+    e2e = world * count * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
+    # sequential plain-GPU launches of the k x k submatrices, same arithmetic
+    dm = [torch.from_numpy(m).to("cuda") for m in mats]
+    ws_b = int(lib.gbperm_perm_workspace_size(kmax, kmax))
+    ws = torch.empty(ws_b, dtype=torch.uint8, device="cuda")
+    sout = torch.zeros(2 * count, dtype=torch.float64, device="cuda")
+    sp = _P(stream.cuda_stream)
+    for i in range(min(8, count)):  # warm the plain path
+        k = dm[i].shape[0]
+        nat.check(lib.gbperm_perm_dev(_P(dm[i].data_ptr()), k, k, k, nat.ARITH_FX64, _P(sout.data_ptr() + 16 * i),
+                                      None, _P(ws.data_ptr()), ws_b, sp))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i, m in enumerate(dm):
+        k = m.shape[0]
+        nat.check(lib.gbperm_perm_dev(_P(m.data_ptr()), k, k, k, nat.ARITH_FX64, _P(sout.data_ptr() + 16 * i),
+                                      None, _P(ws.data_ptr()), ws_b, sp))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    b = sout.cpu().numpy().reshape(-1, 2)
+    b = b[:, 0] + 1j * b[:, 1]
+    diff = float(np.max(np.abs(got - b) / np.abs(b)))
+    avg = statistics.mean(kms)
+    # roofline: the integer multiply-adds of the walked steps (12 per
+    # complex multiply; the plan's algorithmic flops count 6 per multiply)
+    ach = info["flops"] * 2.0 / (avg * 1e-3) / 1e12
+    roof = {"bound": "int", "achieved": ach, "peak": peaks["imad_wide"], "unit": "Tops/s",
+            "frac": ach / peaks["imad_wide"], "traffic": None, "kernel": "rep_batched_kernel",
+            "work_per_launch": f"{info['steps']:.4g} Gray steps of the instances' multiplicity forms "
+                               f"(the expanded k x k sums: {float(np.sum(2.0 ** (ks - 1))):.4g} steps)",
+            "peak_source": "mad.wide.s32 probe (gbperm_probe_peak kind 3), measured in this run",
+            "fp64_equivalent_tflops_of_expanded_work": flops_plain / (avg * 1e-3) / 1e12}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        orc = _oracle()
+        order = np.argsort(-ks)[::64]
+        t = time.perf_counter()
+        done_flops, nd = 0.0, 0
+        for i in order:
+            if time.perf_counter() - t > args.cpu_seconds:
+                break
+            orc.bbfg_repeated(U, pairs[i][0], pairs[i][1], prec=0)
+            done_flops += 8.0 * ks[i] * 2.0 ** (ks[i] - 1)
+            nd += 1
+        dt = time.perf_counter() - t
+        cpu = {"value": count / (dt * flops_plain / done_flops), "unit": "perm/s", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": f"{nd} size-stratified instances as repeated permanents (the reference's batched "
+                         f"calculator's form; C oracle, {os.cpu_count()} threads), scaled to the batch by their "
+                         f"expanded flops"}
+    if rank == 0:
+        _line(args, world, value, "perm/s", 1000 * wall / args.steps,
+              {"workload": workload_desc(args) + "; the draws as state pairs of the unitary (multiplicity form)",
+               "arith": "fx", "plan_build_s": t_plan, "items": info["items"],
+               "l2": "tables resident (< 50 MB); compute-bound"},
+              roof, cpu, {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": 16 * modes * modes + 16 * modes * count,
+                          "d2h_bytes_per_step": 16 * count}, 5 * args.steps,
+              {"sequential_plain_gpu": {"ms": seq_ms, "perm_per_s": count / (seq_ms * 1e-3),
+                                        "arith": "fx", "batched_speedup": seq_ms / avg,
+                                        "max_rel_diff_vs_batched": diff},
+               "steps_walked_over_expanded": info["steps"] / float(np.sum(2.0 ** (ks - 1))),
+               "kernel_ms": kms}, clocks=clocks)
+    plan.close()
+    return 0
+
+
 def _batched(args, rank, world, torch):
+    if args.mode == "fx":
+        return _batched_multiplicity(args, rank, world, torch)
     from piquassoboost_gb300 import _native as nat
     from piquassoboost_gb300.workloads import batched_instances, haar_block, repeated_instance
 
@@ -971,6 +1094,60 @@ def _mesh(args, rank, world, torch):
     return 0
 
 
+# ---------------------------------------------------------------- sampler
+_SAMPLER_MODES, _SAMPLER_PHOTONS = 40, 20
+
+
+def _sampler_instance(seed):
+    from piquassoboost_gb300.workloads import haar_unitary
+    U = haar_unitary(_SAMPLER_MODES, seed)
+    inp = np.zeros(_SAMPLER_MODES, dtype=np.int64)
+    inp[:_SAMPLER_PHOTONS] = 1
+    return U, inp
+
+
+def _sampler(args, rank, world, torch):
+    """Seeded boson samples through the native sampler (gbperm_sampler_*):
+    one sample (20 probability layers, each one GPU Gray sweep) per step."""
+    from piquassoboost_gb300 import _native as nat
+
+    U, inp = _sampler_instance(args.seed + 1000 * rank)
+    peak = nat.probe_peak("fp64")
+    smp = nat.Sampler(U, seed=args.seed + rank, mode="fp64")
+    first = smp.simulate(inp, 1)                 # the oracle's first sample is checked below
+    for _ in range(max(0, args.warmup - 1)):
+        smp.simulate(inp, 1)
+    st = nat.Stats()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    smp.simulate(inp, args.steps, stats=st)
+    wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
+    clocks = clk.stop()
+    value = world * args.steps / wall
+    cpu, match = None, None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        orc = _oracle()
+        t = time.perf_counter()
+        ref = orc.sample_b(U, inp, 1, args.seed + rank, threads=0)
+        dt = time.perf_counter() - t
+        match = bool(np.array_equal(ref[0], first[0]))
+        cpu = {"value": 1.0 / dt, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"one seeded sample (the oracle's C restatement of the reference sampler, pmf layers on "
+                         f"{os.cpu_count()} threads)"}
+    if rank == 0:
+        _line(args, world, value, "samples/s", 1000 * wall / args.steps,
+              {"workload": workload_desc(args), "arith": "fp64", "l2": "inputs < 30 KB; compute- and launch-bound"},
+              _roof(st.flops, st.kernel_ms, peak, "pmf_kernel (all layers of the timed samples)"),
+              cpu, {"value": value, "unit": "samples/s",
+                    "h2d_bytes_per_step": _SAMPLER_PHOTONS * (_SAMPLER_MODES * _SAMPLER_MODES * 16 + 32 * _SAMPLER_MODES),
+                    "d2h_bytes_per_step": _SAMPLER_PHOTONS * _SAMPLER_MODES * 24},
+              st.launches, {"gpu_kernel_ms": st.kernel_ms, "first_sample_matches_oracle": match}, clocks=clocks)
+    smp.close()
+    return 0
+
+
 def _reference_secondary(args, world):
     from piquassoboost_gb300.workloads import batched_instances, haar_block, repeated_instance
 
@@ -1029,6 +1206,15 @@ def _reference_secondary(args, world):
         v = args.steps / sum(ts)
         unit, sample = "(loss+grad)/s", ("32 of the 512 terms per step (permanent + 144 minors each, one thread per "
                                          "term), scaled to the batch")
+    elif args.workload == "sampler":
+        U, inp = _sampler_instance(args.seed)
+        ts = []
+        for q in range(args.steps):
+            t = time.perf_counter()
+            orc.sample_b(U, inp, 1, args.seed + q, threads=0)
+            ts.append(time.perf_counter() - t)
+        v = args.steps / sum(ts)
+        unit, sample = "samples/s", "one seeded sample per step (C restatement of the reference sampler)"
     elif args.workload == "pmf":
         from piquassoboost_gb300.workloads import pmf_layer_instance
 

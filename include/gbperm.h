@@ -152,10 +152,36 @@ int gbperm_perm_chinhuh(const double* A, int64_t rows, int64_t cols, int64_t ld,
  * (ChinHuhPermanentCalculator_Wrapper.hpp:233-323).  Pairs whose plain
  * expansion is not much longer than their mixed-radix Gray code are expanded
  * and share one persistent batched launch; the others run as repeated
- * launches.  out: 2 * count doubles.  Any invalid pair fails the call. */
+ * launches.  With GBPERM_ARITH_FX64 every pair runs in one persistent
+ * multiplicity launch (gbperm_rep_batch_*) when each has at most 40
+ * occupied modes on its product side.  out: 2 * count doubles.  Any invalid
+ * pair fails the call. */
 int gbperm_perm_repeated_batched(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mults,
                                  int64_t ncol, const int64_t* row_mults, int64_t nrow, int64_t count, int arith,
                                  double* out, gbperm_stats* stats);
+
+/* A reusable plan for many repeated permanents of one interferometer, all
+ * in one persistent launch (the same inputs as gbperm_perm_repeated_batched;
+ * replaces BatchednPermanentCalculator::calculate, BatchedPermanentCalculator
+ * .cpp:109-296, which evaluates each pair through adaptInterferometer and the
+ * repeated calculator, :118-143).  Every pair keeps its multiplicities: the
+ * mixed-radix Gray code of its cheaper side, so a pair with repeated modes
+ * walks far fewer steps than its expanded matrix would.  Integer-mantissa
+ * product only (arith must be GBPERM_ARITH_FX64); at most 40 occupied modes
+ * on a pair's product side (GBPERM_ERR_TOO_LARGE otherwise).  create plans
+ * every pair on the host, uploads the interferometer's submatrices and
+ * tables, and captures the host run as a CUDA graph.  run: host output
+ * (2 * count doubles, caller's order); run_dev: the same kernels enqueued on
+ * `stream` writing 2 * count doubles to device memory.  info: Gray steps,
+ * algorithmic flops and work items of the plan. */
+typedef struct gbperm_rep_batch gbperm_rep_batch;
+int gbperm_rep_batch_create(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mults,
+                            int64_t ncol, const int64_t* row_mults, int64_t nrow, int64_t count, int arith,
+                            gbperm_rep_batch** out);
+int gbperm_rep_batch_run(gbperm_rep_batch* plan, double* out, gbperm_stats* stats);
+int gbperm_rep_batch_run_dev(gbperm_rep_batch* plan, void* d_out, void* stream);
+int gbperm_rep_batch_info(const gbperm_rep_batch* plan, double* steps, double* flops, int64_t* items);
+void gbperm_rep_batch_destroy(gbperm_rep_batch* plan);
 
 /* ------------------------------------------------- batched permanents */
 /* Many plain permanents of uneven sizes in one persistent launch (a CUDA

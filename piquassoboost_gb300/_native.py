@@ -103,6 +103,13 @@ _SIGNATURES = [
     ("gbperm_compute_pmf", ctypes.c_int, [_P, _I64, _I64, _P, _P, ctypes.c_int, _P, _P, _P]),
     ("gbperm_perm_repeated_batched", ctypes.c_int,
      [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _I64, ctypes.c_int, _P, _P]),
+    ("gbperm_rep_batch_create", ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _I64, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbperm_rep_batch_run", ctypes.c_int, [_P, _P, _P]),
+    ("gbperm_rep_batch_run_dev", ctypes.c_int, [_P, _P, _P]),
+    ("gbperm_rep_batch_info", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                              ctypes.POINTER(_I64)]),
+    ("gbperm_rep_batch_destroy", None, [_P]),
     ("gbperm_sampler_create", ctypes.c_int, [_P, _I64, _I64, ctypes.c_uint64, ctypes.c_int,
                                               ctypes.POINTER(ctypes.c_void_p)]),
     ("gbperm_sampler_set_matrix", ctypes.c_int, [_P, _P, _I64, _I64]),
@@ -359,6 +366,57 @@ def compute_pmf(interferometer, sample, current_input, mode="fp64", stats: Stats
     return pmf, add
 
 
+class RepBatchPlan:
+    """A reusable persistent-launch plan for many repeated permanents of one
+    interferometer (gbperm_rep_batch_*): pairs of (input_state,
+    output_state) over the matrix's columns and rows, integer-mantissa
+    product."""
+
+    def __init__(self, matrix, pairs):
+        lib = load()
+        a = as_matrix(matrix)
+        rows, cols = a.shape
+        ins = [as_state(i) for i, _ in pairs]
+        outs = [as_state(o) for _, o in pairs]
+        ncol = max([len(x) for x in ins] + [0])
+        nrow = max([len(x) for x in outs] + [0])
+        cm = np.zeros((len(pairs), ncol), dtype=np.int64)
+        rm = np.zeros((len(pairs), nrow), dtype=np.int64)
+        for k, (i, o) in enumerate(zip(ins, outs)):
+            cm[k, :len(i)] = i
+            rm[k, :len(o)] = o
+        self.count = len(pairs)
+        self._a = a
+        self._h = ctypes.c_void_p()
+        check(lib.gbperm_rep_batch_create(a.ctypes.data_as(_P), rows, cols, cols, cm.ctypes.data_as(_P), ncol,
+                                          rm.ctypes.data_as(_P), nrow, self.count, ARITH_FX64, ctypes.byref(self._h)))
+
+    def run(self, stats: Stats | None = None) -> np.ndarray:
+        out = np.zeros(2 * max(self.count, 1))
+        check(load().gbperm_rep_batch_run(self._h, out.ctypes.data_as(_P),
+                                          ctypes.byref(stats) if stats is not None else None))
+        return out[0:2 * self.count:2] + 1j * out[1:2 * self.count:2]
+
+    def run_dev(self, d_out_ptr: int, stream_ptr: int | None = None):
+        check(load().gbperm_rep_batch_run_dev(self._h, _P(d_out_ptr), _P(stream_ptr or 0)))
+
+    def info(self):
+        steps, flops, items = ctypes.c_double(), ctypes.c_double(), _I64()
+        check(load().gbperm_rep_batch_info(self._h, ctypes.byref(steps), ctypes.byref(flops), ctypes.byref(items)))
+        return {"steps": steps.value, "flops": flops.value, "items": items.value}
+
+    def close(self):
+        if self._h:
+            load().gbperm_rep_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Sampler:
     """Handle of a native boson sampler (gbperm_sampler_*): the generalised
     Clifford & Clifford B form over GPU pmf layers, with the reference's
@@ -419,8 +477,36 @@ def probe_peak(kind: str) -> float:
     return v.value
 
 
-def perm_grad(matrix, stats: Stats | None = None):
-    """Permanent and full gradient G[k, l] = dperm/da_kl (host buffers)."""
+_grad_lock = threading.Lock()
+
+
+class grad_arithmetic:
+    """Context manager selecting the gradient sweep's product (the library's
+    process-wide option "grad.arith"): "fast" (double-float, recomputed with
+    the integer-mantissa product on the device when its range check fails or
+    its error estimate is above 1e-10; the default) or "fx" (integer-mantissa
+    product throughout).  Python threads that switch it are serialised."""
+
+    def __init__(self, mode):
+        self.arith = arith_of(mode)
+        if self.arith not in (ARITH_DF32, ARITH_FX64):
+            raise ValueError("the gradient runs the 'fast' or the 'fx' product")
+
+    def __enter__(self):
+        _grad_lock.acquire()
+        self.prev = get_option("grad.arith")
+        set_option("grad.arith", self.arith)
+        return self
+
+    def __exit__(self, *exc):
+        set_option("grad.arith", self.prev)
+        _grad_lock.release()
+        return False
+
+
+def perm_grad(matrix, stats: Stats | None = None, mode: str | None = None):
+    """Permanent and full gradient G[k, l] = dperm/da_kl (host buffers).
+    mode None keeps the current gradient arithmetic (see grad_arithmetic)."""
     lib = load()
     a = as_matrix(matrix)
     n = a.shape[0]
@@ -429,12 +515,20 @@ def perm_grad(matrix, stats: Stats | None = None):
     require_device()
     perm = np.zeros(2)
     g = np.zeros((n, n), dtype=np.complex128)
-    check(lib.gbperm_perm_grad(a.ctypes.data_as(_P), n, n, perm.ctypes.data_as(_P), None,
-                               g.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
+
+    def call():
+        check(lib.gbperm_perm_grad(a.ctypes.data_as(_P), n, n, perm.ctypes.data_as(_P), None,
+                                   g.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
+
+    if mode is None:
+        call()
+    else:
+        with grad_arithmetic(mode):
+            call()
     return complex(perm[0], perm[1]), g
 
 
-def perm_grad_batched(matrices, stats: Stats | None = None):
+def perm_grad_batched(matrices, stats: Stats | None = None, mode: str | None = None):
     """Permanents and full gradients of a batch of equal-size square matrices
     (host buffers, one set of launches): returns (perms[count], grads[count, n, n])."""
     lib = load()
@@ -444,6 +538,15 @@ def perm_grad_batched(matrices, stats: Stats | None = None):
     count, n = a.shape[0], a.shape[1]
     perms = np.zeros(count, dtype=np.complex128)
     grads = np.zeros((count, n, n), dtype=np.complex128)
-    check(lib.gbperm_perm_grad_batched(a.ctypes.data_as(_P), n, count, perms.ctypes.data_as(_P),
-                                       grads.ctypes.data_as(_P), ctypes.byref(stats) if stats is not None else None))
+
+    def call():
+        check(lib.gbperm_perm_grad_batched(a.ctypes.data_as(_P), n, count, perms.ctypes.data_as(_P),
+                                           grads.ctypes.data_as(_P),
+                                           ctypes.byref(stats) if stats is not None else None))
+
+    if mode is None:
+        call()
+    else:
+        with grad_arithmetic(mode):
+            call()
     return perms, grads

@@ -23,6 +23,7 @@ struct Options {
     std::atomic<int64_t> batched_item_log2{0};
     std::atomic<int64_t> df_escalate{1};
     std::atomic<int64_t> plain_fx_group{0};
+    std::atomic<int64_t> grad_arith{1};
     std::atomic<int64_t>* find(const char* key) {
         if (!std::strcmp(key, "plain.seg_log2")) return &plain_seg_log2;
         if (!std::strcmp(key, "plain.grid")) return &plain_grid;
@@ -32,6 +33,7 @@ struct Options {
         if (!std::strcmp(key, "batched.item_log2")) return &batched_item_log2;
         if (!std::strcmp(key, "df.escalate")) return &df_escalate;
         if (!std::strcmp(key, "plain.fx_group")) return &plain_fx_group;
+        if (!std::strcmp(key, "grad.arith")) return &grad_arith;
         return nullptr;
     }
 };

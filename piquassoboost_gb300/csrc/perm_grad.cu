@@ -39,6 +39,7 @@
 
 #include "gbperm.h"
 #include "gbperm_capi_internal.h"
+#include "gbperm_fx.cuh"
 
 namespace gbperm {
 
@@ -96,7 +97,11 @@ struct GradArgs {
     int seg_log2;              // each walk covers 2^seg_log2 Gray steps
     unsigned long long nseg;   // walks per matrix
     const int* df_info;        // per matrix {boost, ok}
-    float4* warp_g;            // per matrix and warp: n x n complex double-float tiles (re_h, re_l, im_h, im_l)
+    float4* warp_g;            // per matrix and warp: n x n complex double-float tiles (re_h, re_l, im_h, im_l);
+                               // the integer-mantissa twin stores double2 tiles (16 bytes too) here
+    double* warp_s2 = nullptr; // double-float sweep: per matrix and warp, sum of |term 2^40|^2
+    const int* gate = nullptr; // integer-mantissa twin: run only for matrices whose gate[2 i + 1]
+                               // is 0 (the double-float product is not in use); null: always
 };
 
 // Reduce-scatter of v[0..CPL) over the kGroups walks of a warp (lanes with
@@ -179,6 +184,12 @@ __global__ void __launch_bounds__(kThreads, 3) grad_kernel(GradArgs p) {
     const unsigned long long Lsteps = 1ull << L;
     long long cre[CPL], cim[CPL];
     cf Q[CPL];
+    // this thread's sum of |term 2^40|^2, in shared memory: a register pair
+    // more would make the 8-column shape spill
+    __shared__ double s_s2t[kThreads];
+    __shared__ float s_s2f[kThreads];  // the same since the last fold, in float
+    s_s2t[threadIdx.x] = 0.0;
+    s_s2f[threadIdx.x] = 0.f;
 
     auto g_add = [&](int r, const cf& s) {
         if (writer) {
@@ -290,6 +301,14 @@ __global__ void __launch_bounds__(kThreads, 3) grad_kernel(GradArgs p) {
                 const cf o1 = shfl_xor_cf(part, 1);
                 const cf pair = cf_mul(part, o1);
                 const cf o23 = shfl_xor_cf(pair, 2);
+                // |term|^2 = |pair|^2 |o23|^2, each factor scaled by 2^20 (the
+                // range boost centres the terms near 2^-40), for the error
+                // estimate: one walk's lane g = 0 adds it
+                if (g == 0) {
+                    const float ar = pair.rh * 0x1p20f, ai = pair.ih * 0x1p20f;
+                    const float br = o23.rh * 0x1p20f, bi = o23.ih * 0x1p20f;
+                    s_s2f[threadIdx.x] = fmaf(fmaf(ar, ar, ai * ai), fmaf(br, br, bi * bi), s_s2f[threadIdx.x]);
+                }
                 cf seed = cf_scale_sign(cf_mul(o1, o23), sbit);  // s(delta) folded in once
                 seed.rh = __fmul_rn(seed.rh, wgt);
                 seed.rl = __fmul_rn(seed.rl, wgt);
@@ -311,6 +330,8 @@ __global__ void __launch_bounds__(kThreads, 3) grad_kernel(GradArgs p) {
                     }
                 }
             }
+            s_s2t[threadIdx.x] += (double)s_s2f[threadIdx.x];
+            s_s2f[threadIdx.x] = 0.f;
             // end of a chunk (or of the walk): fold Q into every row of G,
             // G[r] += delta_r(kend-1) * Q, then restart Q
             const unsigned long long idx = i0 + kend - 1;
@@ -334,6 +355,282 @@ __global__ void __launch_bounds__(kThreads, 3) grad_kernel(GradArgs p) {
         const int rr = e / n, j = e % n;
         outg[(hot0 + rr) * n + j] = G[rr * NP + j];
     }
+    if (p.warp_s2) {
+        const double s2 = warp_sum_d(s_s2t[threadIdx.x]);
+        if (lane == 0) p.warp_s2[slot] = s2;
+    }
+}
+
+// ------------------------------------------------ integer-mantissa twin
+// The same sweep with the product on 64-bit integer mantissas
+// (gbperm_fx.cuh): prefix, partial, butterfly and suffix products as above,
+// each multiply keeping 55-57 significant bits; the running sums Q, the
+// reduce-scatter of the flipping row and the G tiles in double (FP64 pipe).
+// Padded columns hold the exact column value 1 (2^62 in the fixed point),
+// which the integer multiply passes through to within half a unit.  It is
+// the double-float sweep's fallback for matrices whose range check fails or
+// whose error estimate is above 1e-10 (gate), and the whole sweep when the
+// integer-mantissa product is requested (no gate).
+template <int CPL>
+__device__ __forceinline__ double2 reduce_scatter_d(double2 (&v)[CPL]) {
+    int width = CPL;
+#pragma unroll
+    for (int m = kGroups / 2; m >= 1; m >>= 1) {
+        if (width > 1) {
+            const int half = width / 2;
+#pragma unroll
+            for (int c = 0; c < CPL / 2; ++c)
+                if (c < half) {
+                    v[c].x += __shfl_xor_sync(0xffffffffu, v[c + half].x, m * kGroup);
+                    v[c].y += __shfl_xor_sync(0xffffffffu, v[c + half].y, m * kGroup);
+                }
+            width = half;
+        } else {
+            v[0].x += __shfl_xor_sync(0xffffffffu, v[0].x, m * kGroup);
+            v[0].y += __shfl_xor_sync(0xffffffffu, v[0].y, m * kGroup);
+        }
+    }
+    return v[0];
+}
+
+template <int CPL>
+__global__ void __launch_bounds__(kThreads, 3) grad_fx_kernel(GradArgs p) {
+    constexpr int NP = CPL * kGroup;
+    constexpr long long kOne = 1ll << GBPERM_FIX_BITS;  // the column value 1
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    longlong2* s_a2 = reinterpret_cast<longlong2*>(smem_raw);           // n x NP (interleaved)
+    double2* s_g = reinterpret_cast<double2*>(s_a2 + p.n * NP);         // (warps) x kHot x NP
+    const int n = p.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane % kGroup, grp = lane / kGroup;
+    const int j0 = g * CPL;
+    const size_t inst = blockIdx.y;
+    if (p.gate && p.gate[2 * inst + 1] != 0) return;  // the double-float result stands
+    const longlong2* A1 = p.a1 + inst * n * n;
+    const longlong2* A2 = p.a2 + inst * n * n;
+    const int hot0 = n > kHot ? n - kHot : 0;
+    double2* G = s_g + (size_t)warp * kHot * NP;
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (kThreads / 32);
+    const unsigned long long gwarp = (unsigned long long)blockIdx.x * (kThreads / 32) + warp;
+    const size_t slot = inst * warps_total + gwarp;
+    double2* outg = reinterpret_cast<double2*>(p.warp_g) + slot * n * n;
+    for (int e = threadIdx.x; e < n * NP; e += blockDim.x) {
+        const int r = e / NP, q = e % NP;
+        const int j = (q % kGroup) * CPL + q / kGroup;
+        s_a2[e] = j < n ? A2[r * n + j] : make_longlong2(0, 0);
+    }
+    for (int e = lane; e < kHot * NP; e += 32) G[e] = make_double2(0.0, 0.0);
+    for (int e = lane; e < hot0 * n; e += 32) outg[e] = make_double2(0.0, 0.0);
+    __syncthreads();
+    const int pm = perm_mask<CPL>(grp);
+    const int my_col = j0 + pm;
+    const bool writer = (grp & (kGroups / CPL - 1)) == 0 && my_col < n;
+    const int L = p.seg_log2;
+    const unsigned long long Lsteps = 1ull << L;
+    long long cre[CPL], cim[CPL];
+    double2 Q[CPL];
+
+    auto g_add = [&](int r, const double2& v) {
+        if (writer) {
+            double2* dst = r >= hot0 ? G + (r - hot0) * NP + my_col : outg + r * n + my_col;  // r warp-uniform
+            double2 gg = *dst;
+            gg.x += v.x;
+            gg.y += v.y;
+            *dst = gg;
+        }
+    };
+
+    for (unsigned long long wb = gwarp * kGroups; wb < p.nseg; wb += warps_total * kGroups) {
+        const unsigned long long s_raw = wb + grp;
+        const bool active = s_raw < p.nseg;
+        const unsigned long long i0 = (active ? s_raw : 0ull) << L;
+        const unsigned long long g0 = i0 ^ (i0 >> 1);
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            const int j = j0 + (c ^ pm);
+            const longlong2 v = j < n ? A1[j] : make_longlong2(kOne, 0);
+            cre[c] = v.x;
+            cim[c] = v.y;
+            Q[c] = make_double2(0.0, 0.0);
+        }
+        for (int r = 1; r < n; ++r) {
+            const long long m = -(long long)((g0 >> (n - 1 - r)) & 1ull);
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                const int j = j0 + (c ^ pm);
+                const longlong2 v = j < n ? A1[r * n + j] : make_longlong2(0, 0);
+                cre[c] += (v.x ^ m) - m;
+                cim[c] += (v.y ^ m) - m;
+            }
+        }
+        unsigned long long sbit = (unsigned long long)(__popcll(g0) & 1) << 63;
+        for (unsigned long long k0 = 0; k0 < Lsteps; k0 += kChunk) {
+            const unsigned long long kend = k0 + kChunk < Lsteps ? k0 + kChunk : Lsteps;
+            for (unsigned long long k = k0; k < kend; ++k) {
+                const unsigned long long idx = i0 + k;
+                if (k != 0) {
+                    const int b = __ffsll((long long)k) - 1;                  // warp-uniform
+                    const int r = n - 1 - b;                                    // the row that flips
+                    const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;  // new delta_r = -1
+                    const bool mid = b + 1 >= L;
+                    double2 v[CPL];
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        v[c] = Q[c];
+                        if (mid) {
+                            const double f = sub ? 2.0 : -2.0;
+                            v[c].x *= f;
+                            v[c].y *= f;
+                        }
+                    }
+                    double2 sv = reduce_scatter_d<CPL>(v);
+                    if (!mid) {
+                        const double f = sub ? 2.0 : -2.0;
+                        sv.x *= f;
+                        sv.y *= f;
+                    }
+                    g_add(r, sv);
+                    const long long m = sub ? -1ll : 0ll;
+                    const longlong2* a = s_a2 + r * NP + g;
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v2 = a[(c ^ pm) * kGroup];
+                        cre[c] += (v2.x ^ m) - m;
+                        cim[c] += (v2.y ^ m) - m;
+                    }
+                    sbit ^= 0x8000000000000000ull;
+                }
+                // prefix products pre[c] = prod_{c' < c} x_c' (normalised,
+                // shift counts spre), the lane's partial product `part`
+                fxl pre[CPL];
+                int spre[CPL];
+                fxl part;
+                int spart;
+                if (CPL > 1) {
+                    spre[1] = fx_norm_col(cre[0], cim[0], pre[1]);
+#pragma unroll
+                    for (int c = 2; c < CPL; ++c) {
+                        long long rr, ri;
+                        fx_mul(pre[c - 1], fx_col(cre[c - 1], cim[c - 1]), rr, ri);
+                        spre[c] = spre[c - 1] - 1 + fx_norm(rr, ri, pre[c]);
+                    }
+                    long long rr, ri;
+                    fx_mul(pre[CPL - 1], fx_col(cre[CPL - 1], cim[CPL - 1]), rr, ri);
+                    spart = spre[CPL - 1] - 1 + fx_norm(rr, ri, part);
+                } else {
+                    spart = fx_norm_col(cre[0], cim[0], part);
+                }
+                // product of the other three lanes' partials (fx_mul is
+                // symmetric, so partners compute identical values)
+                const fxl o1 = shfl_xor_fxl(part, 1);
+                const int so1 = __shfl_xor_sync(0xffffffffu, spart, 1);
+                fxl pair;
+                int spair;
+                {
+                    long long rr, ri;
+                    fx_mul(part, o1, rr, ri);
+                    spair = spart + so1 - 1 + fx_norm(rr, ri, pair);
+                }
+                const fxl o23 = shfl_xor_fxl(pair, 2);
+                const int so23 = __shfl_xor_sync(0xffffffffu, spair, 2);
+                fxl suf;
+                int ssuf;
+                {
+                    long long rr, ri;
+                    fx_mul(o1, o23, rr, ri);
+                    ssuf = so1 + so23 - 1 + fx_norm(rr, ri, suf);
+                }
+                // W_c = pre[c] * (others) * prod_{c' > c} x_c', signed, into Q
+#pragma unroll
+                for (int c = CPL - 1; c >= 0; --c) {
+                    long long wr, wi;
+                    int sw;
+                    if (c == 0) {
+                        wr = fx_join(suf.rh, suf.rl);
+                        wi = fx_join(suf.ih, suf.il);
+                        sw = ssuf;
+                    } else {
+                        fx_mul(pre[c], suf, wr, wi);
+                        sw = spre[c] + ssuf - 1;
+                    }
+                    if (active) {
+                        const int e = -61 - sw;
+                        Q[c].x += __longlong_as_double(__double_as_longlong(fx_to_double(wr, e)) ^ (long long)sbit);
+                        Q[c].y += __longlong_as_double(__double_as_longlong(fx_to_double(wi, e)) ^ (long long)sbit);
+                    }
+                    if (c > 0) {
+                        long long rr, ri;
+                        fx_mul(suf, fx_col(cre[c], cim[c]), rr, ri);
+                        ssuf = ssuf - 1 + fx_norm(rr, ri, suf);
+                    }
+                }
+            }
+            // end of a chunk (or of the walk): G[r] += delta_r(kend-1) Q, restart Q
+            const unsigned long long idx = i0 + kend - 1;
+            const unsigned long long gray = idx ^ (idx >> 1);
+            for (int r = 0; r < n; ++r) {
+                const bool neg = r > 0 && ((gray >> (n - 1 - r)) & 1ull);
+                double2 v[CPL];
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) v[c] = neg ? make_double2(-Q[c].x, -Q[c].y) : Q[c];
+                g_add(r, reduce_scatter_d<CPL>(v));
+            }
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) Q[c] = make_double2(0.0, 0.0);
+        }
+    }
+    __syncwarp();
+    for (int e = lane; e < (n - hot0) * n; e += 32) {
+        const int rr = e / n, j = e % n;
+        outg[(hot0 + rr) * n + j] = G[rr * NP + j];
+    }
+}
+
+// Finalize stages of the twin: kFinWarps warp tiles per partial summed in
+// double in a fixed order, then the partials in double-double; the exponent
+// is the FP64 one (no boost).  Gated like the sweep.
+__global__ void grad_partial_fx_kernel(const double2* warp_g, int nwarps, int n, double2* part, const int* gate) {
+    const int ne = n * n;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const size_t inst = blockIdx.z;
+    if (gate && gate[2 * inst + 1] != 0) return;
+    warp_g += inst * nwarps * n * n;
+    part += inst * gridDim.y * ne;
+    const int w0 = blockIdx.y * kFinWarps;
+    const int w1 = min(w0 + kFinWarps, nwarps);
+    double re = 0.0, im = 0.0;
+    for (int w = w0; w < w1; ++w) {
+        const double2 v = warp_g[(size_t)w * n * n + e];
+        re += v.x;
+        im += v.y;
+    }
+    part[(size_t)blockIdx.y * ne + e] = make_double2(re, im);
+}
+
+__global__ void grad_finalize_fx_kernel(const double2* part, int nchunks, int n, const int* exp64, const int* col_e,
+                                        const int* row_k, const int* gate, double* grad) {
+    const int ne = n * n;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const size_t inst = blockIdx.y;
+    if (gate && gate[2 * inst + 1] != 0) return;
+    part += inst * nchunks * ne;
+    exp64 += inst;
+    col_e += inst * n;
+    row_k += inst * n;
+    grad += inst * 2 * n * n;
+    cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    for (int c = 0; c < nchunks; ++c) {
+        const double2 v = part[(size_t)c * ne + e];
+        acc.re = dd_add_d(acc.re, v.x);
+        acc.im = dd_add_d(acc.im, v.y);
+    }
+    const int l = e % n, k = e / n;
+    double r2[2];
+    write_result(acc, *exp64 - col_e[l] - row_k[k], r2, nullptr);
+    grad[2 * e] = r2[0];
+    grad[2 * e + 1] = r2[1];
 }
 
 // First finalize stage: element e of the gradient summed over kFinWarps
@@ -404,20 +701,37 @@ __device__ __forceinline__ dd two_prod(double a, double b) {
 // best-conditioned row is then summed in double-double (products exact by
 // FMA) with one term per lane, so the sweep needs no separate permanent
 // term.
+//
+// Two passes share it.  After the double-float sweep (est != null): a matrix
+// whose range check failed gets NaN here (its twin pass follows); otherwise
+// lane 0 also forms the relative rounding-error estimate of the sweep,
+//     sqrt(n) 2^-46 sqrt(sum |term 2^40|^2) 2^-40 / |perm 2^-exp|,
+// (the model of the forward double-float kernels; the gradient entries are
+// minors of the same matrix) and, when it is above 1e-10 and `escalate` is
+// set, clears df_info[1] so that the integer-mantissa twin queued behind
+// recomputes the gradient and the permanent.  After the twin (est == null):
+// matrices whose df_info[1] is set keep the double-float values (df_info
+// null: every matrix is the twin's).
 __global__ void grad_perm_kernel(const double2* A, long long ld, long long stride, int n, const double* grad,
-                                 const int* df_info, double* perm2, double* perm4) {
+                                 int* df_info, double* perm2, double* perm4, const double* warp_s2, int nwarps,
+                                 const int* exp_in, double* est, int escalate) {
     const size_t inst = blockIdx.x;
     const int k = threadIdx.x;
     A += inst * stride;
     grad += inst * 2 * n * n;
-    df_info += 2 * inst;
+    if (df_info) df_info += 2 * inst;
     perm2 += 2 * inst;
     if (perm4) perm4 += 4 * inst;
-    if (df_info[1] == 0) {
-        if (k == 0) {
-            perm2[0] = perm2[1] = nan("");
-            if (perm4) perm4[0] = perm4[1] = perm4[2] = perm4[3] = nan("");
+    if (est) {
+        if (df_info[1] == 0) {
+            if (k == 0) {
+                perm2[0] = perm2[1] = nan("");
+                if (perm4) perm4[0] = perm4[1] = perm4[2] = perm4[3] = nan("");
+                est[inst] = -1.0;
+            }
+            return;
         }
+    } else if (df_info && df_info[1] != 0) {
         return;
     }
     // condition estimate of every row's expansion in plain FP64 (it only
@@ -474,6 +788,18 @@ __global__ void grad_perm_kernel(const double2* A, long long ld, long long strid
             perm4[3] = s.im.lo;
         }
     }
+    if (est) {
+        // the sweep's sum of |term 2^40|^2 over the matrix's warps, in a fixed order
+        double q = 0.0;
+        for (int w = k; w < nwarps; w += 32) q += warp_s2[inst * nwarps + w];
+        q = warp_sum_d(q);
+        if (k == 0) {
+            const double mag = ldexp(hypot(s.re.hi, s.im.hi), -exp_in[inst]);
+            const double e = sqrt((double)n) * 0x1p-46 * sqrt(q) * 0x1p-40 / mag;
+            est[inst] = e;
+            if (escalate && !(e <= kDfEscalate)) df_info[1] = 0;
+        }
+    }
 }
 
 template <int CPL>
@@ -496,7 +822,9 @@ struct GradPlan {
 // Largest batch one launch takes (gridDim.y); larger batches are cut.
 constexpr int kMaxBatchLaunch = 65535;
 
-static GradPlan plan_grad(int n, int count) {
+// fx: plan for the integer-mantissa sweep alone (otherwise for the
+// double-float sweep, whose twin then runs on the same plan)
+static GradPlan plan_grad(int n, int count, bool fx = false) {
     GradPlan gp;
     gp.cpl = n <= 16 ? 4 : 8;
     gp.count = count;
@@ -505,13 +833,11 @@ static GradPlan plan_grad(int n, int count) {
     int sms = device_sms(dev);
     int nb = 0;
     size_t smem = gp.cpl == 4 ? grad_smem<4>(n) : grad_smem<8>(n);
-    if (gp.cpl == 4) {
-        allow_max_dynamic_smem((const void*)grad_kernel<4>);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, grad_kernel<4>, kThreads, smem);
-    } else {
-        allow_max_dynamic_smem((const void*)grad_kernel<8>);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, grad_kernel<8>, kThreads, smem);
-    }
+    const void* kern = gp.cpl == 4 ? (fx ? (const void*)grad_fx_kernel<4> : (const void*)grad_kernel<4>)
+                                   : (fx ? (const void*)grad_fx_kernel<8> : (const void*)grad_kernel<8>);
+    allow_max_dynamic_smem(kern);
+    allow_max_dynamic_smem(gp.cpl == 4 ? (const void*)grad_fx_kernel<4> : (const void*)grad_fx_kernel<8>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kThreads, smem);
     if (nb < 1) nb = 1;
     const long long grid_full = (long long)sms * nb;
     const long long gx_max = std::max(1ll, grid_full / std::max(1, count));
@@ -547,7 +873,7 @@ static GradPlan plan_grad(int n, int count) {
 }
 
 struct GradWs {
-    size_t a1, a2, exp, dfi, cole, rowk, warp_g, part, total;
+    size_t a1, a2, exp, exp64, dfi, cole, rowk, warp_g, part, warp_s2, est, total;
 };
 
 static GradWs grad_ws_layout(int n, const GradPlan& gp) {
@@ -562,11 +888,14 @@ static GradWs grad_ws_layout(int n, const GradPlan& gp) {
     w.a1 = take(c * n * n * sizeof(longlong2));
     w.a2 = take(c * n * n * sizeof(longlong2));
     w.exp = take(c * sizeof(int));
+    w.exp64 = take(c * sizeof(int));
     w.dfi = take(c * 2 * sizeof(int));
     w.cole = take(c * n * sizeof(int));
     w.rowk = take(c * n * sizeof(int));
     w.warp_g = take(c * gp.nwarps * n * n * sizeof(float4));
     w.part = take(c * gp.nchunks * n * n * sizeof(float4));
+    w.warp_s2 = take(c * gp.nwarps * sizeof(double));
+    w.est = take(c * sizeof(double));
     w.total = off;
     return w;
 }
@@ -575,7 +904,8 @@ static size_t grad_ws_bytes(int n, int count) {
     size_t most = 256;
     for (int done = 0; done < count; done += kMaxBatchLaunch) {
         const int c = std::min(kMaxBatchLaunch, count - done);
-        most = std::max(most, grad_ws_layout(n, plan_grad(n, c)).total);
+        most = std::max(most, grad_ws_layout(n, plan_grad(n, c, false)).total);
+        most = std::max(most, grad_ws_layout(n, plan_grad(n, c, true)).total);
         if (count > kMaxBatchLaunch) break;  // all full launches have the same layout; the last is smaller
     }
     return most;
@@ -584,12 +914,20 @@ static size_t grad_ws_bytes(int n, int count) {
 // Device-side gradient of `count` matrices: matrix b is dA + b * stride
 // (n x n complex128, leading dimension ld); grad out count x n x n complex128
 // row-major, perm out count x 2 doubles, optional perm dd count x 4 doubles.
+// arith GBPERM_ARITH_DF32: the double-float sweep, each matrix recomputed by
+// the integer-mantissa twin on the device when its range check fails or its
+// error estimate is above 1e-10 (d_est: count doubles receiving the
+// estimates, -1 for a failed range check); GBPERM_ARITH_FX64: the twin alone.
+// d_flags (count x 2 ints, optional): df_info after the run ({boost, ok}; ok
+// 0 = the twin's values).
 static int run_grad_dev(const double2* dA, long long ld, long long stride, int n, int count, void* ws,
                         size_t ws_bytes, double* d_grad, double* d_perm, double* d_perm4, cudaStream_t st,
-                        GradPlan* used) {
+                        GradPlan* used, int arith, double* d_est = nullptr, int* d_flags = nullptr) {
+    const bool fx_only = arith == GBPERM_ARITH_FX64;
+    const bool escalate = g_opt.df_escalate.load() != 0;
     for (int done = 0; done < count; done += kMaxBatchLaunch) {
         const int c = std::min(kMaxBatchLaunch, count - done);
-        GradPlan gp = plan_grad(n, c);
+        GradPlan gp = plan_grad(n, c, fx_only);
         if (used) *used = gp;
         const GradWs w = grad_ws_layout(n, gp);
         if (ws_bytes < w.total) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad: workspace too small");
@@ -597,11 +935,14 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         longlong2* a1 = reinterpret_cast<longlong2*>(base + w.a1);
         longlong2* a2 = reinterpret_cast<longlong2*>(base + w.a2);
         int* exp_out = reinterpret_cast<int*>(base + w.exp);
+        int* exp64 = reinterpret_cast<int*>(base + w.exp64);
         int* df_info = reinterpret_cast<int*>(base + w.dfi);
         int* col_e = reinterpret_cast<int*>(base + w.cole);
         int* row_k = reinterpret_cast<int*>(base + w.rowk);
         float4* warp_g = reinterpret_cast<float4*>(base + w.warp_g);
         float4* fin_part = reinterpret_cast<float4*>(base + w.part);
+        double* warp_s2 = reinterpret_cast<double*>(base + w.warp_s2);
+        double* est = d_est ? d_est + done : reinterpret_cast<double*>(base + w.est);
         PrepArgs pa;
         pa.col_e_out = col_e;
         pa.A = dA + (long long)done * stride;
@@ -614,12 +955,13 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         pa.a1 = a1;
         pa.a2 = a2;
         pa.exp_out = exp_out;
-        pa.df = 1;
+        pa.df = fx_only ? 0 : 1;
         pa.df_info = df_info;
         pa.count = c;
         pa.a_stride = stride;
         pa.row_balance = 1;
         pa.row_k_out = row_k;
+        pa.exp_fp64_out = exp64;
         cudaError_t e = launch_prepare(pa, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: prepare");
         GradArgs g;
@@ -631,22 +973,57 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         g.df_info = df_info;
         g.warp_g = warp_g;
         const dim3 grid(gp.grid, c);
-        if (gp.cpl == 4) grad_kernel<4><<<grid, kThreads, grad_smem<4>(n), st>>>(g);
-        else grad_kernel<8><<<grid, kThreads, grad_smem<8>(n), st>>>(g);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: kernel");
-        // the boost is read on the device by the finalize kernel via df_info
         const int ne = n * n;
-        grad_partial_kernel<<<dim3((ne + 127) / 128, gp.nchunks, c), 128, 0, st>>>(warp_g, gp.nwarps, n, fin_part);
         double* gout = d_grad + (size_t)done * 2 * n * n;
-        grad_finalize_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(fin_part, gp.nchunks, n, exp_out, col_e,
-                                                                        row_k, df_info, gout);
-        grad_perm_kernel<<<c, 32, 0, st>>>(dA + (long long)done * stride, ld, stride, n, gout, df_info,
-                                           d_perm + (size_t)done * 2, d_perm4 ? d_perm4 + (size_t)done * 4 : nullptr);
+        const double2* Ab = dA + (long long)done * stride;
+        double* pout = d_perm + (size_t)done * 2;
+        double* p4 = d_perm4 ? d_perm4 + (size_t)done * 4 : nullptr;
+        if (!fx_only) {
+            g.warp_s2 = warp_s2;
+            if (gp.cpl == 4) grad_kernel<4><<<grid, kThreads, grad_smem<4>(n), st>>>(g);
+            else grad_kernel<8><<<grid, kThreads, grad_smem<8>(n), st>>>(g);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: kernel");
+            // the boost is read on the device by the finalize kernel via df_info
+            grad_partial_kernel<<<dim3((ne + 127) / 128, gp.nchunks, c), 128, 0, st>>>(warp_g, gp.nwarps, n,
+                                                                                       fin_part);
+            grad_finalize_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(fin_part, gp.nchunks, n, exp_out,
+                                                                            col_e, row_k, df_info, gout);
+            grad_perm_kernel<<<c, 32, 0, st>>>(Ab, ld, stride, n, gout, df_info, pout, p4, warp_s2, gp.nwarps,
+                                               exp_out, est, escalate ? 1 : 0);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: finalize");
+        }
+        // the integer-mantissa twin: every matrix (fx_only), or those the
+        // range check or the error estimate handed over
+        g.warp_s2 = nullptr;
+        g.gate = fx_only ? nullptr : df_info;
+        if (gp.cpl == 4) grad_fx_kernel<4><<<grid, kThreads, grad_smem<4>(n), st>>>(g);
+        else grad_fx_kernel<8><<<grid, kThreads, grad_smem<8>(n), st>>>(g);
         e = cudaGetLastError();
-        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: finalize");
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: fx kernel");
+        double2* part2 = reinterpret_cast<double2*>(fin_part);
+        grad_partial_fx_kernel<<<dim3((ne + 127) / 128, gp.nchunks, c), 128, 0, st>>>(
+            reinterpret_cast<const double2*>(warp_g), gp.nwarps, n, part2, g.gate);
+        grad_finalize_fx_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(part2, gp.nchunks, n, exp64, col_e,
+                                                                           row_k, g.gate, gout);
+        grad_perm_kernel<<<c, 32, 0, st>>>(Ab, ld, stride, n, gout, fx_only ? nullptr : df_info, pout, p4, nullptr,
+                                           0, nullptr, nullptr, 0);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: fx finalize");
+        if (d_flags) {
+            if (fx_only) e = cudaMemsetAsync(d_flags + 2 * (size_t)done, 0, 2 * sizeof(int) * (size_t)c, st);
+            else e = cudaMemcpyAsync(d_flags + 2 * (size_t)done, df_info, 2 * sizeof(int) * (size_t)c,
+                                     cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: flags");
+        }
     }
     return GBPERM_OK;
+}
+
+// the gradient sweep's arithmetic (option "grad.arith")
+static int grad_arith() {
+    return g_opt.grad_arith.load() == GBPERM_ARITH_FX64 ? GBPERM_ARITH_FX64 : GBPERM_ARITH_DF32;
 }
 
 }  // namespace gbperm
@@ -674,7 +1051,7 @@ int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, vo
         return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_dev: workspace must be 256-byte aligned");
     return run_grad_dev(static_cast<const double2*>(dA), ld, 0, (int)n, 1, workspace, workspace_bytes,
                         static_cast<double*>(d_grad), static_cast<double*>(d_perm), static_cast<double*>(d_perm_dd),
-                        static_cast<cudaStream_t>(stream), nullptr);
+                        static_cast<cudaStream_t>(stream), nullptr, grad_arith());
 }
 
 int gbperm_perm_grad_batched_dev(const void* dA, int64_t n, int64_t count, int64_t ld, int64_t stride, void* d_perm,
@@ -689,7 +1066,7 @@ int gbperm_perm_grad_batched_dev(const void* dA, int64_t n, int64_t count, int64
         return fail(GBPERM_ERR_ARG, "gbperm_perm_grad_batched_dev: workspace must be 256-byte aligned");
     return run_grad_dev(static_cast<const double2*>(dA), ld, stride, (int)n, (int)count, workspace, workspace_bytes,
                         static_cast<double*>(d_grad), static_cast<double*>(d_perm), nullptr,
-                        static_cast<cudaStream_t>(stream), nullptr);
+                        static_cast<cudaStream_t>(stream), nullptr, grad_arith());
 }
 
 // Host-buffer form shared by the single and batched entry points: count
@@ -703,26 +1080,24 @@ static int perm_grad_host(const double* A, int64_t n, int64_t count, int64_t ld,
     if (count < 0 || count > INT32_MAX) return fail(GBPERM_ERR_ARG, std::string(who) + ": bad count");
     if (count == 0) return GBPERM_OK;
     if (!A || ld < n || stride < n * ld) return fail(GBPERM_ERR_ARG, std::string(who) + ": bad matrix");
-    for (int64_t b = 0; b < count; ++b) {
-        const double* Ab = A + 2 * b * stride;
-        if (!all_finite(Ab, n, n, ld)) continue;  // NaN out, below
-        int boost = 0;
-        if (!df_boost(Ab, n, n, ld, nullptr, nullptr, &boost, true))
-            return fail(GBPERM_ERR_TOO_LARGE,
-                        std::string(who) + ": matrix dynamic range beyond the double-float product");
-    }
+    // matrices beyond the double-float product's range are handed to the
+    // integer-mantissa twin by the device range check
+    const int arith = grad_arith();
     const size_t nn = (size_t)n * n;
     const size_t mat_bytes = align_up((size_t)count * nn * sizeof(double2), 256);
     const size_t perm_bytes = align_up((size_t)count * 6 * sizeof(double), 256);
+    const size_t est_bytes = align_up((size_t)count * (sizeof(double) + 2 * sizeof(int)), 256);
     const size_t ws = grad_ws_bytes((int)n, (int)count);
     ThreadCtx& c = thread_ctx();
-    int rc = c.ensure(mat_bytes * 2 + perm_bytes + ws);
+    int rc = c.ensure(mat_bytes * 2 + perm_bytes + est_bytes + ws);
     if (rc) return rc;
     char* base = static_cast<char*>(c.dbuf);
     double2* dA = reinterpret_cast<double2*>(base);
     double* dgrad = reinterpret_cast<double*>(base + mat_bytes);
     double* dperm = reinterpret_cast<double*>(base + 2 * mat_bytes);
-    void* dws = base + 2 * mat_bytes + perm_bytes;
+    double* dest = reinterpret_cast<double*>(base + 2 * mat_bytes + perm_bytes);
+    int* dflags = reinterpret_cast<int*>(dest + count);
+    void* dws = base + 2 * mat_bytes + perm_bytes + est_bytes;
     // dense upload: matrix b as n rows of n complex128; non-finite matrices
     // are replaced by zeros on the device and answered with NaN
     std::vector<double2> h((size_t)count * nn);
@@ -740,12 +1115,18 @@ static int perm_grad_host(const double* A, int64_t n, int64_t count, int64_t ld,
     if (stats) cudaEventRecord(c.ev0, c.stream);
     GradPlan used;
     rc = run_grad_dev(dA, n, (long long)nn, (int)n, (int)count, dws, ws, dgrad, dperm,
-                      count == 1 ? dperm + 2 : nullptr, c.stream, &used);
+                      count == 1 ? dperm + 2 : nullptr, c.stream, &used, arith, dest, dflags);
     if (rc) return rc;
     if (stats) cudaEventRecord(c.ev1, c.stream);
     std::vector<double> hp(count == 1 ? 6 : 2 * (size_t)count);
+    std::vector<double> hest((size_t)count, 0.0);
+    std::vector<int> hflags(2 * (size_t)count, 0);
     e = cudaMemcpyAsync(grads, dgrad, (size_t)count * nn * sizeof(double2), cudaMemcpyDeviceToHost, c.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), dperm, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess && arith != GBPERM_ARITH_FX64)
+        e = cudaMemcpyAsync(hest.data(), dest, hest.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     if (e != cudaSuccess) return cuda_fail(e, (std::string(who) + ": kernel").c_str());
     for (int64_t b = 0; b < count; ++b) {
@@ -761,10 +1142,21 @@ static int perm_grad_host(const double* A, int64_t n, int64_t count, int64_t ld,
         stats->kernel_ms = ms;
         stats->steps = (double)count * std::ldexp(1.0, (int)n - 1);
         stats->flops = 8.0 * (double)n * stats->steps;
-        stats->launches = 5 * (int)((count + kMaxBatchLaunch - 1) / kMaxBatchLaunch);
+        const int launches_per = arith == GBPERM_ARITH_FX64 ? 5 : 9;
+        stats->launches = launches_per * (int)((count + kMaxBatchLaunch - 1) / kMaxBatchLaunch);
         stats->grid = used.grid;
         stats->seg_log2 = used.seg_log2;
-        stats->arith = GBPERM_ARITH_DF32;
+        // arith: FX64 when the twin produced any matrix's values; err_est:
+        // the largest double-float estimate among the matrices it kept
+        bool any_fx = arith == GBPERM_ARITH_FX64;
+        double worst = 0.0;
+        for (int64_t b = 0; b < count; ++b) {
+            if (bad[b]) continue;
+            if (hflags[2 * b + 1] == 0) any_fx = true;
+            else if (hest[b] > worst) worst = hest[b];
+        }
+        stats->arith = any_fx ? GBPERM_ARITH_FX64 : GBPERM_ARITH_DF32;
+        stats->err_est = worst;
     }
     return GBPERM_OK;
 }

@@ -21,23 +21,6 @@ namespace {
 
 constexpr int kThreads = 128;
 
-// x^e of a column sum (e >= 2) as normalised limbs; returns the shift count
-// sigma of the result.  Out of line: reached only for columns of
-// multiplicity above 1.
-__device__ __noinline__ int fx_pow_col(long long cr, long long ci, int e, fxl* out) {
-    fxl z;
-    const int sz = fx_norm_col(cr, ci, z);
-    fxl r = z;
-    int sig = sz;
-    for (int k = 1; k < e; ++k) {
-        long long pr, pi;
-        fx_mul(r, z, pr, pi);
-        sig += sz - 1 + fx_norm(pr, pi, r);
-    }
-    *out = r;
-    return sig;
-}
-
 template <int CPL, int GROUP>
 __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
     constexpr int NP = CPL * GROUP;
@@ -184,32 +167,21 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
                 if (c < nr) {
+                    // a column of power e multiplies its chain e times by the
+                    // same column factor (inline: powers are mostly 1 or 2);
+                    // power 0 among the real columns cannot occur (the host
+                    // drops empty columns)
                     const int e = s_cpow[j0 + c];
-                    if (e == 1) {
-                        if (c < 2) {
-                            sig += fx_norm_col(cre[c], cim[c], ch[c]);
-                        } else {
-                            long long rr, ri;
-                            fx_mul(ch[c & 1], fx_col(cre[c], cim[c]), rr, ri);
-                            sig += fx_norm(rr, ri, ch[c & 1]) - 1;
-                        }
-                    } else if (e > 1) {
-                        fxl x;
-                        const int sx = fx_pow_col(cre[c], cim[c], e, &x);
-                        if (c < 2) {
-                            ch[c] = x;
-                            sig += sx;
-                        } else {
-                            long long rr, ri;
-                            fx_mul(ch[c & 1], x, rr, ri);
-                            sig += sx + fx_norm(rr, ri, ch[c & 1]) - 1;
-                        }
-                    } else if (c < 2) {
-                        // a column of power 0 among the real ones cannot
-                        // occur (the host drops empty columns); keep the
-                        // chain defined as the value 1 = 2^58 2^-58
-                        ch[c] = fxl{1 << 27, 0, 0, 0};
-                        sig += -3;
+                    const fxl y = fx_col(cre[c], cim[c]);
+                    int t = 0;
+                    if (c < 2) {
+                        sig += fx_norm_col(cre[c], cim[c], ch[c]);
+                        t = 1;
+                    }
+                    for (; t < e; ++t) {
+                        long long rr, ri;
+                        fx_mul(ch[c & 1], y, rr, ri);
+                        sig += fx_norm(rr, ri, ch[c & 1]) - 1;
                     }
                 }
             }

@@ -52,6 +52,20 @@ extern "C" int gbperm_perm_repeated_batched(const double* A, int64_t rows, int64
                                             int64_t nrow, int64_t count, int arith, double* out,
                                             gbperm_stats* stats) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (arith == GBPERM_ARITH_FX64) {
+        // integer-mantissa product: every pair in one persistent
+        // multiplicity launch; pairs with more than 40 occupied product-side
+        // modes fall back to the launches below with the FP64 product
+        gbperm_rep_batch* plan = nullptr;
+        int rc = gbperm_rep_batch_create(A, rows, cols, ld, col_mults, ncol, row_mults, nrow, count, arith, &plan);
+        if (rc == GBPERM_OK) {
+            rc = gbperm_rep_batch_run(plan, out, stats);
+            gbperm_rep_batch_destroy(plan);
+            return rc;
+        }
+        if (rc != GBPERM_ERR_TOO_LARGE) return rc;
+        arith = GBPERM_ARITH_FP64;
+    }
     if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_repeated_batched: unknown arithmetic");
     if (count < 0 || rows < 0 || cols < 0 || nrow < 0 || ncol < 0)

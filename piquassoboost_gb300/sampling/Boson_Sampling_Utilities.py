@@ -19,8 +19,10 @@ value set for permanent library.").  Three ids are added: 20 (GB300 FP64),
 product).  The reference's "long double" ids (plain 0, 8, 11; repeated 1, 8)
 run the integer-mantissa product: 55-57 significant bits per complex
 multiply, more than the FP64 product's 53 (it does not reach the x87
-extended type's 64).  Lists of matrices or of states run through the batched
-launches, which have no integer-mantissa product: there "fx" uses FP64.
+extended type's 64).  Lists of states run through one persistent
+multiplicity launch with that product; lists of matrices run through the
+plain batched launch, which has no integer-mantissa product: there "fx" uses
+FP64.
 
 Every class also takes a keyword-only ``backend``: None (default) keeps the
 arithmetic of its library id, "fp64" selects the FP64 product, "fx" the
@@ -146,7 +148,7 @@ class ChinHuhPermanentCalculator_wrapper:
                     row = [(fixed_in, out) for out in outs[i]]
                 shape.append(len(row))
                 pairs.extend(row)
-            vals = nat.perm_repeated_many(self._matrix, pairs, mode=_batched_mode(mode))
+            vals = nat.perm_repeated_many(self._matrix, pairs, mode=mode)
             res, k = [], 0
             for n in shape:
                 res.append(vals[k:k + n])

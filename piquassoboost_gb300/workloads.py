@@ -52,6 +52,28 @@ def batched_instances(count: int, seed: int, modes: int = 100, kmin: int = 8, km
     return mats
 
 
+def batched_index_sets(count: int, seed: int, modes: int = 100, kmin: int = 8, kmax: int = 28):
+    """The draws behind batched_instances (same seed, same stream): the
+    unitary and, per instance, its row and column index draws; instance i of
+    batched_instances is u[np.ix_(rows[i], cols[i])]."""
+    u = haar_unitary(modes, seed)
+    rng = np.random.default_rng(seed + 104729)
+    ks = rng.integers(kmin, kmax + 1, size=count)
+    rows, cols = [], []
+    for k in ks:
+        rows.append(rng.integers(0, modes, size=k))
+        cols.append(rng.integers(0, modes, size=k))
+    return u, rows, cols
+
+
+def index_sets_to_states(rows, cols, modes: int):
+    """Occupation form of index draws: (input_state, output_state) pairs,
+    input = column multiplicities, output = row multiplicities (the
+    reference's (input, output) convention of the repeated calculators)."""
+    return [(np.bincount(c, minlength=modes).astype(np.int64), np.bincount(r, minlength=modes).astype(np.int64))
+            for r, c in zip(rows, cols)]
+
+
 def pmf_layer_instance(seed: int, modes: int = 60, photons: int = 30):
     """The last probability layer of a Clifford & Clifford run: Haar
     `modes`-mode unitary, one input photon in each of modes 0..photons-1, and

@@ -123,3 +123,70 @@ def test_batched_fast_within_bar_of_fp64():
     d = np.array(nat.perm_batched(mats, mode="fp64"))
     assert np.max(np.abs(f - d) / np.abs(d)) <= 1e-10
     assert 0.0 < st.err_est <= 1e-10
+
+
+# ------------------------------------------------ multiplicity batch plan
+def _pairs_batch(count, seed, modes, kmin, kmax):
+    from piquassoboost_gb300.workloads import batched_index_sets, index_sets_to_states
+    U, rows, cols = batched_index_sets(count, seed=seed, modes=modes, kmin=kmin, kmax=kmax)
+    return U, rows, cols, index_sets_to_states(rows, cols, modes)
+
+
+def test_rep_batch_matches_expanded_submatrices():
+    # the draws of the batched configuration (rows and columns with
+    # repetition from one Haar unitary) as state pairs: every permanent
+    # against the integer-mantissa plain kernel on its expanded submatrix
+    U, rows, cols, pairs = _pairs_batch(96, seed=7, modes=60, kmin=4, kmax=20)
+    plan = nat.RepBatchPlan(U, pairs)
+    got = plan.run()
+    assert plan.info()["steps"] > 0
+    for i, (r, c) in enumerate(zip(rows, cols)):
+        ref = nat.perm(U[np.ix_(r, c)], mode="fx")
+        assert abs(got[i] - ref) <= TOL * abs(ref), (i, got[i], ref)
+    # a second run of the same plan gives the same bits
+    assert np.array_equal(plan.run(), got)
+    plan.close()
+
+
+def test_rep_batch_vs_oracle_and_edge_pairs():
+    from piquassoboost_gb300.workloads import haar_unitary
+    m = 12
+    U = haar_unitary(m, 3)
+    rng = np.random.default_rng(12)
+    pairs = []
+    for _ in range(20):
+        k = int(rng.integers(1, 9))
+        pairs.append((rng.multinomial(k, np.ones(m) / m), rng.multinomial(k, np.ones(m) / m)))
+    pairs.append((np.zeros(m, dtype=np.int64), np.zeros(m, dtype=np.int64)))   # no photons -> 1
+    pairs.append((np.eye(m, dtype=np.int64)[2] * 3, np.eye(m, dtype=np.int64)[5] * 3))  # one mode each side
+    plan = nat.RepBatchPlan(U, pairs)
+    got = plan.run()
+    for i, (cin, rout) in enumerate(pairs):
+        ref, dref = orc.bbfg_repeated(U, cin, rout, prec=1)
+        if abs(ref) < 1e-300:
+            assert abs(got[i]) < 1e-12
+        else:
+            assert orc.rel_err(got[i], dref) <= TOL, (i, got[i], ref)
+    # the batched entry point with the integer-mantissa product runs the plan
+    many = nat.perm_repeated_many(U, pairs, mode="fx")
+    assert np.allclose(many, got, rtol=0, atol=0)
+
+
+def test_rep_batch_device_form_and_limits():
+    torch = pytest.importorskip("torch")
+    U, rows, cols, pairs = _pairs_batch(40, seed=8, modes=50, kmin=6, kmax=16)
+    plan = nat.RepBatchPlan(U, pairs)
+    host = plan.run()
+    d_out = torch.zeros(2 * len(pairs), dtype=torch.float64, device="cuda")
+    plan.run_dev(d_out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    dev = d_out.cpu().numpy()
+    assert np.array_equal(dev[0::2] + 1j * dev[1::2], host)
+    plan.close()
+    # more than 40 occupied modes on both sides: rejected by the plan
+    from piquassoboost_gb300.workloads import haar_unitary
+    big = haar_unitary(44, 1)
+    ones = np.ones(44, dtype=np.int64)
+    with pytest.raises(nat.GBPermError) as ei:
+        nat.RepBatchPlan(big, [(ones, ones)])
+    assert ei.value.code == nat.GBPERM_ERR_TOO_LARGE

@@ -40,15 +40,121 @@ def test_grad_sampled_minors(n):
         assert abs(G[k, l] - ref) <= 1e-10 * max(abs(ref), 1e-3 * gnorm)
 
 
+@pytest.mark.parametrize("n", [2, 5, 9, 12])
+def test_grad_fx_all_minors(n):
+    # the integer-mantissa sweep: every entry against binary128 minors
+    A = haar_block(n, seed=1700 + n)
+    st = nat.Stats()
+    p, G = nat.perm_grad(A, mode="fx", stats=st)
+    assert st.arith == nat.ARITH_FX64
+    _, q = orc.bbfg(A, prec=1)
+    assert orc.rel_err(p, q) <= 1e-10
+    gnorm = np.abs(G).max()
+    for k in range(n):
+        for l in range(n):
+            ref, _ = orc.bbfg(_minor(A, k, l), prec=1) if n > 1 else (1.0, None)
+            assert abs(G[k, l] - ref) <= 1e-10 * max(abs(ref), 1e-3 * gnorm), (k, l, G[k, l], ref)
+
+
+@pytest.mark.parametrize("n", [20, 24])
+def test_grad_fx_more_accurate_than_fast(n):
+    # worst entry error against the FP64 kernel's minors, fx vs double-float
+    A = haar_block(n, seed=1800 + n)
+    _, Gf = nat.perm_grad(A, mode="fast")
+    _, Gx = nat.perm_grad(A, mode="fx")
+    rng = np.random.default_rng(n)
+    gnorm = np.abs(Gx).max()
+    worst = {"fast": 0.0, "fx": 0.0}
+    for _ in range(8):
+        k, l = (int(x) for x in rng.integers(0, n, size=2))
+        m = nat.perm(_minor(A, k, l), mode="fx")
+        d = max(abs(m), 1e-3 * gnorm)
+        worst["fast"] = max(worst["fast"], abs(Gf[k, l] - m) / d)
+        worst["fx"] = max(worst["fx"], abs(Gx[k, l] - m) / d)
+    assert worst["fx"] <= 1e-12 and worst["fast"] <= 1e-10, worst
+
+
+def test_grad_wide_column_range():
+    # columns scaled by 2^-300 .. 2^300: each column is normalised by its own
+    # power of two, so the double-float sweep keeps the bar
+    rng = np.random.default_rng(51)
+    n = 10
+    A = haar_block(n, seed=51) * np.exp2(rng.integers(-300, 300, n))[None, :]
+    p, G = nat.perm_grad(A)
+    ref = nat.perm(A, mode="fx")
+    assert abs(p - ref) <= 1e-10 * abs(ref)
+    for k, l in ((0, 0), (3, 7), (9, 2)):
+        m = nat.perm(_minor(A, k, l), mode="fx")
+        assert abs(G[k, l] - m) <= 1e-10 * abs(m), (k, l)
+
+
+def test_grad_range_check_failure_runs_fx_twin():
+    # a zero column fails the double-float range check (no scale for it):
+    # the device hands the matrix to the integer-mantissa twin, which used
+    # to be an error.  The permanent is 0; the minors without that column
+    # survive.
+    n = 8
+    A = haar_block(n, seed=8).copy()
+    A[:, 3] = 0.0
+    st = nat.Stats()
+    p, G = nat.perm_grad(A, stats=st)
+    assert st.arith == nat.ARITH_FX64
+    assert p == 0
+    gnorm = np.abs(G).max()
+    assert gnorm > 0
+    for k in range(n):
+        for l in range(n):
+            m = nat.perm(_minor(A, k, l), mode="fx")
+            assert abs(G[k, l] - m) <= 1e-10 * max(abs(m), 1e-3 * gnorm)
+
+
+def test_grad_escalates_above_error_bar():
+    # positive entries: the Gray terms dwarf the permanent, the double-float
+    # estimate exceeds 1e-10 and the twin recomputes on the device
+    rng = np.random.default_rng(28)
+    G0 = np.abs(rng.standard_normal((28, 28))) + 0.1
+    st = nat.Stats()
+    p, G = nat.perm_grad(G0, stats=st)
+    assert st.arith == nat.ARITH_FX64
+    px, Gx = nat.perm_grad(G0, mode="fx")
+    assert abs(p - px) <= 1e-12 * abs(px)
+    assert np.max(np.abs(G - Gx)) <= 1e-12 * np.max(np.abs(Gx))
+    ref = nat.perm(G0, mode="fx")
+    assert abs(p - ref) <= 1e-10 * abs(ref)
+    # a Haar block stays on the double-float sweep, with its estimate reported
+    st2 = nat.Stats()
+    nat.perm_grad(haar_block(16, seed=16), stats=st2)
+    assert st2.arith == nat.ARITH_DF32 and 0.0 < st2.err_est <= 1e-10
+
+
+def test_grad_batched_mixed_escalation():
+    # one launch: Haar members stay double-float, a positive member and an
+    # out-of-range member go to the twin; each matches its own single call
+    rng = np.random.default_rng(9)
+    mats = [haar_block(12, seed=s) for s in range(3)]
+    mats.append(np.abs(rng.standard_normal((12, 12))) + 0.1)
+    zc = haar_block(12, seed=77).copy()
+    zc[:, 5] = 0.0
+    mats.append(zc)
+    mats = np.stack(mats)
+    perms, grads = nat.perm_grad_batched(mats)
+    for b in range(len(mats)):
+        ref = nat.perm(mats[b], mode="fx")
+        assert abs(perms[b] - ref) <= 1e-10 * abs(ref) or perms[b] == ref == 0, b
+        _, G = nat.perm_grad(mats[b], mode="fx")
+        assert np.max(np.abs(grads[b] - G)) <= 1e-10 * np.max(np.abs(G)), b
+
+
+@pytest.mark.parametrize("mode", ["fast", "fx"])
 @pytest.mark.parametrize("n", [28, 32])
-def test_grad_large_sampled_minors_and_differences(n):
+def test_grad_large_sampled_minors_and_differences(n, mode):
     # the gradient sizes of the differentiable-permanent configuration:
     # 16 seeded entries against their minors (n - 1 permanents on the FP64
     # kernel, itself pinned to the oracle) and 3 against FP64 central
     # differences (the permanent is linear in each entry, so the difference
     # quotient is exact up to rounding)
     A = haar_block(n, seed=900 + n)
-    p, G = nat.perm_grad(A)
+    p, G = nat.perm_grad(A, mode=mode)
     ref = nat.perm(A, mode="fp64")
     assert abs(p - ref) <= 1e-10 * abs(ref)
     gnorm = np.abs(G).max()
