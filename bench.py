@@ -154,14 +154,21 @@ def host_threads() -> int:
     return os.cpu_count() or 1
 
 
+# committed ncu summaries holding the DRAM bytes of one launch of each
+# product's plain kernel; the traffic is the fixed-point tables and the
+# per-block partial sums, so it does not grow with the Gray steps
+_TRAFFIC_PROFILES = {"fx": "plain_fx_kernel_n28.md", "fast": "plain_df_kernel_n36_launches.md",
+                     "fp64": "plain_kernel_fp64_n28.md"}
+
+
 def traffic_from_profile(n: int, mode: str):
-    """DRAM bytes per launch of the permanent kernel, from the committed ncu
-    summary of this workload (profiles/bench_plain_n36_launches.md), or None."""
-    if n != 36 or mode != "fast":
+    """DRAM bytes per launch of the plain kernel of `mode`, read from the
+    committed ncu summary of that kernel (profiles/), or None."""
+    name = _TRAFFIC_PROFILES.get(mode)
+    if name is None:
         return None
-    path = os.path.join(ROOT, "profiles", "bench_plain_n36_launches.md")
     try:
-        text = open(path).read()
+        text = open(os.path.join(ROOT, "profiles", name)).read()
     except OSError:
         return None
     import re
