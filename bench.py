@@ -75,9 +75,11 @@ def parse():
     if args.batch_count < 1 or not 8 <= args.batch_kmax <= 32:
         ap.error("--batch-count must be >= 1 and --batch-kmax in 8..32")
     if args.mode is None:
-        args.mode = "fx" if args.workload in ("plain", "repeated", "batched") else "fp64"
-    if args.mode == "fx" and args.workload not in ("plain", "repeated", "batched"):
-        ap.error("--mode fx: the integer-mantissa product serves the plain, repeated and batched workloads")
+        args.mode = {"plain": "fx", "repeated": "fx", "batched": "fx", "grad": "fast"}.get(args.workload, "fp64")
+    if args.mode == "fx" and args.workload not in ("plain", "repeated", "batched", "grad"):
+        ap.error("--mode fx: the integer-mantissa product serves the plain, repeated, batched and grad workloads")
+    if args.workload == "grad" and args.mode == "fp64":
+        ap.error("--workload grad: the gradient sweep runs the 'fast' or the 'fx' product")
     return args
 
 
@@ -333,9 +335,10 @@ def run_ours(args, rank, world, local):
     d_out = torch.zeros(2, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     # prepare + permanent kernel; the double-float kernel also queues its
-    # FP64 twin (it returns at once unless the range check or the error
-    # estimate hands it the permanent)
-    launches_per_step = {"fast": 3}.get(args.mode, 2)
+    # integer-mantissa twin (it returns at once unless the range check or
+    # the error estimate hands it the permanent); above 36 rows the fast
+    # mode runs the integer-mantissa kernel alone
+    launches_per_step = 3 if args.mode == "fast" and n <= nat.get_option("df.max_rows") else 2
 
     def step(i, a=arith):
         rc = lib.gbperm_perm_dev(ctypes.c_void_p(d_mats[i].data_ptr()), n, n, n, a,
@@ -410,7 +413,7 @@ def run_ours(args, rank, world, local):
             vals.append(v)
             if mode == "fast":
                 ests.append(st.err_est)
-                esc += int(st.arith == nat.ARITH_FP64)
+                esc += int(st.arith != nat.ARITH_DF32)
         if mode == "fp64":
             ref64 = dict(zip(idx, vals))
             if args.mode == "fp64":
@@ -427,8 +430,8 @@ def run_ours(args, rank, world, local):
         else:
             d.update({"dtype": "f32 pairs (double-float product)", "kernel": "plain_df_kernel",
                       "escalated_steps": esc, "err_est": ests,
-                      "note": "an escalated step reruns the permanent on the FP64 kernel: kernel_ms includes "
-                              "the double-float pass it discards"})
+                      "note": "an escalated step reruns the permanent on the integer-mantissa kernel: "
+                              "kernel_ms includes the double-float pass it discards"})
         products[mode] = d
         if mode != "fp64":
             products[mode]["rel_err_vs_fp64_kernel"] = [abs(v - ref64[i]) / abs(ref64[i]) for i, v in zip(idx, vals)]
@@ -516,10 +519,11 @@ def run_ours(args, rank, world, local):
 _P = ctypes.c_void_p
 
 
-def _line(args, world, value, unit, ms_per_step, config, roofline, cpu, e2e, launches, extra=None, clocks=None):
+def _line(args, world, value, unit, ms_per_step, config, roofline, cpu, e2e, launches, extra=None, clocks=None,
+          dtype="f64"):
     d = {"metric": METRIC, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
          "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "roofline": roofline,
+         "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config, "roofline": roofline,
          "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches}
     if clocks is not None:
         d["clocks"] = clocks
@@ -573,30 +577,55 @@ def _max_over_ranks(torch, world, t):
 
 # --------------------------------------------------------------- repeated
 def _repeated(args, rank, world, torch):
+    """One 60-mode / 30-photon repeated permanent per step through the
+    host-buffer entry point (the public call); each timed instance is then
+    run through the other products for their rates and the check against
+    the FP64 kernel."""
     from piquassoboost_gb300 import _native as nat
-    from piquassoboost_gb300.workloads import batched_instances, haar_block, repeated_instance
+    from piquassoboost_gb300.workloads import repeated_instance
 
     mode = args.mode
     cases = [repeated_instance(seed=1000 * rank + s, modes=60, photons=30, max_mult=4)
              for s in range(args.warmup + args.steps)]
-    peak = nat.probe_peak("fp64")
+    peaks = {k: nat.probe_peak(k) for k in ("fp64", "imad_wide")}
     st = nat.Stats()
     for U, i, o in cases[:args.warmup]:
         nat.perm_repeated(U, i, o, mode=mode)
-    kms, flops = [], 0.0
+    kms, flops, imad, got, launches = [], 0.0, 0.0, [], 0
     clk = ClockSampler(torch.cuda.current_device())
     clk.start()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for U, i, o in cases[args.warmup:]:
-        nat.perm_repeated(U, i, o, mode=mode, stats=st)
+        got.append(nat.perm_repeated(U, i, o, mode=mode, stats=st))
         kms.append(st.kernel_ms)
         flops += st.flops
+        # 12 32x32->64 multiply-adds per complex multiply, photons - 1
+        # multiplies per Gray step
+        imad += 12.0 * (int(np.sum(o)) - 1) * st.steps
+        launches += st.launches
     wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
     clocks = clk.stop()
     # the host-buffer call is the public API: e2e == the timed loop itself
     value = world * args.steps / (sum(kms) * 1e-3)
     e2e = world * args.steps / wall
+    products, ref64 = {}, []
+    for other in ("fp64", "fx", "fast"):
+        if other == mode:
+            continue
+        ms, vals, esc = [], [], 0
+        for U, i, o in cases[args.warmup:]:
+            s2 = nat.Stats()
+            vals.append(nat.perm_repeated(U, i, o, mode=other, stats=s2))
+            ms.append(s2.kernel_ms)
+            esc += int(other == "fast" and s2.arith != nat.ARITH_DF32)
+        products[other] = {"kernel_ms": ms, "perm_per_s": len(ms) / (sum(ms) * 1e-3)}
+        if other == "fast":
+            products[other]["escalated_or_skipped"] = esc
+        if other == "fp64":
+            ref64 = vals
+            products[other]["frac_of_fp64_peak"] = flops / (sum(ms) * 1e-3) / 1e12 / peaks["fp64"]
+    rel = [abs(a - b) / abs(b) for a, b in zip(got, ref64)] if ref64 else []
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = _oracle()
@@ -610,14 +639,26 @@ def _repeated(args, rank, world, torch):
         cpu = {"value": n / dt, "unit": "perm/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} full permanents of the first timed instance (reference repeated BBFG double "
                          f"algorithm as the C oracle, {os.cpu_count()} threads)"}
+    avg = statistics.mean(kms)
+    if mode == "fx":
+        ach = imad / args.steps / (avg * 1e-3) / 1e12
+        roof = {"bound": "int", "achieved": ach, "peak": peaks["imad_wide"], "unit": "Tops/s",
+                "frac": ach / peaks["imad_wide"], "traffic": None, "kernel": "repeated_fx_kernel",
+                "work_per_launch": "12 (photons - 1) multiply-adds per Gray step of the multiplicity form",
+                "peak_source": "mad.wide.s32 probe (gbperm_probe_peak kind 3), measured in this run",
+                "fp64_equivalent_tflops": flops / args.steps / (avg * 1e-3) / 1e12}
+    else:
+        roof = _roof(flops / args.steps, avg, peaks["fp64"],
+                     "repeated_df_kernel" if mode == "fast" else "repeated_kernel")
     if rank == 0:
         _line(args, world, value, "perm/s", 1000 * wall / args.steps,
               {"workload": workload_desc(args), "arith": mode,
                "l2": "inputs < 100 KB; compute-bound, no flush"},
-              _roof(flops / args.steps, statistics.mean(kms), peak,
-                    {"fast": "repeated_df_kernel", "fx": "repeated_fx_kernel"}.get(mode, "repeated_kernel")),
-              cpu, {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": 60 * 60 * 16 + 2 * 60 * 8,
-                    "d2h_bytes_per_step": 48}, (3 if mode == "fast" else 2) * args.steps, clocks=clocks)
+              roof, cpu, {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": 60 * 60 * 16 + 2 * 60 * 8,
+                          "d2h_bytes_per_step": 48}, launches,
+              {"kernel_ms": kms, "products": products, "rel_err_vs_fp64_kernel": rel,
+               "max_rel_err": max(rel) if rel else None}, clocks=clocks,
+              dtype={"fx": "int64", "fp64": "f64", "fast": "f32x2"}[mode])
     return 0
 
 
@@ -695,8 +736,8 @@ def _batched_multiplicity(args, rank, world, torch):
     diff = float(np.max(np.abs(got - b) / np.abs(b)))
     avg = statistics.mean(kms)
     # roofline: the integer multiply-adds of the walked steps (12 per
-    # complex multiply; the plan's algorithmic flops count 6 per multiply)
-    ach = info["flops"] * 2.0 / (avg * 1e-3) / 1e12
+    # complex multiply, photons - 1 multiplies per step)
+    ach = info["mul_ops"] / (avg * 1e-3) / 1e12
     roof = {"bound": "int", "achieved": ach, "peak": peaks["imad_wide"], "unit": "Tops/s",
             "frac": ach / peaks["imad_wide"], "traffic": None, "kernel": "rep_batched_kernel",
             "work_per_launch": f"{info['steps']:.4g} Gray steps of the instances' multiplicity forms "
@@ -845,58 +886,75 @@ def _batched(args, rank, world, torch):
 
 # ------------------------------------------------------------------- grad
 def _grad(args, rank, world, torch):
+    """Permanent + full gradient per step (n <= 32). mode "fast": the
+    double-float sweep, recomputed on the device by the integer-mantissa
+    sweep when its range check fails or its estimate is above 1e-10 (the
+    library's default); "fx": the integer-mantissa sweep alone. The forward
+    it is compared with is the same product's plain permanent, as users get
+    it (escalation on)."""
     from piquassoboost_gb300 import _native as nat
-    from piquassoboost_gb300.workloads import batched_instances, haar_block, repeated_instance
+    from piquassoboost_gb300.workloads import haar_block
 
     from piquassoboost_gb300.torch_perm import permanent_and_grad, permanent_fwd
 
+    mode = args.mode
     n = args.n if args.n <= 32 else 32
-    mats = [torch.tensor(haar_block(n, seed=args.seed + 1000 * rank + s), device="cuda")
-            for s in range(args.warmup + args.steps)]
+    host = [haar_block(n, seed=args.seed + 1000 * rank + s) for s in range(args.warmup + args.steps)]
+    mats = [torch.tensor(h, device="cuda") for h in host]
     peak = nat.probe_peak("fp64")
-    for k in range(args.warmup):
-        permanent_and_grad(mats[k])
-        permanent_fwd(mats[k], mode="fast")
-    torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    clk = ClockSampler(torch.cuda.current_device())
-    clk.start()
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        ev[k][0].record(stream)
-        permanent_and_grad(mats[args.warmup + k])
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
-    clocks = clk.stop()
-    gms = [a.elapsed_time(b) for a, b in ev]
-    # the forward the gradient sweep is compared with: the same double-float
-    # product alone (escalation to FP64 off, as the gradient sweep has none)
-    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    nat.set_option("df.escalate", 0)
-    try:
+    with nat.grad_arithmetic(mode):
+        for k in range(args.warmup):
+            permanent_and_grad(mats[k])
+            permanent_fwd(mats[k], mode=mode)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        clk = ClockSampler(torch.cuda.current_device())
+        clk.start()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            permanent_and_grad(mats[args.warmup + k])
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = _max_over_ranks(torch, world, time.perf_counter() - t0)
+        clocks = clk.stop()
+        gms = [a.elapsed_time(b) for a, b in ev]
+        fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         for k in range(args.steps):
             fev[k][0].record(stream)
-            permanent_fwd(mats[args.warmup + k], mode="fast")
+            permanent_fwd(mats[args.warmup + k], mode=mode)
             fev[k][1].record(stream)
         torch.cuda.synchronize()
-    finally:
-        nat.set_option("df.escalate", 1)
-    fms = [a.elapsed_time(b) for a, b in fev]
+        fms = [a.elapsed_time(b) for a, b in fev]
+        # e2e through the host-buffer entry point; its stats say which steps
+        # the integer-mantissa sweep recomputed
+        esc, ests = 0, []
+        t1 = time.perf_counter()
+        for k in range(args.steps):
+            st = nat.Stats()
+            nat.perm_grad(host[args.warmup + k], stats=st)
+            ests.append(st.err_est)
+            esc += int(mode == "fast" and st.arith == nat.ARITH_FX64)
+        e2e = world * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
     flops = 8.0 * n * 2.0 ** (n - 1)
-    t1 = time.perf_counter()
-    for k in range(args.steps):
-        nat.perm_grad(mats[args.warmup + k].cpu().numpy())
-    e2e = world * args.steps / _max_over_ranks(torch, world, time.perf_counter() - t1)
+    roof = _roof(flops, statistics.mean(gms), peak, "grad_kernel" if mode == "fast" else "grad_fx_kernel")
+    roof["note"] = ("achieved counts the forward sum's FP64-equivalent flops (8 n 2^(n-1)) per forward+gradient "
+                    "step; the sweep computes in " + ("float pairs on the FP32 pipe" if mode == "fast" else
+                                                      "integer mantissas on the integer pipe") +
+                    ", so frac is not an FP64-pipe fraction")
     if rank == 0:
         _line(args, world, world * args.steps / wall, "(perm+grad)/s", 1000 * wall / args.steps,
-              {"workload": workload_desc(args), "n": n, "arith": "fast"},
-              _roof(flops, statistics.mean(gms), peak, "grad_kernel (forward flops only)"),
-              None, {"value": e2e, "unit": "(perm+grad)/s", "h2d_bytes_per_step": n * n * 16,
-                     "d2h_bytes_per_step": n * n * 16 + 16}, 5 * args.steps,
+              {"workload": workload_desc(args), "n": n, "arith": mode},
+              roof, None, {"value": e2e, "unit": "(perm+grad)/s", "h2d_bytes_per_step": n * n * 16,
+                           "d2h_bytes_per_step": n * n * 16 + 16},
+              # double-float chain (prepare, sweep, partial, finalize, perm)
+              # and its gated integer-mantissa twin chain; fx alone: 5
+              (9 if mode == "fast" else 5) * args.steps,
               {"forward_only_ms": statistics.mean(fms), "grad_ms": statistics.mean(gms),
-               "grad_over_forward": statistics.mean(gms) / statistics.mean(fms)}, clocks=clocks)
+               "grad_over_forward": statistics.mean(gms) / statistics.mean(fms),
+               "escalated_steps": esc, "err_est": ests}, clocks=clocks,
+              dtype="f32x2" if mode == "fast" else "int64")
     return 0
 
 

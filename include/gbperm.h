@@ -43,13 +43,20 @@ extern "C" {
  * point in both; the cross-thread reduction is double-double in both). */
 #define GBPERM_ARITH_FP64 0  /* IEEE double product on the FP64 pipe */
 #define GBPERM_ARITH_DF32 1  /* double-float product on the FP32 pipe (~2^-46 per
-                                complex multiply); used for up to 48 columns when
-                                the matrix's dynamic range allows, else FP64 */
+                                complex multiply), tried first for up to 48 columns
+                                within the size rules ("df.max_rows",
+                                "df.max_photons") when the matrix's dynamic range
+                                allows; the integer-mantissa product recomputes on
+                                the device when the range check fails or the error
+                                estimate exceeds 1e-10, and runs alone beyond the
+                                size rules (plain and repeated; pmf and the batched
+                                plans recompute in FP64) */
 #define GBPERM_ARITH_FX64 2  /* integer-mantissa product on the integer pipes: 64-bit
                                 mantissas in 31-bit limbs, 55-57 significant bits per
                                 complex multiply (the FP64 product keeps 53); any
-                                dynamic range, no FP64 fallback needed.  Plain
-                                permanents (gbperm_perm, gbperm_perm_dev) */
+                                dynamic range, no FP64 fallback needed.  Plain and
+                                repeated permanents, the gradient sweep and the
+                                repeated batch plans */
 
 /* Largest supported matrix side (columns of the product, rows of the Gray code). */
 #define GBPERM_MAX_DIM 64
@@ -67,9 +74,11 @@ typedef struct gbperm_stats {
                               estimated relative rounding error of its result,
                               sqrt(n) 2^-46 sqrt(sum |term|^2) / |perm| (pmf: the largest over the
                               layer's permanents; batched: the largest over the results kept in
-                              double-float).  Above 1e-10 the FP64 product recomputed the result on
-                              the device (batched: per instance, in a second pass of the plan) and
-                              arith reports FP64.  0 when only the FP64 product ran */
+                              double-float).  Above 1e-10 the result was recomputed on the device
+                              by the integer-mantissa product (plain, repeated, gradient; arith
+                              reports FX64) or the FP64 product (pmf, batched: per instance, in a
+                              second pass of the plan; arith reports FP64).  0 when the
+                              double-float product did not run */
 } gbperm_stats;
 
 /* ------------------------------------------------------------- library */
@@ -91,8 +100,16 @@ int gbperm_device_count(void);
  *   "plain.fx_group"      lanes sharing one Gray segment in the integer-mantissa kernel
  *                         (0 = by column count: pairs up to 40 columns; 4 = quads from 22)
  *   "df.escalate"         1 (default): a double-float result whose error estimate exceeds
- *                         1e-10 is recomputed by the FP64 kernel; 0: keep it (stats.err_est
- *                         still reports the estimate)
+ *                         1e-10 is recomputed on the device (integer-mantissa twin for
+ *                         plain, repeated and gradient; FP64 for pmf and batched); 0: keep
+ *                         it (stats.err_est still reports the estimate)
+ *   "df.max_rows"         GBPERM_ARITH_DF32 on a square plain matrix with more rows runs the
+ *                         integer-mantissa product alone (default 36)
+ *   "df.max_photons"      GBPERM_ARITH_DF32 on a repeated permanent (or pmf layer) with more
+ *                         photons runs the integer-mantissa (pmf: FP64) product alone
+ *                         (default 24)
+ *   "grad.arith"          product of the gradient sweep: 1 (default, double-float with the
+ *                         integer-mantissa twin) or 2 (integer-mantissa throughout)
  */
 int gbperm_set_option(const char* key, int64_t value);
 int64_t gbperm_get_option(const char* key);
@@ -109,10 +126,10 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
 /* Device-pointer form.  dA: device complex128 matrix; d_out: 2 doubles on
  * the device; d_out_dd: NULL or 4 doubles on the device.  The workspace must
  * hold gbperm_perm_workspace_size(rows, cols) bytes, 256-byte aligned.  With
- * GBPERM_ARITH_DF32 the range check runs on the device and the FP64 product
- * takes over when it fails, or when the double-float result's estimated
- * relative rounding error exceeds 1e-10 (decided on the device, no host
- * round trip). */
+ * GBPERM_ARITH_DF32 the range check runs on the device and the
+ * integer-mantissa product takes over when it fails, or when the
+ * double-float result's estimated relative rounding error exceeds 1e-10
+ * (decided on the device, no host round trip). */
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols);
 int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int arith, void* d_out,
                     void* d_out_dd, void* workspace, size_t workspace_bytes, void* stream);
@@ -173,14 +190,17 @@ int gbperm_perm_repeated_batched(const double* A, int64_t rows, int64_t cols, in
  * tables, and captures the host run as a CUDA graph.  run: host output
  * (2 * count doubles, caller's order); run_dev: the same kernels enqueued on
  * `stream` writing 2 * count doubles to device memory.  info: Gray steps,
- * algorithmic flops and work items of the plan. */
+ * algorithmic flops (as gbperm_stats.flops counts them), 32x32->64 integer
+ * multiply-adds of the products (12 per complex multiply, photons - 1
+ * multiplies per step) and work items of the plan; any pointer may be null. */
 typedef struct gbperm_rep_batch gbperm_rep_batch;
 int gbperm_rep_batch_create(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mults,
                             int64_t ncol, const int64_t* row_mults, int64_t nrow, int64_t count, int arith,
                             gbperm_rep_batch** out);
 int gbperm_rep_batch_run(gbperm_rep_batch* plan, double* out, gbperm_stats* stats);
 int gbperm_rep_batch_run_dev(gbperm_rep_batch* plan, void* d_out, void* stream);
-int gbperm_rep_batch_info(const gbperm_rep_batch* plan, double* steps, double* flops, int64_t* items);
+int gbperm_rep_batch_info(const gbperm_rep_batch* plan, double* steps, double* flops, double* mul_ops,
+                          int64_t* items);
 void gbperm_rep_batch_destroy(gbperm_rep_batch* plan);
 
 /* ------------------------------------------------- batched permanents */
@@ -265,15 +285,18 @@ void gbperm_sampler_destroy(gbperm_sampler* s);
 /* ----------------------------------------------- permanent + gradient */
 /* Permanent of an n x n matrix and its full gradient G[k][l] = dperm/da_kl
  * (= perm of A without row k and column l) in one Gray-code sweep, for
- * n <= 32, with the double-float product.  No reference counterpart: this is
- * the adjoint of BBFGPermanentCalculator::calculate
- * (BBFGPermanentCalculator.hpp:87-235).  grad receives n x n complex128,
- * row-major.  GBPERM_ERR_TOO_LARGE when n > 32 or when the matrix's dynamic
- * range does not fit the double-float product. */
+ * n <= 32.  No reference counterpart: this is the adjoint of
+ * BBFGPermanentCalculator::calculate (BBFGPermanentCalculator.hpp:87-235).
+ * grad receives n x n complex128, row-major.  Product ("grad.arith"): the
+ * double-float sweep, recomputed on the device by the integer-mantissa sweep
+ * when the matrix's dynamic range fails the double-float range check or the
+ * permanent's error estimate exceeds 1e-10 (stats.arith then reports FX64);
+ * or the integer-mantissa sweep alone.  GBPERM_ERR_TOO_LARGE when n > 32. */
 int gbperm_perm_grad(const double* A, int64_t n, int64_t ld, double* perm, double* perm_dd, double* grad,
                      gbperm_stats* stats);
 size_t gbperm_perm_grad_workspace_size(int64_t n);
-/* Device-pointer form; on a range-check failure perm and grad are NaN. */
+/* Device-pointer form: the same products and the same on-device
+ * recomputation, with no host round trip. */
 int gbperm_perm_grad_dev(const void* dA, int64_t n, int64_t ld, void* d_perm, void* d_perm_dd, void* d_grad,
                          void* workspace, size_t workspace_bytes, void* stream);
 /* Batch of `count` n x n matrices in one set of launches (no reference

@@ -108,7 +108,7 @@ _SIGNATURES = [
     ("gbperm_rep_batch_run", ctypes.c_int, [_P, _P, _P]),
     ("gbperm_rep_batch_run_dev", ctypes.c_int, [_P, _P, _P]),
     ("gbperm_rep_batch_info", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
-                                              ctypes.POINTER(_I64)]),
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)]),
     ("gbperm_rep_batch_destroy", None, [_P]),
     ("gbperm_sampler_create", ctypes.c_int, [_P, _I64, _I64, ctypes.c_uint64, ctypes.c_int,
                                               ctypes.POINTER(ctypes.c_void_p)]),
@@ -401,9 +401,10 @@ class RepBatchPlan:
         check(load().gbperm_rep_batch_run_dev(self._h, _P(d_out_ptr), _P(stream_ptr or 0)))
 
     def info(self):
-        steps, flops, items = ctypes.c_double(), ctypes.c_double(), _I64()
-        check(load().gbperm_rep_batch_info(self._h, ctypes.byref(steps), ctypes.byref(flops), ctypes.byref(items)))
-        return {"steps": steps.value, "flops": flops.value, "items": items.value}
+        steps, flops, mul_ops, items = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), _I64()
+        check(load().gbperm_rep_batch_info(self._h, ctypes.byref(steps), ctypes.byref(flops), ctypes.byref(mul_ops),
+                                           ctypes.byref(items)))
+        return {"steps": steps.value, "flops": flops.value, "mul_ops": mul_ops.value, "items": items.value}
 
     def close(self):
         if self._h:

@@ -413,7 +413,7 @@ struct gbperm_rep_batch {
     long long count = 0;        // state pairs
     int ninst = 0, nitems = 0;  // device instances and work items
     int cpl = 8, grp = 1, grid = 1;
-    double steps = 0.0, flops = 0.0;
+    double steps = 0.0, flops = 0.0, mul_ops = 0.0;
     void* dbuf = nullptr;
     RArgs args{};
     int* d_index = nullptr;
@@ -495,6 +495,7 @@ int gbperm_rep_batch_create(const double* A, int64_t rows, int64_t cols, int64_t
         repeated_low_digits(&h, [spi](unsigned long long) { return (unsigned long long)spi; }, 8.0);
         p->steps += h.steps;
         p->flops += h.flops;
+        p->mul_ops += 12.0 * (double)(h.photons - 1) * h.steps;
     }
     // instances by cost, largest first; an instance's items are contiguous
     std::vector<int> order(hs.size());
@@ -673,10 +674,12 @@ int gbperm_rep_batch_run_dev(gbperm_rep_batch* p, void* d_out, void* stream) {
     return e == cudaSuccess ? GBPERM_OK : cuda_fail(e, "gbperm_rep_batch_run_dev");
 }
 
-int gbperm_rep_batch_info(const gbperm_rep_batch* p, double* steps, double* flops, int64_t* items) {
+int gbperm_rep_batch_info(const gbperm_rep_batch* p, double* steps, double* flops, double* mul_ops,
+                          int64_t* items) {
     if (!p) return fail(GBPERM_ERR_ARG, "gbperm_rep_batch_info: null plan");
     if (steps) *steps = p->steps;
     if (flops) *flops = p->flops;
+    if (mul_ops) *mul_ops = p->mul_ops;
     if (items) *items = p->nitems;
     return GBPERM_OK;
 }

@@ -156,6 +156,12 @@ static void plain_geometry(int rows, int grid_full, int seg_threads, int* grid, 
     *seg_log2 = l;
 }
 
+int plain_arith(int64_t rows, int64_t cols, int arith) {
+    if (arith != GBPERM_ARITH_DF32) return arith;
+    if (cols > kDfMaxCols || (rows == cols && rows > g_opt.df_max_rows.load())) return GBPERM_ARITH_FX64;
+    return arith;
+}
+
 PlainPlan plan_plain(int rows, int cols, int arith) {
     PlainPlan p;
     p.df = arith == GBPERM_ARITH_DF32;
@@ -163,14 +169,17 @@ PlainPlan plan_plain(int rows, int cols, int arith) {
     int dev = 0;
     cudaGetDevice(&dev);
     int sms = device_sms(dev);
+    // the double-float kernel's twin is the integer-mantissa kernel: it
+    // recomputes on the device when the range check fails or the estimate
+    // is above the bar
+    if (p.df) p.fx = true;
     if (p.fx) {
-        // the integer-mantissa kernel runs alone: no FP64 twin to plan
         fx_shape(cols, (int)g_opt.plain_fx_group.load(), &p.cpl_fx, &p.grp_fx);
         plain_geometry(rows, sms * plain_fx_blocks_per_sm(rows, p.cpl_fx, p.grp_fx), p.grp_fx, &p.grid_fx,
                        &p.seg_log2_fx);
-        return p;
+    } else {
+        plain_geometry(rows, sms * plain_blocks_per_sm(rows, cols), 1, &p.grid, &p.seg_log2);
     }
-    plain_geometry(rows, sms * plain_blocks_per_sm(rows, cols), 1, &p.grid, &p.seg_log2);
     if (p.df) {
         df_shape(cols, (int)g_opt.plain_df_group.load(), &p.cpl, &p.grp);
         plain_geometry(rows, sms * plain_df_blocks_per_sm(rows, p.cpl, p.grp), p.grp, &p.grid_df, &p.seg_log2_df);
@@ -220,29 +229,30 @@ int run_plain_dev(const double2* dA, int64_t ld, int rows, int cols, void* ws, s
     pa.exp_fp64_out = pa.exp_out + 1;
     cudaError_t e = launch_prepare(pa, st);
     if (e != cudaSuccess) return cuda_fail(e, "prepare launch");
-    if (plan.fx) {
-        e = launch_plain_fx(pa.a1, pa.a2, pa.exp_out, rows, cols, plan.cpl_fx, plan.grp_fx, plan.grid_fx,
-                            plan.seg_log2_fx, base + w.kern, d_out2, d_out4, st);
-        if (e != cudaSuccess) return cuda_fail(e, "plain fx launch");
-        if (d_err) {
-            e = cudaMemsetAsync(d_err, 0, sizeof(double), st);
-            if (e != cudaSuccess) return cuda_fail(e, "plain fx error slot");
-        }
-        return GBPERM_OK;
-    }
     if (plan.df) {
         // the double-float kernel returns at once if the device range check
-        // failed; its FP64 twin below returns at once unless that check
-        // failed or the double-float result's error estimate was above the bar
+        // failed; its integer-mantissa twin below returns at once unless that
+        // check failed or the double-float result's error estimate was above
+        // the bar
         double* err = d_err ? d_err : reinterpret_cast<double*>(base + w.scale + 8);
         e = cudaMemsetAsync(err, 0, sizeof(double), st);
         if (e != cudaSuccess) return cuda_fail(e, "plain df error slot");
         e = launch_plain_df(pa.a1, pa.a2, pa.exp_out, pa.df_info, rows, cols, plan.cpl, plan.grp, plan.grid_df,
                             plan.seg_log2_df, base + w.kern, d_out2, d_out4, err, g_opt.df_escalate.load() != 0, st);
         if (e != cudaSuccess) return cuda_fail(e, "plain df launch");
+    } else if (plan.fx && d_err) {
+        e = cudaMemsetAsync(d_err, 0, sizeof(double), st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain fx error slot");
     }
-    e = launch_plain(pa.a1, pa.a2, pa.exp_fp64_out, plan.df ? pa.df_info : nullptr, rows, cols, plan.grid,
-                     plan.seg_log2, base + w.kern, d_out2, d_out4, st);
+    if (plan.fx) {
+        // scaled by the exponent without the double-float boost
+        e = launch_plain_fx(pa.a1, pa.a2, pa.exp_fp64_out, plan.df ? pa.df_info : nullptr, rows, cols, plan.cpl_fx,
+                            plan.grp_fx, plan.grid_fx, plan.seg_log2_fx, base + w.kern, d_out2, d_out4, st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain fx launch");
+        return GBPERM_OK;
+    }
+    e = launch_plain(pa.a1, pa.a2, pa.exp_fp64_out, nullptr, rows, cols, plan.grid, plan.seg_log2, base + w.kern,
+                     d_out2, d_out4, st);
     if (e != cudaSuccess) return cuda_fail(e, "plain launch");
     return GBPERM_OK;
 }
@@ -299,9 +309,9 @@ int64_t gbperm_get_option(const char* key) {
 size_t gbperm_perm_workspace_size(int64_t rows, int64_t cols) {
     if (rows <= 0 || cols <= 0 || rows > GBPERM_MAX_DIM || cols > GBPERM_MAX_DIM) return 256;
     // the largest of the arithmetics' needs (grids may differ)
-    PlainPlan plan = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
-    PlainPlan pfx = plan_plain((int)rows, (int)cols, GBPERM_ARITH_FX64);
-    const int g = plan.max_grid() > pfx.max_grid() ? plan.max_grid() : pfx.max_grid();
+    PlainPlan plan = plan_plain((int)rows, (int)cols, cols <= kDfMaxCols ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FX64);
+    PlainPlan p64 = plan_plain((int)rows, (int)cols, GBPERM_ARITH_FP64);
+    const int g = plan.max_grid() > p64.max_grid() ? plan.max_grid() : p64.max_grid();
     return plain_ws_layout((int)rows, (int)cols, g, nullptr);
 }
 
@@ -328,8 +338,7 @@ int gbperm_perm_dev(const void* dA, int64_t rows, int64_t cols, int64_t ld, int 
         return fail(GBPERM_ERR_TOO_LARGE, "gbperm_perm_dev: matrix larger than 64 x 64");
     if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
         return fail(GBPERM_ERR_ARG, "gbperm_perm_dev: workspace must be 256-byte aligned");
-    const int a = (arith == GBPERM_ARITH_DF32 && cols > kDfMaxCols) ? GBPERM_ARITH_FP64 : arith;
-    PlainPlan plan = plan_plain((int)rows, (int)cols, a);
+    PlainPlan plan = plan_plain((int)rows, (int)cols, plain_arith(rows, cols, arith));
     return run_plain_dev(static_cast<const double2*>(dA), ld, (int)rows, (int)cols, workspace,
                          workspace_bytes, static_cast<double*>(d_out), static_cast<double*>(d_out_dd), st,
                          plan);
@@ -352,13 +361,15 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
     }
     if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_perm: unknown arithmetic");
+    // the double-float product where the size rule and the host range check
+    // allow it, else the integer-mantissa product alone
+    const int a = plain_arith(rows, cols, arith);
     bool df = false;
     int boost = 0;
-    if (arith == GBPERM_ARITH_DF32 && cols <= kDfMaxCols)
-        df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost, rows == cols);
-    const bool fx = arith == GBPERM_ARITH_FX64;
+    if (a == GBPERM_ARITH_DF32) df = df_boost(A, rows, cols, ld, nullptr, nullptr, &boost, rows == cols);
+    const bool fx = a == GBPERM_ARITH_FX64 || (a == GBPERM_ARITH_DF32 && !df);
     PlainPlan plan = plan_plain((int)rows, (int)cols,
-                                fx ? GBPERM_ARITH_FX64 : (df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64));
+                                df ? GBPERM_ARITH_DF32 : (fx ? GBPERM_ARITH_FX64 : GBPERM_ARITH_FP64));
     size_t mat_bytes = align_up((size_t)rows * cols * sizeof(double2), 256);
     size_t ws = plain_ws_layout((int)rows, (int)cols, plan.max_grid(), nullptr);
     ThreadCtx& c = thread_ctx();
@@ -390,13 +401,14 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         stats->steps = std::ldexp(1.0, (int)rows - 1);
         stats->flops = 8.0 * (double)cols * stats->steps;
         stats->launches = df ? 3 : 2;
-        stats->grid = fx ? plan.grid_fx : (df ? plan.grid_df : plan.grid);
-        stats->seg_log2 = fx ? plan.seg_log2_fx : (df ? plan.seg_log2_df : plan.seg_log2);
-        // h[6]: the double-float estimate, -1 when the range check sent the
-        // matrix to the FP64 kernel; above the bar the FP64 twin recomputed
+        stats->grid = df ? plan.grid_df : (fx ? plan.grid_fx : plan.grid);
+        stats->seg_log2 = df ? plan.seg_log2_df : (fx ? plan.seg_log2_fx : plan.seg_log2);
+        // h[6]: the double-float estimate, -1 when the device range check
+        // sent the matrix to the twin; above the bar the integer-mantissa
+        // twin recomputed
         const bool ran_df = df && h[6] >= 0.0;
         const bool used_df = ran_df && (h[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
-        stats->arith = fx ? GBPERM_ARITH_FX64 : (used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
+        stats->arith = used_df ? GBPERM_ARITH_DF32 : (fx ? GBPERM_ARITH_FX64 : GBPERM_ARITH_FP64);
         stats->err_est = ran_df ? h[6] : 0.0;
     }
     return GBPERM_OK;

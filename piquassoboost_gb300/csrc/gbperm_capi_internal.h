@@ -24,6 +24,11 @@ struct Options {
     std::atomic<int64_t> df_escalate{1};
     std::atomic<int64_t> plain_fx_group{0};
     std::atomic<int64_t> grad_arith{1};
+    // the double-float product is tried first only up to these sizes (plain:
+    // rows of a square matrix; repeated and pmf: photons); above them its
+    // error estimate mostly exceeds 1e-10 and the accurate product runs alone
+    std::atomic<int64_t> df_max_rows{36};
+    std::atomic<int64_t> df_max_photons{24};
     std::atomic<int64_t>* find(const char* key) {
         if (!std::strcmp(key, "plain.seg_log2")) return &plain_seg_log2;
         if (!std::strcmp(key, "plain.grid")) return &plain_grid;
@@ -34,6 +39,8 @@ struct Options {
         if (!std::strcmp(key, "df.escalate")) return &df_escalate;
         if (!std::strcmp(key, "plain.fx_group")) return &plain_fx_group;
         if (!std::strcmp(key, "grad.arith")) return &grad_arith;
+        if (!std::strcmp(key, "df.max_rows")) return &df_max_rows;
+        if (!std::strcmp(key, "df.max_photons")) return &df_max_photons;
         return nullptr;
     }
 };
@@ -62,7 +69,7 @@ struct PlainPlan {
     int grid_df = 1;
     int seg_log2_df = 0;
     int cpl = 8, grp = 1;  // double-float lane-group shape
-    bool fx = false;       // integer-mantissa kernel (runs alone, no FP64 twin)
+    bool fx = false;       // integer-mantissa kernel: alone, or as the double-float kernel's twin
     int grid_fx = 1;
     int seg_log2_fx = 0;
     int cpl_fx = 8, grp_fx = 1;
@@ -79,6 +86,9 @@ struct PlainWs {
 // arith: GBPERM_ARITH_*; the caller maps DF32 to FP64 beyond kDfMaxCols or
 // when the host range check fails
 PlainPlan plan_plain(int rows, int cols, int arith);
+// The arithmetic a plain request runs: DF32 becomes FX64 beyond kDfMaxCols
+// columns or above the df.max_rows size rule
+int plain_arith(int64_t rows, int64_t cols, int arith);
 size_t plain_ws_layout(int rows, int cols, int grid, PlainWs* w);
 // d_err: optional device double that receives the double-float product's
 // relative rounding-error estimate (0 when the FP64 product runs)

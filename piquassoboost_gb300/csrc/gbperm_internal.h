@@ -100,14 +100,16 @@ cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* ex
                          double* out2, double* out4, cudaStream_t st);
 
 // Integer-mantissa product (perm_plain_fx.cu): lane-group shape for a column
-// count, occupancy and launch.  No range check and no FP64 twin.
+// count, occupancy and launch.  No range check.  gate: the double-float
+// kernel's {boost, ok} flags when launched as its twin (the kernel returns at
+// once while ok is set), else null.
 // group: 0 = by column count (lane pairs up to 40 columns), 4 = lane quads
 // from 22 columns on
 void fx_shape(int cols, int group, int* cpl, int* grp);
 int plain_fx_blocks_per_sm(int rows, int cpl, int grp);
-cudaError_t launch_plain_fx(const longlong2* a1, const longlong2* a2, const int* exp_in, int rows, int cols,
-                            int cpl, int grp, int grid, int seg_log2, void* ws, double* out2, double* out4,
-                            cudaStream_t st);
+cudaError_t launch_plain_fx(const longlong2* a1, const longlong2* a2, const int* exp_in, const int* gate, int rows,
+                            int cols, int cpl, int grp, int grid, int seg_log2, void* ws, double* out2,
+                            double* out4, cudaStream_t st);
 
 // Range boost o for the double-float product (host): columns are first
 // scaled to their L1 bound (< 1); o then centres the typical term

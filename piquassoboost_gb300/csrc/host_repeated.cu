@@ -288,17 +288,18 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         if (out_dd) out_dd[0] = out_dd[1] = out_dd[2] = out_dd[3] = NAN;
         return GBPERM_OK;
     }
-    // double-float product when requested and the dynamic range allows it
+    // double-float product when requested, within the size rule, and the
+    // dynamic range allows it; otherwise (and as its twin) the
+    // integer-mantissa product
     bool df = false;
     int dcpl = 0, dgrp = 0, grid_df = 1;
-    if (arith == GBPERM_ARITH_DF32 && h.C <= kDfMaxCols) {
+    if (arith == GBPERM_ARITH_DF32 && h.C <= kDfMaxCols && h.photons <= g_opt.df_max_photons.load()) {
         int boost = 0;
         std::vector<int> cw(h.cpow.begin(), h.cpow.end());
         df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), cw.data(), &boost);
     }
     if (df) repeated_df_shape(h.C, &dcpl, &dgrp);
-    // integer-mantissa product: runs alone (no FP64 twin)
-    const bool fx = arith == GBPERM_ARITH_FX64;
+    const bool fx = arith == GBPERM_ARITH_FX64 || arith == GBPERM_ARITH_DF32;
     int xcpl = 0, xgrp = 0, grid_fx = 1;
     if (fx) repeated_fx_shape(h.C, &xcpl, &xgrp);
     int dev = 0;
@@ -316,11 +317,11 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         [&](unsigned long long P) {
             RepArgs t = a;
             t.P = P;
-            if (fx) return sms * (unsigned long long)repeated_fx_blocks_per_sm(t, xcpl, xgrp) * (128ull / xgrp);
             if (df) return sms * (unsigned long long)repeated_df_blocks_per_sm(t, dcpl, dgrp) * (128ull / dgrp);
+            if (fx) return sms * (unsigned long long)repeated_fx_blocks_per_sm(t, xcpl, xgrp) * (128ull / xgrp);
             return sms * (unsigned long long)repeated_blocks_per_sm(t) * 128ull;
         },
-        fx ? 4.0 : (df ? 6.5 : 2.0));
+        df ? 6.5 : (fx ? 4.0 : 2.0));
     a.q = h.q;
     a.P = h.P;
     a.nseg = h.nseg;
@@ -399,13 +400,15 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
             e = launch_repeated_df(a, dcpl, dgrp, grid_df, base + w.kern, g_opt.df_escalate.load() != 0, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: df launch");
     }
+    // the twin (or the product alone) scales by the exponent without the
+    // double-float boost; as the twin it returns at once unless the range
+    // check failed or the estimate was above the bar
+    a.exp_in = pa.exp_fp64_out;
+    a.err_out = nullptr;
     if (fx) {
         e = launch_repeated_fx(a, xcpl, xgrp, grid_fx, base + w.kern, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: fx launch");
     } else {
-        // the FP64 twin scales by the exponent without the double-float boost
-        a.exp_in = pa.exp_fp64_out;
-        a.err_out = nullptr;
         e = launch_repeated(a, grid, base + w.kern, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_repeated: launch");
     }
@@ -424,11 +427,11 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
         stats->steps = h.steps;
         stats->flops = h.flops;
         stats->launches = df ? 3 : 2;
-        stats->grid = fx ? grid_fx : (df ? grid_df : grid);
+        stats->grid = df ? grid_df : (fx ? grid_fx : grid);
         stats->seg_log2 = h.q;
         const bool ran_df = df && hres[6] >= 0.0;
         const bool used_df = ran_df && (hres[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
-        stats->arith = fx ? GBPERM_ARITH_FX64 : (used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
+        stats->arith = used_df ? GBPERM_ARITH_DF32 : (fx ? GBPERM_ARITH_FX64 : GBPERM_ARITH_FP64);
         stats->err_est = ran_df ? hres[6] : 0.0;
     }
     return GBPERM_OK;

@@ -33,6 +33,9 @@ __global__ void __launch_bounds__(kThreads, (CPL <= 16 ? 4 : 3)) plain_fx_kernel
     longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);
     longlong2* s_a2 = s_a1 + p.rows * NP;
     const int rows = p.rows, cols = p.cols;
+    // launched as the twin of the double-float kernel: run only when the
+    // range check or the error estimate handed the permanent over
+    if (p.df_info && p.df_info[1] != 0) return;
     for (int e = threadIdx.x; e < rows * NP; e += blockDim.x) {
         int r = e / NP, j = e % NP;
         longlong2 z = make_longlong2(0, 0);
@@ -257,9 +260,9 @@ int plain_fx_blocks_per_sm(int rows, int cpl, int grp) {
     return 1;
 }
 
-cudaError_t launch_plain_fx(const longlong2* a1, const longlong2* a2, const int* exp_in, int rows, int cols,
-                            int cpl, int grp, int grid, int seg_log2, void* ws, double* out2, double* out4,
-                            cudaStream_t st) {
+cudaError_t launch_plain_fx(const longlong2* a1, const longlong2* a2, const int* exp_in, const int* gate, int rows,
+                            int cols, int cpl, int grp, int grid, int seg_log2, void* ws, double* out2,
+                            double* out4, cudaStream_t st) {
     PlainArgs a;
     a.a1 = a1;
     a.a2 = a2;
@@ -271,7 +274,7 @@ cudaError_t launch_plain_fx(const longlong2* a1, const longlong2* a2, const int*
     a.block_part = reinterpret_cast<cdd*>(w);
     a.done = reinterpret_cast<unsigned int*>(w + align_up((size_t)grid * sizeof(cdd), 256));
     a.exp_in = exp_in;
-    a.df_info = nullptr;
+    a.df_info = gate;
     a.out2 = out2;
     a.out4 = out4;
     cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);

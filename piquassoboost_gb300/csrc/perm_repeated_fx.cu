@@ -33,6 +33,9 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
     __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
     __shared__ long long s_stride[kMaxDigits];
     const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    // launched as the twin of the double-float kernel: run only when the
+    // range check or the error estimate handed the permanent over
+    if (p.df_info && p.df_info[1] != 0) return;
     for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
         int r = e / NP, j = e % NP;
         s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
