@@ -773,7 +773,7 @@ def _batched_multiplicity(args, rank, world, torch):
                                         "arith": "fx", "batched_speedup": seq_ms / avg,
                                         "max_rel_diff_vs_batched": diff},
                "steps_walked_over_expanded": info["steps"] / float(np.sum(2.0 ** (ks - 1))),
-               "kernel_ms": kms}, clocks=clocks)
+               "kernel_ms": kms}, clocks=clocks, dtype="int64")
     plan.close()
     return 0
 

@@ -105,9 +105,11 @@ int gbperm_device_count(void);
  *                         it (stats.err_est still reports the estimate)
  *   "df.max_rows"         GBPERM_ARITH_DF32 on a square plain matrix with more rows runs the
  *                         integer-mantissa product alone (default 36)
- *   "df.max_photons"      GBPERM_ARITH_DF32 on a repeated permanent (or pmf layer) with more
- *                         photons runs the integer-mantissa (pmf: FP64) product alone
- *                         (default 24)
+ *   "df.max_photons"      GBPERM_ARITH_DF32 on a repeated permanent with more photons runs
+ *                         the integer-mantissa product alone (default 24)
+ *   "df.pmf_max_photons"  GBPERM_ARITH_DF32 on a pmf layer whose sample has more photons
+ *                         runs the FP64 layer alone (default 0: the double-float layer
+ *                         measured no faster up to 20 photons and escalates from 24 on)
  *   "grad.arith"          product of the gradient sweep: 1 (default, double-float with the
  *                         integer-mantissa twin) or 2 (integer-mantissa throughout)
  */

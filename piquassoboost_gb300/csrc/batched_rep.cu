@@ -166,6 +166,12 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
         const unsigned char* __restrict__ sq = p.seq + in.t_off;
         // this lane's real columns (0 for a lane past the instance's columns)
         const int nr = max(0, min(CPL, C - j0));
+        // bit c: this lane's column c has power > 1 (loaded once per item;
+        // the step loop runs the common power-1 multiply unconditionally)
+        unsigned int extra = 0u;
+#pragma unroll
+        for (int c = 0; c < CPL; ++c)
+            if (c < nr && __ldg(&cpow[j0 + c]) > 1) extra |= 1u << c;
         const unsigned long long h_raw = item.base + 2ull * (unsigned long long)grp + (unsigned long long)item.par;
         const bool active = h_raw < in.nseg && io.finite;
         const unsigned long long h = h_raw < in.nseg ? h_raw : item.base + (unsigned long long)item.par;
@@ -274,18 +280,22 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
             for (int c = 0; c < CPL; ++c) {
                 if (c < nr) {
                     // a column of power e multiplies its chain e times by the
-                    // same column factor (inline: powers are mostly 1 or 2)
-                    const int e = __ldg(&cpow[j0 + c]);
+                    // same column factor; powers above 1 are rare
                     const fxl y = fx_col(cre[c], cim[c]);
-                    int t = 0;
                     if (c < 2) {
                         sig += fx_norm_col(cre[c], cim[c], ch[c]);
-                        t = 1;
-                    }
-                    for (; t < e; ++t) {
+                    } else {
                         long long rr, ri;
                         fx_mul(ch[c & 1], y, rr, ri);
                         sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                    }
+                    if ((extra >> c) & 1u) {
+                        const int e = __ldg(&cpow[j0 + c]);
+                        for (int t = 1; t < e; ++t) {
+                            long long rr, ri;
+                            fx_mul(ch[c & 1], y, rr, ri);
+                            sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                        }
                     }
                 }
             }
@@ -492,6 +502,7 @@ int gbperm_rep_batch_create(const double* A, int64_t rows, int64_t cols, int64_t
     const int spi = 32 / p->grp;
     // segment length per instance: one item's SPI lane groups share it
     for (RepHost& h : hs) {
+        deal_columns_by_power(&h, p->grp, p->cpl);
         repeated_low_digits(&h, [spi](unsigned long long) { return (unsigned long long)spi; }, 8.0);
         p->steps += h.steps;
         p->flops += h.flops;

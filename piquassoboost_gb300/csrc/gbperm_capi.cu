@@ -401,14 +401,14 @@ int gbperm_perm(const double* A, int64_t rows, int64_t cols, int64_t ld, int ari
         stats->steps = std::ldexp(1.0, (int)rows - 1);
         stats->flops = 8.0 * (double)cols * stats->steps;
         stats->launches = df ? 3 : 2;
-        stats->grid = df ? plan.grid_df : (fx ? plan.grid_fx : plan.grid);
-        stats->seg_log2 = df ? plan.seg_log2_df : (fx ? plan.seg_log2_fx : plan.seg_log2);
+        stats->grid = df ? plan.grid_df : (plan.fx ? plan.grid_fx : plan.grid);
+        stats->seg_log2 = df ? plan.seg_log2_df : (plan.fx ? plan.seg_log2_fx : plan.seg_log2);
         // h[6]: the double-float estimate, -1 when the device range check
         // sent the matrix to the twin; above the bar the integer-mantissa
         // twin recomputed
         const bool ran_df = df && h[6] >= 0.0;
         const bool used_df = ran_df && (h[6] <= kDfEscalate || g_opt.df_escalate.load() == 0);
-        stats->arith = used_df ? GBPERM_ARITH_DF32 : (fx ? GBPERM_ARITH_FX64 : GBPERM_ARITH_FP64);
+        stats->arith = used_df ? GBPERM_ARITH_DF32 : (plan.fx ? GBPERM_ARITH_FX64 : GBPERM_ARITH_FP64);
         stats->err_est = ran_df ? h[6] : 0.0;
     }
     return GBPERM_OK;

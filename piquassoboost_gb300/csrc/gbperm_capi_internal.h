@@ -25,10 +25,15 @@ struct Options {
     std::atomic<int64_t> plain_fx_group{0};
     std::atomic<int64_t> grad_arith{1};
     // the double-float product is tried first only up to these sizes (plain:
-    // rows of a square matrix; repeated and pmf: photons); above them its
-    // error estimate mostly exceeds 1e-10 and the accurate product runs alone
+    // rows of a square matrix; repeated and pmf: photons of the permanents);
+    // above them its error estimate mostly exceeds 1e-10 (plain, repeated)
+    // and the accurate product alone is faster than the double-float pass
+    // plus its twin.  For the pmf layer the double-float kernel measured no
+    // faster than the FP64 one up to 20 photons and escalated from 24 on, so
+    // its rule defaults to 0: the fast mode runs the FP64 layer
     std::atomic<int64_t> df_max_rows{36};
     std::atomic<int64_t> df_max_photons{24};
+    std::atomic<int64_t> df_pmf_max_photons{0};
     std::atomic<int64_t>* find(const char* key) {
         if (!std::strcmp(key, "plain.seg_log2")) return &plain_seg_log2;
         if (!std::strcmp(key, "plain.grid")) return &plain_grid;
@@ -41,6 +46,7 @@ struct Options {
         if (!std::strcmp(key, "grad.arith")) return &grad_arith;
         if (!std::strcmp(key, "df.max_rows")) return &df_max_rows;
         if (!std::strcmp(key, "df.max_photons")) return &df_max_photons;
+        if (!std::strcmp(key, "df.pmf_max_photons")) return &df_pmf_max_photons;
         return nullptr;
     }
 };
@@ -120,6 +126,13 @@ struct RepWs {
 int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const int64_t* col_mult,
                   int64_t ncol, const int64_t* row_mult, int64_t nrow, RepHost* h, double* trivial,
                   bool* is_trivial, bool allow_transpose, int col_surplus, bool chinhuh = false);
+// Reorder the product-side columns (M, cpow, col_src) for a kernel whose
+// lane groups of `group` lanes hold `cpl` contiguous columns each: the
+// columns sorted by power are dealt slot by slot across the lanes, so that
+// slot c of every lane holds nearly the same power and the lanes' extra
+// multiplies for powers above 1 line up.  A permutation of the columns
+// leaves the repeated permanent unchanged.
+void deal_columns_by_power(RepHost* h, int group, int cpl);
 // Split the Gray range into segments of P = prod_{i<q} (D_i + 1) steps: the
 // q low digits walk inside a segment from the tables wlow / seq, the high
 // digits are decoded once per segment.  q minimises

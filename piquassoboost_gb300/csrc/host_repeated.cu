@@ -172,6 +172,38 @@ int repeated_plan(const double* A, int64_t rows, int64_t cols, int64_t ld, const
     return GBPERM_OK;
 }
 
+void deal_columns_by_power(RepHost* h, int group, int cpl) {
+    const int C = h->C;
+    if (group <= 1 || C <= 1 || C > group * cpl) return;
+    // sorted by power, largest first; ties keep their order
+    std::vector<int> s(C);
+    for (int c = 0; c < C; ++c) s[c] = c;
+    std::stable_sort(s.begin(), s.end(), [h](int a, int b) { return h->cpow[a] > h->cpow[b]; });
+    // lane l holds positions [l cpl, l cpl + n_l); slot c of every lane in
+    // turn takes the next columns of the sorted list
+    std::vector<int> perm(C, -1);  // perm[new position] = old column
+    int next = 0;
+    for (int c = 0; c < cpl && next < C; ++c)
+        for (int l = 0; l < group && next < C; ++l) {
+            const int pos = l * cpl + c;
+            if (pos < C && c < std::min(cpl, C - l * cpl)) perm[pos] = s[next++];
+        }
+    std::vector<double> M(h->M.size());
+    std::vector<int> cp(C), src(C);
+    for (int j = 0; j < C; ++j) {
+        const int o = perm[j];
+        for (int r = 0; r < h->R; ++r) {
+            M[2 * ((size_t)r * C + j)] = h->M[2 * ((size_t)r * C + o)];
+            M[2 * ((size_t)r * C + j) + 1] = h->M[2 * ((size_t)r * C + o) + 1];
+        }
+        cp[j] = h->cpow[o];
+        src[j] = h->col_src[o];
+    }
+    h->M.swap(M);
+    h->cpow.swap(cp);
+    h->col_src.swap(src);
+}
+
 void repeated_low_digits(RepHost* h, const std::function<unsigned long long(unsigned long long)>& slots,
                          double seg_cost) {
     const unsigned long long T = h->nseg * h->P;
@@ -302,6 +334,8 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
     const bool fx = arith == GBPERM_ARITH_FX64 || arith == GBPERM_ARITH_DF32;
     int xcpl = 0, xgrp = 0, grid_fx = 1;
     if (fx) repeated_fx_shape(h.C, &xcpl, &xgrp);
+    if (df) deal_columns_by_power(&h, dgrp, dcpl);
+    else if (fx) deal_columns_by_power(&h, xgrp, xcpl);
     int dev = 0;
     cudaGetDevice(&dev);
     const unsigned long long sms = (unsigned long long)device_sms(dev);

@@ -65,6 +65,13 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
     // real columns of this lane: contiguous from its first column (>= 1, the
     // host picks shapes with C > (GROUP - 1) * CPL)
     const int nr = C - j0 < CPL ? C - j0 : CPL;
+    // bit c: this lane's column c has power > 1 (the step loop runs the
+    // common power-1 multiply unconditionally); power 0 among the real
+    // columns cannot occur (the host drops empty columns)
+    unsigned int extra = 0u;
+#pragma unroll
+    for (int c = 0; c < CPL; ++c)
+        if (c < nr && s_cpow[j0 + c] > 1) extra |= 1u << c;
     const bool leader = (g == 0);
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
@@ -171,20 +178,24 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
             for (int c = 0; c < CPL; ++c) {
                 if (c < nr) {
                     // a column of power e multiplies its chain e times by the
-                    // same column factor (inline: powers are mostly 1 or 2);
-                    // power 0 among the real columns cannot occur (the host
-                    // drops empty columns)
-                    const int e = s_cpow[j0 + c];
+                    // same column factor (the host lays the columns out so
+                    // that column c of every lane group has nearly the same
+                    // power: the extra multiplies diverge little)
                     const fxl y = fx_col(cre[c], cim[c]);
-                    int t = 0;
                     if (c < 2) {
                         sig += fx_norm_col(cre[c], cim[c], ch[c]);
-                        t = 1;
-                    }
-                    for (; t < e; ++t) {
+                    } else {
                         long long rr, ri;
                         fx_mul(ch[c & 1], y, rr, ri);
                         sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                    }
+                    if ((extra >> c) & 1u) {
+                        const int e = s_cpow[j0 + c];
+                        for (int t = 1; t < e; ++t) {
+                            long long rr, ri;
+                            fx_mul(ch[c & 1], y, rr, ri);
+                            sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                        }
                     }
                 }
             }

@@ -821,10 +821,9 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         a.nd = h.nd;
         pmf_shape(C, &cpl, &grp);
         // double-float product for up to 32 columns (4 lanes x 8), up to the
-        // df.max_photons size rule (above it most layers' estimates exceed
-        // 1e-10), when the dynamic range allows; the device check decides
-        // between the twins
-        if (arith == GBPERM_ARITH_DF32 && grp == 4 && ns <= g_opt.df_max_photons.load()) {
+        // df.pmf_max_photons size rule, when the dynamic range allows; the
+        // device check decides between the twins
+        if (arith == GBPERM_ARITH_DF32 && grp == 4 && ns <= g_opt.df_pmf_max_photons.load()) {
             int boost = 0;
             df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), h.cpow.data(), &boost);
         }

@@ -18,6 +18,29 @@ with open(os.path.join(HERE, "golden", "reference_calculators.json")) as _f:
     PMF_GOLD = json.load(_f).get("pmf", [])
 
 
+@pytest.fixture(autouse=True)
+def _double_float_layers():
+    # the fast mode's pmf rule (df.pmf_max_photons, default 0) sends every
+    # layer to the FP64 kernel; lifted here so that "fast" exercises the
+    # double-float layer and its FP64 twin
+    nat.require_device()
+    nat.set_option("df.pmf_max_photons", 64)
+    yield
+    nat.set_option("df.pmf_max_photons", 0)
+
+
+def test_pmf_fast_default_rule_runs_fp64():
+    nat.set_option("df.pmf_max_photons", 0)
+    U = haar_unitary(12, 3)
+    cin = np.array([1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0])
+    sample = np.array([0, 2, 0, 1, 0, 0, 0, 1, 0, 0, 1, 0])
+    st = nat.Stats()
+    a, x = nat.compute_pmf(U, sample, cin, mode="fast", stats=st)
+    assert st.arith == nat.ARITH_FP64
+    b, y = nat.compute_pmf(U, sample, cin, mode="fp64")
+    assert np.array_equal(a, b) and np.array_equal(x, y)
+
+
 def _check(U, sample, cin, mode="fp64"):
     pmf, add = nat.compute_pmf(U, sample, cin, mode=mode)
     rpmf, radd = orc.compute_pmf(U, sample, cin, prec=1)
