@@ -146,7 +146,6 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
     const int lane = threadIdx.x & 31;
     const int g = lane % GROUP;
     const int grp = lane / GROUP;
-    const int j0 = g * CPL;
     long long cre[CPL], cim[CPL];
     for (;;) {
         int it = 0;
@@ -164,8 +163,13 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
         const longlong2* __restrict__ a2 = p.a2 + in.m_off;
         const double* __restrict__ wl = p.wlow + in.t_off;
         const unsigned char* __restrict__ sq = p.seq + in.t_off;
-        // this lane's real columns (0 for a lane past the instance's columns)
-        const int nr = max(0, min(CPL, C - j0));
+        // this lane's real columns: the instance's columns split evenly over
+        // the group (a warp runs the longest lane's columns, so an even split
+        // costs ceil(C / GROUP) column updates per step, not CPL); 0 for a
+        // lane past the instance's columns
+        const int cpl_i = (C + GROUP - 1) / GROUP;
+        const int j0 = g * cpl_i;
+        const int nr = max(0, min(cpl_i, C - j0));
         // bit c: this lane's column c has power > 1 (loaded once per item;
         // the step loop runs the common power-1 multiply unconditionally)
         unsigned int extra = 0u;
@@ -502,7 +506,7 @@ int gbperm_rep_batch_create(const double* A, int64_t rows, int64_t cols, int64_t
     const int spi = 32 / p->grp;
     // segment length per instance: one item's SPI lane groups share it
     for (RepHost& h : hs) {
-        deal_columns_by_power(&h, p->grp, p->cpl);
+        deal_columns_by_power(&h, p->grp, (h.C + p->grp - 1) / p->grp);
         repeated_low_digits(&h, [spi](unsigned long long) { return (unsigned long long)spi; }, 8.0);
         p->steps += h.steps;
         p->flops += h.flops;

@@ -61,10 +61,13 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
     __syncthreads();
 
     const int g = threadIdx.x % GROUP;
-    const int j0 = g * CPL;
-    // real columns of this lane: contiguous from its first column (>= 1, the
-    // host picks shapes with C > (GROUP - 1) * CPL)
-    const int nr = C - j0 < CPL ? C - j0 : CPL;
+    // the columns split evenly over the group (the warp runs the longest
+    // lane's columns)
+    const int cpl_i = (C + GROUP - 1) / GROUP;
+    const int j0 = g * cpl_i;
+    // real columns of this lane: contiguous from its first column (>= 1:
+    // C > (GROUP - 1) ceil(C / GROUP) for every shape the host picks)
+    const int nr = C - j0 < cpl_i ? C - j0 : cpl_i;
     // bit c: this lane's column c has power > 1 (the step loop runs the
     // common power-1 multiply unconditionally); power 0 among the real
     // columns cannot occur (the host drops empty columns)
