@@ -160,7 +160,7 @@ def host_threads() -> int:
 # product's plain kernel; the traffic is the fixed-point tables and the
 # per-block partial sums, so it does not grow with the Gray steps
 _TRAFFIC_PROFILES = {"fx": "plain_fx_kernel_n28.md", "fast": "plain_df_kernel_n36_launches.md",
-                     "fp64": "plain_kernel_fp64_n28.md"}
+                     "fp64": "plain_group_kernel_fp64_n28.md"}
 
 
 def traffic_from_profile(n: int, mode: str):
@@ -423,7 +423,7 @@ def run_ours(args, rank, world, local):
         d = {"kernel_ms": ms, "perm_per_s": len(ms) / (sum(ms) * 1e-3),
              "fp64_equivalent_tflops": flops / (statistics.mean(ms) * 1e-3) / 1e12}
         if mode == "fp64":
-            d.update({"dtype": "f64", "kernel": "plain_kernel",
+            d.update({"dtype": "f64", "kernel": "plain_group_kernel" if n > 8 else "plain_kernel",
                       "frac_of_fp64_peak": d["fp64_equivalent_tflops"] / peaks["fp64"]})
         elif mode == "fx":
             d.update({"dtype": "int64 mantissas (>= f64 accuracy)", "kernel": "plain_fx_kernel"})
@@ -463,7 +463,8 @@ def run_ours(args, rank, world, local):
     else:
         roof = {"bound": "fp64", "achieved": ach_flops, "peak": peaks["fp64"], "unit": "TFLOP/s",
                 "frac": ach_flops / peaks["fp64"], "traffic": traffic_from_profile(n, args.mode),
-                "kernel": ("plain_df_kernel" if args.mode == "fast" else "plain_kernel"),
+                "kernel": ("plain_df_kernel" if args.mode == "fast" else
+                           ("plain_group_kernel" if n > 8 else "plain_kernel")),
                 "work_per_launch": f"8 n 2^(n-1) = {flops:.4g} algorithmic FP64-equivalent flops",
                 "peak_source": "DFMA probe (gbperm_probe_peak kind 0), measured in this run"}
         if args.mode == "fast":

