@@ -75,9 +75,11 @@ def parse():
     if args.batch_count < 1 or not 8 <= args.batch_kmax <= 32:
         ap.error("--batch-count must be >= 1 and --batch-kmax in 8..32")
     if args.mode is None:
-        args.mode = {"plain": "fx", "repeated": "fx", "batched": "fx", "grad": "fast"}.get(args.workload, "fp64")
-    if args.mode == "fx" and args.workload not in ("plain", "repeated", "batched", "grad"):
-        ap.error("--mode fx: the integer-mantissa product serves the plain, repeated, batched and grad workloads")
+        args.mode = {"plain": "fx", "repeated": "fx", "batched": "fx", "grad": "fast", "pmf": "fx",
+                     "sampler": "fx"}.get(args.workload, "fp64")
+    if args.mode == "fx" and args.workload not in ("plain", "repeated", "batched", "grad", "pmf", "sampler"):
+        ap.error("--mode fx: the integer-mantissa product serves the plain, repeated, batched, grad, pmf and "
+                 "sampler workloads")
     if args.workload == "grad" and args.mode == "fp64":
         ap.error("--workload grad: the gradient sweep runs the 'fast' or the 'fx' product")
     return args
@@ -973,13 +975,23 @@ def _pmf(args, rank, world, torch):
     st = nat.Stats()
     for U, smp, cin in layers[:args.warmup]:
         nat.compute_pmf(U, smp, cin, mode=args.mode)
+    # the FP64 layer on the first timed instance, for the products' ratio
+    ref = {}
+    if args.mode != "fp64":
+        U, smp, cin = layers[args.warmup]
+        s64 = nat.Stats()
+        a64, x64 = nat.compute_pmf(U, smp, cin, mode="fp64", stats=s64)
+        ref = {"ms": s64.kernel_ms, "pmf": a64, "addends": x64}
     kms, flops, nperm = [], 0.0, 0
     clk = ClockSampler(torch.cuda.current_device())
     clk.start()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    first = None
     for U, smp, cin in layers[args.warmup:]:
-        nat.compute_pmf(U, smp, cin, mode=args.mode, stats=st)
+        res = nat.compute_pmf(U, smp, cin, mode=args.mode, stats=st)
+        if first is None:
+            first = res
         kms.append(st.kernel_ms)
         flops += st.flops
         nperm += int(np.count_nonzero(cin))
@@ -1005,12 +1017,18 @@ def _pmf(args, rank, world, torch):
         _line(args, world, value, "layers/s", 1000 * wall / args.steps,
               {"workload": workload_desc(args), "arith": args.mode, "l2": "inputs < 100 KB; compute-bound, no flush"},
               _roof(flops / args.steps, statistics.mean(kms), peak,
-                    "pmf_df_kernel (FP64-equivalent flops of the FP64 form)" if args.mode == "fast"
-                    else "pmf_kernel (executed FP64 flops)"),
+                    {"fast": "pmf_df_kernel (FP64-equivalent flops of the FP64 form)",
+                     "fx": "pmf_fx_kernel (FP64-equivalent flops of the FP64 form; computes on the integer pipes)"}
+                    .get(args.mode, "pmf_kernel (executed FP64 flops)")),
               cpu, {"value": e2e, "unit": "layers/s", "h2d_bytes_per_step": 60 * 60 * 16 + 2 * 60 * 8,
-                    "d2h_bytes_per_step": 60 * 8 + 60 * 16}, (5 if args.mode == "fast" else 3) * args.steps,
-              {"permanents_per_s": value * nperm / args.steps,
-               "kernel_ms": kms}, clocks=clocks)
+                    "d2h_bytes_per_step": 60 * 8 + 60 * 16}, st.launches * args.steps,
+              {"permanents_per_s": value * nperm / args.steps, "kernel_ms": kms,
+               "fp64_layer": ({"ms": ref["ms"], "speedup": ref["ms"] / kms[0],
+                               "max_rel_diff_addends": float(np.max(np.abs(first[1] - ref["addends"])) /
+                                                             np.max(np.abs(ref["addends"]))),
+                               "max_abs_diff_pmf": float(np.max(np.abs(first[0] - ref["pmf"])))}
+                              if ref else None)},
+              clocks=clocks, dtype={"fx": "int64", "fp64": "f64", "fast": "f32x2"}[args.mode])
     return 0
 
 
@@ -1179,7 +1197,7 @@ def _sampler(args, rank, world, torch):
 
     U, inp = _sampler_instance(args.seed + 1000 * rank)
     peak = nat.probe_peak("fp64")
-    smp = nat.Sampler(U, seed=args.seed + rank, mode="fp64")
+    smp = nat.Sampler(U, seed=args.seed + rank, mode=args.mode)
     first = smp.simulate(inp, 1)                 # the oracle's first sample is checked below
     for _ in range(max(0, args.warmup - 1)):
         smp.simulate(inp, 1)
@@ -1204,12 +1222,15 @@ def _sampler(args, rank, world, torch):
                          f"{os.cpu_count()} threads)"}
     if rank == 0:
         _line(args, world, value, "samples/s", 1000 * wall / args.steps,
-              {"workload": workload_desc(args), "arith": "fp64", "l2": "inputs < 30 KB; compute- and launch-bound"},
-              _roof(st.flops, st.kernel_ms, peak, "pmf_kernel (all layers of the timed samples)"),
+              {"workload": workload_desc(args), "arith": args.mode,
+               "l2": "inputs < 30 KB; compute- and launch-bound"},
+              _roof(st.flops, st.kernel_ms, peak, {"fx": "pmf_fx_kernel", "fast": "pmf_df_kernel"}.get(
+                  args.mode, "pmf_kernel") + " (all layers of the timed samples; FP64-equivalent flops)"),
               cpu, {"value": value, "unit": "samples/s",
                     "h2d_bytes_per_step": _SAMPLER_PHOTONS * (_SAMPLER_MODES * _SAMPLER_MODES * 16 + 32 * _SAMPLER_MODES),
                     "d2h_bytes_per_step": _SAMPLER_PHOTONS * _SAMPLER_MODES * 24},
-              st.launches, {"gpu_kernel_ms": st.kernel_ms, "first_sample_matches_oracle": match}, clocks=clocks)
+              st.launches, {"gpu_kernel_ms": st.kernel_ms, "first_sample_matches_oracle": match}, clocks=clocks,
+              dtype={"fx": "int64", "fp64": "f64", "fast": "f32x2"}[args.mode])
     smp.close()
     return 0
 

@@ -55,8 +55,8 @@ extern "C" {
                                 mantissas in 31-bit limbs, 55-57 significant bits per
                                 complex multiply (the FP64 product keeps 53); any
                                 dynamic range, no FP64 fallback needed.  Plain and
-                                repeated permanents, the gradient sweep and the
-                                repeated batch plans */
+                                repeated permanents, the gradient sweep, the
+                                repeated batch plans, pmf layers and the sampler */
 
 /* Largest supported matrix side (columns of the product, rows of the Gray code). */
 #define GBPERM_MAX_DIM 64
@@ -108,8 +108,9 @@ int gbperm_device_count(void);
  *   "df.max_photons"      GBPERM_ARITH_DF32 on a repeated permanent with more photons runs
  *                         the integer-mantissa product alone (default 24)
  *   "df.pmf_max_photons"  GBPERM_ARITH_DF32 on a pmf layer whose sample has more photons
- *                         runs the FP64 layer alone (default 0: the double-float layer
- *                         measured no faster up to 20 photons and escalates from 24 on)
+ *                         runs the integer-mantissa layer (default 0: the double-float
+ *                         layer measured no faster than FP64 up to 20 photons and
+ *                         escalates from 24 on)
  *   "grad.arith"          product of the gradient sweep: 1 (default, double-float with the
  *                         integer-mantissa twin) or 2 (integer-mantissa throughout)
  */
@@ -253,8 +254,11 @@ int gbperm_perm_batched(const double* packed, const int64_t* rows, const int64_t
  * with one photon removed from mode l; addends (NULL or 2 m doubles)
  * receives the perm_l as complex128 (0 for empty input modes).  All perm_l
  * come from one Gray-code sweep over the sample.  arith as for the
- * permanents (the double-float product serves up to 32 occupied input modes
- * and falls back to FP64 beyond that or when the range check fails).  Up to
+ * permanents: GBPERM_ARITH_FX64 runs every product on integer mantissas
+ * (no twin); GBPERM_ARITH_DF32 runs the double-float product up to 32
+ * occupied input modes within the "df.pmf_max_photons" rule (recomputed in
+ * FP64 on the device when the range check fails or an estimate is above
+ * 1e-10) and the integer-mantissa layer otherwise.  Up to
  * 64 sample photons and 64 occupied input modes; a photon-count mismatch ->
  * GBPERM_ERR_STATE_SUM. */
 int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sample, const int64_t* current_input,
@@ -273,8 +277,9 @@ int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const int64_t* sa
  * sample first draws its surviving photon count from the binomial law with
  * eta = transmissivity^2.  The sampler keeps its own copy of U (m x m,
  * leading dimension ld) and its own generator (the reference shares one
- * generator across all strategy objects).  simulate writes nsamples rows of
- * m occupations (int64) into out; the input state has m entries. */
+ * generator across all strategy objects).  arith selects the pmf layers'
+ * product (gbperm_compute_pmf).  simulate writes nsamples rows of m
+ * occupations (int64) into out; the input state has m entries. */
 typedef struct gbperm_sampler gbperm_sampler;
 int gbperm_sampler_create(const double* U, int64_t m, int64_t ld, uint64_t seed, int arith, gbperm_sampler** out);
 int gbperm_sampler_set_matrix(gbperm_sampler* s, const double* U, int64_t m, int64_t ld);

@@ -347,8 +347,9 @@ def compute_pmf(interferometer, sample, current_input, mode="fp64", stats: Stats
     """One probability layer of the Clifford & Clifford sampler on the GPU
     (gbperm_compute_pmf): returns (pmf, addends), pmf normalised to sum 1 over
     the m output modes and addends[l] the permanent with one photon removed
-    from input mode l (0 where the input mode is empty).  mode "fast" uses the
-    double-float product."""
+    from input mode l (0 where the input mode is empty).  mode "fx" runs the
+    integer-mantissa product, "fast" the double-float one (FP64 beyond the
+    df.pmf_max_photons rule)."""
     lib = load()
     u = as_matrix(interferometer)
     m = u.shape[0]

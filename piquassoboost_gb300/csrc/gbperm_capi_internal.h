@@ -30,7 +30,7 @@ struct Options {
     // and the accurate product alone is faster than the double-float pass
     // plus its twin.  For the pmf layer the double-float kernel measured no
     // faster than the FP64 one up to 20 photons and escalated from 24 on, so
-    // its rule defaults to 0: the fast mode runs the FP64 layer
+    // its rule defaults to 0: the fast mode runs the integer-mantissa layer
     std::atomic<int64_t> df_max_rows{36};
     std::atomic<int64_t> df_max_photons{24};
     std::atomic<int64_t> df_pmf_max_photons{0};

@@ -33,6 +33,7 @@
 
 #include "gbperm.h"
 #include "gbperm_capi_internal.h"
+#include "gbperm_fx.cuh"
 
 namespace gbperm {
 
@@ -664,6 +665,269 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
     for (int i = threadIdx.x; i < m; i += blockDim.x) pmf[i] = pmf[i] / tot;
 }
 
+// ------------------------------------------ integer-mantissa product
+// The same sweep with every product on 64-bit integer mantissas
+// (gbperm_fx.cuh: 31-bit limbs, twelve mad.wide.s32 and a renormalising
+// shift per complex multiply, 55-57 significant bits, no range limit): per
+// step and lane the powers P_c = x_c^(c_c), the lane's partial product, the
+// other lanes' partials by shuffle (limbs and shift count), a suffix chain,
+// and LO_c = others x prefix_c x suffix_c x x_c^(c_c - 1).  Each LO_c is
+// converted to double with integer instructions and accumulated with the
+// step's weight by one FP64 FMA per component, so the FP64 pipe carries 2
+// instructions per column and step where pmf_kernel needs about 14.  The
+// row tables are interleaved by lane as in pmf_df_kernel.  No twin: the
+// product needs no range check and is at least as accurate as FP64.
+
+struct fxs {  // mantissa limbs and shift count: the value m 2^(-61 - s)
+    fxl m;
+    int s;
+};
+
+__device__ __forceinline__ fxs fxs_one() { return fxs{fxl{1 << 27, 0, 0, 0}, -3}; }  // 2^58 2^-58
+
+__device__ __forceinline__ fxs fxs_mul(const fxs& a, const fxs& b) {
+    long long rr, ri;
+    fx_mul(a.m, b.m, rr, ri);
+    fxs r;
+    r.s = a.s + b.s - 1;
+    r.s += fx_norm(rr, ri, r.m);
+    return r;
+}
+
+// the column factor x = C 2^-62 of an exact column sum, normalised
+__device__ __forceinline__ fxs fxs_col(long long cr, long long ci) {
+    fxs r;
+    r.s = fx_norm_col(cr, ci, r.m);
+    return r;
+}
+
+// z x^e (e >= 1), out of line: only columns of multiplicity > 1 reach it
+__device__ __noinline__ fxs fxs_mul_pow(fxs z, fxs x, int e) {
+    for (int t = 0; t < e; ++t) z = fxs_mul(z, x);
+    return z;
+}
+
+__device__ __forceinline__ fxs shfl_fxs(const fxs& v, int src) {
+    return fxs{fxl{__shfl_sync(0xffffffffu, v.m.rh, src), __shfl_sync(0xffffffffu, v.m.rl, src),
+                   __shfl_sync(0xffffffffu, v.m.ih, src), __shfl_sync(0xffffffffu, v.m.il, src)},
+               __shfl_sync(0xffffffffu, v.s, src)};
+}
+
+template <int CPL, int G>
+__global__ void __launch_bounds__(kThreads) pmf_fx_kernel(RepArgs p, cdd* col_part) {
+    constexpr int NP = CPL * G;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cdd* s_acc = reinterpret_cast<cdd*>(smem_raw);                           // CPL x kThreads
+    longlong2* s_a1 = reinterpret_cast<longlong2*>(s_acc + CPL * kThreads);  // R x NP (interleaved)
+    longlong2* s_a2 = s_a1 + p.R * NP;                                       // nd x NP (interleaved)
+    double* s_w = reinterpret_cast<double*>(s_a2 + p.nd * NP);               // P
+    unsigned char* s_seq = reinterpret_cast<unsigned char*>(s_w + p.P);      // P
+    __shared__ int s_cpow[NP];
+    __shared__ int s_D[kMaxDigits], s_r[kMaxRows];
+    __shared__ long long s_stride[kMaxDigits];
+    const int R = p.R, C = p.C, nd = p.nd, q = p.q;
+    // column g*CPL + c of row r at r*NP + c*G + g: a walk's G lanes read
+    // adjacent words
+    for (int e = threadIdx.x; e < R * NP; e += blockDim.x) {
+        const int r = e / NP, qq = e % NP, j = (qq % G) * CPL + qq / G;
+        s_a1[e] = j < C ? p.a1[r * C + j] : make_longlong2(0, 0);
+    }
+    for (int e = threadIdx.x; e < nd * NP; e += blockDim.x) {
+        const int r = e / NP, qq = e % NP, j = (qq % G) * CPL + qq / G;
+        s_a2[e] = j < C ? p.a2[r * C + j] : make_longlong2(0, 0);
+    }
+    for (long long e = threadIdx.x; e < (long long)p.P; e += blockDim.x) {
+        s_w[e] = p.wlow[e];
+        s_seq[e] = p.seq[e];
+    }
+    for (int e = threadIdx.x; e < NP; e += blockDim.x) s_cpow[e] = e < C ? p.cpow[e] : 0;
+    for (int e = threadIdx.x; e < nd; e += blockDim.x) s_D[e] = p.D[e];
+    for (int e = threadIdx.x; e < R; e += blockDim.x) s_r[e] = p.rcoef[e];
+    for (int e = threadIdx.x; e < CPL * kThreads; e += blockDim.x) s_acc[e] = cdd{{0.0, 0.0}, {0.0, 0.0}};
+    if (threadIdx.x == 0) {
+        long long st = 1;
+        for (int i = 0; i < q; ++i) {
+            s_stride[i] = st;
+            st *= (long long)(p.D[i] + 1);
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int g = lane % G;
+    const int lbase = lane - g;
+    const int j0 = g * CPL;
+    // this lane's real columns (the padding columns of the last lanes come
+    // after them)
+    const int nr = max(0, min(CPL, C - j0));
+    unsigned int extra = 0u;  // bit c: column c has power > 1
+#pragma unroll
+    for (int c = 0; c < CPL; ++c)
+        if (c < nr && s_cpow[j0 + c] > 1) extra |= 1u << c;
+    cdd* my_acc = s_acc + threadIdx.x;  // column c at my_acc[c * kThreads]
+    const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / G;
+    const unsigned long long lane_seg = (unsigned long long)(lane / G);
+    constexpr unsigned long long S = 32 / G;  // segments per warp
+    const unsigned long long full = p.nseg / (2 * S) * (2 * S);
+    long long cre[CPL], cim[CPL];
+
+    for (unsigned long long hw = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / G;
+         hw < p.nseg; hw += T) {
+        const unsigned long long h_raw = parity_slot(hw + lane_seg, S, full);
+        const bool active = h_raw < p.nseg;
+        const unsigned long long h = active ? h_raw : 0ull;
+        int gdig[kMaxDigits];
+        {
+            unsigned long long rem = h;
+            int cnt[kMaxDigits];
+            for (int i = q; i < nd; ++i) {
+                unsigned long long L = (unsigned long long)(s_D[i] + 1);
+                cnt[i] = (int)(rem % L);
+                rem /= L;
+            }
+            int par = 0;
+            for (int i = nd - 1; i >= 0; --i) {
+                int c = i >= q ? cnt[i] : 0;
+                int gg = par ? s_D[i] - c : c;
+                gdig[i] = gg;
+                par ^= gg & 1;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cre[c] = 0;
+            cim[c] = 0;
+        }
+        int gsum = 0;
+        double whigh = 1.0;
+        unsigned long long Gd = 0ull;  // low Gray digits, 4 bits each
+        unsigned int dir = 0u;         // bit i set: low digit i moves up next
+        long long widx = 0;
+        for (int i = 0; i < R; ++i) {
+            int gi = i < nd ? gdig[i] : 0;
+            long long coef = (long long)(s_r[i] - 2 * gi);
+            const longlong2* a = s_a1 + i * NP + g;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                longlong2 v = a[c * G];
+                cre[c] += coef * v.x;
+                cim[c] += coef * v.y;
+            }
+            if (i < nd) {
+                gsum += gi;
+                if (i < q) {
+                    Gd |= (unsigned long long)gi << (4 * i);
+                    if (gi == 0) dir |= 1u << i;
+                    widx += (long long)gi * s_stride[i];
+                } else {
+                    whigh *= p.binom[s_D[i] * kBinomStride + gi];
+                }
+            }
+        }
+        double sgn = (gsum & 1) ? -whigh : whigh;
+        if (!active) sgn = 0.0;
+        cd blk[CPL];
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) blk[c] = cd{0.0, 0.0};
+        for (unsigned long long k = 0; k < p.P; ++k) {
+            if (k != 0) {
+                const int d = s_seq[k];  // warp-uniform
+                const bool up = (dir >> d) & 1u;
+                const int sh = 4 * d;
+                int gv = (int)((Gd >> sh) & 15ull);
+                gv += up ? 1 : -1;
+                Gd = (Gd & ~(15ull << sh)) | ((unsigned long long)gv << sh);
+                if (gv == 0 || gv == s_D[d]) dir ^= 1u << d;
+                widx += up ? s_stride[d] : -s_stride[d];
+                const longlong2* a = s_a2 + d * NP + g;
+                if (up) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c * G];
+                        cre[c] -= v.x;
+                        cim[c] -= v.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        longlong2 v = a[c * G];
+                        cre[c] += v.x;
+                        cim[c] += v.y;
+                    }
+                }
+                sgn = -sgn;
+                if ((k & 255ull) == 0) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        cdd t = my_acc[c * kThreads];
+                        t.re = dd_add_d(t.re, blk[c].re);
+                        t.im = dd_add_d(t.im, blk[c].im);
+                        my_acc[c * kThreads] = t;
+                        blk[c] = cd{0.0, 0.0};
+                    }
+                }
+            }
+            // P_c = x_c^(c_c) of the real columns
+            fxs P[CPL];
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (c < nr) {
+                    P[c] = fxs_col(cre[c], cim[c]);
+                    if ((extra >> c) & 1u) P[c] = fxs_mul_pow(P[c], P[c], s_cpow[j0 + c] - 1);
+                } else {
+                    P[c] = fxs_one();
+                }
+            }
+            // the lane's partial product, then the other lanes' partials
+            fxs part = P[0];
+#pragma unroll
+            for (int c = 1; c < CPL; ++c)
+                if (c < nr) part = fxs_mul(part, P[c]);
+            fxs run = shfl_fxs(part, lbase + ((g + 1) % G));
+#pragma unroll
+            for (int t = 2; t < G; ++t) run = fxs_mul(run, shfl_fxs(part, lbase + ((g + t) % G)));
+            // suffix products: suf[c] = prod_{c < c' < nr} P_c'
+            fxs suf[CPL];
+#pragma unroll
+            for (int c = CPL - 1; c >= 0; --c) {
+                if (c + 1 < CPL && c + 1 < nr) suf[c] = (c + 2 < nr) ? fxs_mul(suf[c + 1], P[c + 1]) : P[c + 1];
+                else suf[c] = fxs_one();
+            }
+            // leave-one-out: others x prefix x suffix x x_c^(c_c - 1), times
+            // the step's signed weight, into the column's running sums
+            const double w = sgn * s_w[widx];
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (c < nr) {
+                    fxs lo = (c + 1 < nr) ? fxs_mul(run, suf[c]) : run;
+                    if ((extra >> c) & 1u)
+                        lo = fxs_mul_pow(lo, fxs_col(cre[c], cim[c]), s_cpow[j0 + c] - 1);
+                    const int ex = -61 - lo.s;
+                    blk[c].re = fma(w, fx_to_double(fx_join(lo.m.rh, lo.m.rl), ex), blk[c].re);
+                    blk[c].im = fma(w, fx_to_double(fx_join(lo.m.ih, lo.m.il), ex), blk[c].im);
+                    if (c + 1 < nr) run = fxs_mul(run, P[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            cdd t = my_acc[c * kThreads];
+            t.re = dd_add_d(t.re, blk[c].re);
+            t.im = dd_add_d(t.im, blk[c].im);
+            my_acc[c * kThreads] = t;
+        }
+    }
+    __syncthreads();
+    // column j = g*CPL + c is held by the threads t with t % G == g: sum them
+    // in a fixed order
+    for (int j = threadIdx.x; j < NP; j += blockDim.x) {
+        const int gj = j / CPL, c = j % CPL;
+        cdd b = s_acc[c * kThreads + gj];
+        for (int t = gj + G; t < kThreads; t += G) b = cdd_add(b, s_acc[c * kThreads + t]);
+        if (j < C) col_part[(size_t)blockIdx.x * C + j] = b;
+    }
+}
+
 template <int CPL, int G>
 size_t pmf_smem(const RepArgs& a) {
     return (size_t)CPL * kThreads * sizeof(cdd) + (size_t)(a.R + a.nd) * CPL * G * sizeof(longlong2) +
@@ -716,6 +980,44 @@ cudaError_t pmf_launch(const RepArgs& a, int cpl, int grp, cdd* col_part, int gr
         case 2: return pmf_launch_t<2, 4>(a, col_part, grid, st);
         case 4: return pmf_launch_t<4, 4>(a, col_part, grid, st);
         default: return pmf_launch_t<8, 4>(a, col_part, grid, st);
+    }
+}
+
+template <int CPL, int G>
+int pmf_fx_bps_t(const RepArgs& a) {
+    int nb = 0;
+    size_t smem = pmf_smem<CPL, G>(a);
+    allow_max_dynamic_smem((const void*)pmf_fx_kernel<CPL, G>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pmf_fx_kernel<CPL, G>, kThreads, smem);
+    return nb > 0 ? nb : 1;
+}
+
+template <int CPL, int G>
+cudaError_t pmf_fx_launch_t(const RepArgs& a, cdd* col_part, int grid, cudaStream_t st) {
+    size_t smem = pmf_smem<CPL, G>(a);
+    cudaError_t e = allow_max_dynamic_smem((const void*)pmf_fx_kernel<CPL, G>);
+    if (e != cudaSuccess) return e;
+    pmf_fx_kernel<CPL, G><<<grid, kThreads, smem, st>>>(a, col_part);
+    return cudaGetLastError();
+}
+
+int pmf_fx_bps(const RepArgs& a, int cpl, int grp) {
+    if (grp == 8) return pmf_fx_bps_t<8, 8>(a);
+    switch (cpl) {
+        case 1: return pmf_fx_bps_t<1, 4>(a);
+        case 2: return pmf_fx_bps_t<2, 4>(a);
+        case 4: return pmf_fx_bps_t<4, 4>(a);
+        default: return pmf_fx_bps_t<8, 4>(a);
+    }
+}
+
+cudaError_t pmf_fx_launch(const RepArgs& a, int cpl, int grp, cdd* col_part, int grid, cudaStream_t st) {
+    if (grp == 8) return pmf_fx_launch_t<8, 8>(a, col_part, grid, st);
+    switch (cpl) {
+        case 1: return pmf_fx_launch_t<1, 4>(a, col_part, grid, st);
+        case 2: return pmf_fx_launch_t<2, 4>(a, col_part, grid, st);
+        case 4: return pmf_fx_launch_t<4, 4>(a, col_part, grid, st);
+        default: return pmf_fx_launch_t<8, 4>(a, col_part, grid, st);
     }
 }
 
@@ -778,8 +1080,9 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
                                   const int64_t* current_input, int arith, double* pmf, double* addends,
                                   gbperm_stats* stats) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
-    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: unknown arithmetic");
+    bool fx = arith == GBPERM_ARITH_FX64;
     if (m <= 0) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: no modes");
     if (!U || !sample || !current_input || !pmf) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: null argument");
     if (ld < m) return fail(GBPERM_ERR_ARG, "gbperm_compute_pmf: ld < m");
@@ -822,11 +1125,14 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
         pmf_shape(C, &cpl, &grp);
         // double-float product for up to 32 columns (4 lanes x 8), up to the
         // df.pmf_max_photons size rule, when the dynamic range allows; the
-        // device check decides between the twins
+        // device check decides between it and its FP64 twin.  Otherwise a
+        // double-float request runs the integer-mantissa layer (faster than
+        // the FP64 one and at least as accurate)
         if (arith == GBPERM_ARITH_DF32 && grp == 4 && ns <= g_opt.df_pmf_max_photons.load()) {
             int boost = 0;
             df = df_boost(h.M.data(), h.R, h.C, h.C, h.rcoef.data(), h.cpow.data(), &boost);
         }
+        if (arith == GBPERM_ARITH_DF32 && !df) fx = true;
     }
     ThreadCtx& cx = thread_ctx();
     int rc = cx.ensure(0);  // device check before any runtime query
@@ -844,15 +1150,15 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
             [&](unsigned long long P) {
                 RepArgs t = a;
                 t.P = P;
-                int b = pmf_bps(t, cpl, grp);
+                int b = fx ? pmf_fx_bps(t, cpl, grp) : pmf_bps(t, cpl, grp);
                 if (df) b = std::min(b, pmf_df_bps(t, cpl));
                 return sms * (unsigned long long)b * (unsigned long long)(kThreads / grp);
             },
-            df ? 20.0 : 2.0);
+            df ? 20.0 : (fx ? 4.0 : 2.0));
         a.q = h.q;
         a.P = h.P;
         a.nseg = h.nseg;
-        int bps = pmf_bps(a, cpl, grp);
+        int bps = fx ? pmf_fx_bps(a, cpl, grp) : pmf_bps(a, cpl, grp);
         if (df) bps = std::min(bps, pmf_df_bps(a, cpl));
         unsigned long long full = (unsigned long long)device_sms(dev) * bps;
         unsigned long long per_block = (unsigned long long)(kThreads / grp);
@@ -960,7 +1266,8 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
             e = cudaGetLastError();
             if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: check launch");
         }
-        e = pmf_launch(a, cpl, grp, d_part, grid, st);
+        // the integer-mantissa layer runs alone (no range check, no twin)
+        e = fx ? pmf_fx_launch(a, cpl, grp, d_part, grid, st) : pmf_launch(a, cpl, grp, d_part, grid, st);
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: launch");
     } else {
         // no sample yet: every permanent is of an empty matrix, i.e. 1
@@ -1003,7 +1310,7 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
             cudaMemcpy(&est, d_exp + 8, sizeof(est), cudaMemcpyDeviceToHost);
         }
         const bool used_df = df && !first_photon && info[1];
-        stats->arith = used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->arith = fx ? GBPERM_ARITH_FX64 : (used_df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
         stats->err_est = (df && !first_photon && est >= 0.0) ? est : 0.0;
     }
     return GBPERM_OK;

@@ -79,7 +79,7 @@ extern "C" {
 int gbperm_sampler_create(const double* U, int64_t m, int64_t ld, uint64_t seed, int arith, gbperm_sampler** out) {
     if (!out) return fail(GBPERM_ERR_ARG, "gbperm_sampler_create: null output");
     *out = nullptr;
-    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_sampler_create: unknown arithmetic");
     gbperm_sampler* s = new gbperm_sampler();
     int rc = copy_matrix(s, U, m, ld);

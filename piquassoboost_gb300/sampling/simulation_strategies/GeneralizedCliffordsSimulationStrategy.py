@@ -16,8 +16,10 @@ Deliberate deviations:
     generator between all strategy objects of the process;
   * ``seed=None`` seeds from the clock, as the reference's constructor does
     before a seed is set;
-  * the keyword-only ``backend`` ("fp64" default, or "fast") selects the
-    arithmetic of the pmf layers.
+  * the keyword-only ``backend`` ("fx" default: the integer-mantissa
+    product, at least as accurate as FP64 and faster on GB300; "fp64"; or
+    "fast") selects the arithmetic of the pmf layers.  Every backend
+    reproduces the reference's seeded samples in the tests.
 """
 from __future__ import annotations
 
@@ -40,9 +42,9 @@ class GeneralizedCliffordsBSimulationStrategy:
     _transmissivity = None
 
     def __init__(self, interferometer_matrix, seed=None, *, backend=None):
-        self._backend = backend or "fp64"
-        if self._backend not in ("fp64", "fast"):
-            raise ValueError(f"unknown backend {backend!r}: expected None, 'fp64' or 'fast'")
+        self._backend = backend or "fx"
+        if self._backend not in ("fp64", "fx", "fast"):
+            raise ValueError(f"unknown backend {backend!r}: expected None, 'fp64', 'fx' or 'fast'")
         self._matrix = np.ascontiguousarray(interferometer_matrix, dtype=np.complex128)
         self._sampler = nat.Sampler(self._matrix, _clock_seed() if seed is None else seed, mode=self._backend,
                                     transmissivity=self._transmissivity)

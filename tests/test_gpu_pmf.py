@@ -21,23 +21,25 @@ with open(os.path.join(HERE, "golden", "reference_calculators.json")) as _f:
 @pytest.fixture(autouse=True)
 def _double_float_layers():
     # the fast mode's pmf rule (df.pmf_max_photons, default 0) sends every
-    # layer to the FP64 kernel; lifted here so that "fast" exercises the
-    # double-float layer and its FP64 twin
+    # layer to the integer-mantissa kernel; lifted here so that "fast"
+    # exercises the double-float layer and its FP64 twin
     nat.require_device()
     nat.set_option("df.pmf_max_photons", 64)
     yield
     nat.set_option("df.pmf_max_photons", 0)
 
 
-def test_pmf_fast_default_rule_runs_fp64():
+def test_pmf_fast_default_rule_runs_fx():
+    # beyond df.pmf_max_photons (default 0: every layer) a double-float
+    # request runs the integer-mantissa layer
     nat.set_option("df.pmf_max_photons", 0)
     U = haar_unitary(12, 3)
     cin = np.array([1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0])
     sample = np.array([0, 2, 0, 1, 0, 0, 0, 1, 0, 0, 1, 0])
     st = nat.Stats()
     a, x = nat.compute_pmf(U, sample, cin, mode="fast", stats=st)
-    assert st.arith == nat.ARITH_FP64
-    b, y = nat.compute_pmf(U, sample, cin, mode="fp64")
+    assert st.arith == nat.ARITH_FX64
+    b, y = nat.compute_pmf(U, sample, cin, mode="fx")
     assert np.array_equal(a, b) and np.array_equal(x, y)
 
 
@@ -173,3 +175,46 @@ def test_pmf_reproducible():
     a, x = nat.compute_pmf(U, sample, cin)
     b, y = nat.compute_pmf(U, sample, cin)
     assert np.array_equal(a, b) and np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_pmf_fx_random_layers(seed):
+    # the integer-mantissa layer against the binary128 oracle, lane shapes
+    # 1, 2, 4 and 8 columns per lane
+    rng = np.random.default_rng(300 + seed)
+    m = int(rng.integers(6, 30))
+    U = haar_unitary(m, 300 + seed)
+    k = int(rng.integers(1, min(m, 24)))
+    cin = np.zeros(m, dtype=np.int64)
+    cin[rng.choice(m, k + 1, replace=False)] = 1
+    sample = rng.multinomial(k, np.ones(m) / m).astype(np.int64)
+    st = nat.Stats()
+    _check(U, sample, cin, "fx")
+    nat.compute_pmf(U, sample, cin, mode="fx", stats=st)
+    assert st.arith == nat.ARITH_FX64
+
+
+def test_pmf_fx_repeated_input_and_wide():
+    # input multiplicities above 1 (column powers) and more than 32 occupied
+    # input modes (8 lanes x 8 columns)
+    U = haar_unitary(7, 5)
+    _check(U, np.array([0, 2, 0, 2, 0, 1, 0]), np.array([3, 0, 2, 0, 1, 0, 0]), "fx")
+    m = 40
+    U = haar_unitary(m, 41)
+    cin = np.ones(m, dtype=np.int64)
+    cin[34:] = 0
+    rng = np.random.default_rng(41)
+    sample = rng.multinomial(33, np.ones(m) / m).astype(np.int64)
+    a, x = nat.compute_pmf(U, sample, cin, mode="fx")
+    b, y = nat.compute_pmf(U, sample, cin, mode="fp64")
+    assert np.allclose(a, b, rtol=1e-10, atol=1e-13)
+    assert np.max(np.abs(x - y)) <= 1e-10 * np.max(np.abs(y))
+
+
+def test_pmf_fx_matches_fp64_at_size():
+    # a 40-mode / 20-photon layer: integer-mantissa against the FP64 kernel
+    U, sample, cin = _layer(21, 40, 20)
+    a, x = nat.compute_pmf(U, sample, cin, mode="fx")
+    b, y = nat.compute_pmf(U, sample, cin, mode="fp64")
+    assert np.allclose(a, b, rtol=1e-10, atol=1e-13)
+    assert np.max(np.abs(x - y)) <= 1e-10 * np.max(np.abs(y))

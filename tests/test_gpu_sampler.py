@@ -49,11 +49,12 @@ def test_reproduces_reference_sequences(case):
     assert [s.tolist() for s in samples] == case["samples"]
 
 
-def test_fast_backend_gives_the_same_draws():
+@pytest.mark.parametrize("backend", ["fast", "fx"])
+def test_other_backends_give_the_same_draws(backend):
     nat.require_device()
-    case = FIX["sequences"][0]
-    samples = _strategy(case, backend="fast").simulate(case["input_state"], len(case["samples"]))
-    assert [s.tolist() for s in samples] == case["samples"]
+    for case in FIX["sequences"]:
+        samples = _strategy(case, backend=backend).simulate(case["input_state"], len(case["samples"]))
+        assert [s.tolist() for s in samples] == case["samples"], case["name"]
 
 
 def test_reseed_and_stream_continuation():
