@@ -214,7 +214,10 @@ void gbperm_rep_batch_destroy(gbperm_rep_batch* plan);
  * 109-296).  Instance i is a rows[i] x cols[i] complex128 matrix, dense
  * (ld = cols[i]); the instances are packed back to back in index order.
  * A plan holds the instance sizes, the work list and the device buffers; it
- * belongs to the device current at creation.  out: 2 * count doubles. */
+ * belongs to the device current at creation.  arith: FP64, DF32 (with the
+ * per-instance FP64 redo pass) or FX64 (integer-mantissa worker, lane
+ * groups with each instance's columns split evenly).  out: 2 * count
+ * doubles. */
 typedef struct gbperm_batch_plan gbperm_batch_plan;
 int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t count, int arith,
                              gbperm_batch_plan** out_plan);

@@ -16,9 +16,10 @@
 // fixed order (bitwise-reproducible results) and applies the scale.
 //
 // Arithmetic per instance as in the single-permanent kernels: exact int64
-// column sums; FP64 product (GROUP = 1) or the double-float product with
-// lane groups (GROUP = 2/4), with the FP64 product as the per-instance
-// fallback when the range check fails.
+// column sums; FP64 product (GROUP = 1), the double-float product with lane
+// groups (GROUP = 2/4) with the FP64 product as the per-instance fallback
+// when the range check fails or the error estimate is above the bar, or the
+// integer-mantissa product with lane groups (batched_fx_kernel).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -29,6 +30,7 @@
 
 #include "gbperm.h"
 #include "gbperm_capi_internal.h"
+#include "gbperm_fx.cuh"
 
 namespace gbperm {
 
@@ -363,6 +365,136 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
     }
 }
 
+// Integer-mantissa worker (GBPERM_ARITH_FX64): the items of the FP64 /
+// double-float worker with the product of perm_plain_fx.cu -- each
+// instance's columns split evenly over the GROUP lanes of a walk (a lane
+// holds ceil(cols / GROUP) of them), two product chains per lane on 31-bit
+// limbs, a shuffle butterfly over the group, and the term converted to
+// double with integer instructions.  No range check and no redo pass.
+template <int CPL, int GROUP>
+__global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
+    const int lane = threadIdx.x & 31;
+    const int g = lane % GROUP;
+    const int grp = lane / GROUP;
+    long long cre[CPL], cim[CPL];
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = (int)atomicAdd(p.counter, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= p.nitems) break;
+        const BItem item = p.items[it];
+        const BInstOut io = p.iout[item.inst];
+        const BInst in = p.inst[item.inst];
+        const int rows = in.rows, cols = in.cols;
+        const int cpl_i = (cols + GROUP - 1) / GROUP;
+        const int j0 = g * cpl_i;
+        const int nr = max(0, min(cpl_i, cols - j0));  // 0 for a lane past the columns
+        const unsigned long long s = item.seg0 + (unsigned long long)grp;
+        const bool active = s < in.nseg && io.finite;
+        const unsigned long long i0 = (active ? s : 0ull) << in.seg_log2;
+        const unsigned long long L = 1ull << in.seg_log2;
+        const longlong2* __restrict__ a1 = p.a1 + in.a_off;
+        const longlong2* __restrict__ a2 = p.a2 + in.a_off;
+        const unsigned long long g0 = i0 ^ (i0 >> 1);
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            longlong2 v = c < nr ? __ldg(&a1[j0 + c]) : make_longlong2(0, 0);
+            cre[c] = v.x;
+            cim[c] = v.y;
+        }
+        for (int r = 1; r < rows; ++r) {
+            const long long m = -(long long)((g0 >> (rows - 1 - r)) & 1ull);
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (c < nr) {
+                    longlong2 v = __ldg(&a1[r * cols + j0 + c]);
+                    cre[c] += (v.x ^ m) - m;
+                    cim[c] += (v.y ^ m) - m;
+                }
+            }
+        }
+        cdd acc{{0.0, 0.0}, {0.0, 0.0}};
+        unsigned long long sbit = (unsigned long long)(__popcll(g0) & 1) << 63;
+        double bre = 0.0, bim = 0.0;
+        for (unsigned long long k = 0; k < L; ++k) {
+            if (k != 0) {
+                const int b = __ffsll((long long)k) - 1;
+                const unsigned long long idx = i0 + k;
+                const bool sub = ((idx >> b) ^ (idx >> (b + 1))) & 1ull;
+                const longlong2* a = a2 + (rows - 1 - b) * cols + j0;
+                if (sub) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c)
+                        if (c < nr) {
+                            longlong2 v = __ldg(&a[c]);
+                            cre[c] -= v.x;
+                            cim[c] -= v.y;
+                        }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c)
+                        if (c < nr) {
+                            longlong2 v = __ldg(&a[c]);
+                            cre[c] += v.x;
+                            cim[c] += v.y;
+                        }
+                }
+                sbit ^= 0x8000000000000000ull;
+                if ((k & 255ull) == 0) {
+                    acc.re = dd_add_d(acc.re, bre);
+                    acc.im = dd_add_d(acc.im, bim);
+                    bre = 0.0;
+                    bim = 0.0;
+                }
+            }
+            // the lane's partial product in two chains (sig: shift count)
+            fxl ch[2];
+            int sig = 0;
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                if (c < nr) {
+                    if (c < 2) {
+                        sig += fx_norm_col(cre[c], cim[c], ch[c]);
+                    } else {
+                        long long rr, ri;
+                        fx_mul(ch[c & 1], fx_col(cre[c], cim[c]), rr, ri);
+                        sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                    }
+                }
+            }
+            long long pr = 0, pi = 0;
+            if (nr >= 2) {
+                fx_mul(ch[0], ch[1], pr, pi);
+                sig -= 1;
+            } else if (nr == 1) {
+                pr = fx_join(ch[0].rh, ch[0].rl);
+                pi = fx_join(ch[0].ih, ch[0].il);
+            }
+#pragma unroll
+            for (int m = 1; m < GROUP; m <<= 1) {
+                fxl x;
+                if (nr > 0) sig += fx_norm(pr, pi, x);
+                else x = fxl{1 << 30, 0, 0, 0};  // the column value 1 (2^61, shift count 0)
+                const fxl y = shfl_xor_fxl(x, m);
+                sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
+                fx_mul(x, y, pr, pi);
+            }
+            if (g == 0 && active) {
+                const int e = -61 - sig;
+                bre += __longlong_as_double(__double_as_longlong(fx_to_double(pr, e)) ^ (long long)sbit);
+                bim += __longlong_as_double(__double_as_longlong(fx_to_double(pi, e)) ^ (long long)sbit);
+            }
+        }
+        acc.re = dd_add_d(acc.re, bre);
+        acc.im = dd_add_d(acc.im, bim);
+        acc = warp_sum_cdd(acc);
+        if (lane == 0) {
+            p.item_part[it] = acc;
+            p.item_s2[it] = 0.0;
+        }
+    }
+}
+
 // warp per instance: lane l sums items l, l + 32, ... in order, then a fixed
 // butterfly (deterministic; a large instance has thousands of items)
 __global__ void batched_finalize_kernel(BArgs p) {
@@ -460,6 +592,48 @@ cudaError_t batch_launch(const BArgs& a, int cpl, int grp, bool df, int grid, cu
     return cudaErrorInvalidValue;
 }
 
+// integer-mantissa shapes (CPL, GROUP): an instance's columns are split
+// evenly, so CPL only bounds ceil(cols / GROUP)
+#define GBPERM_BATCH_FX_SHAPES(X) X(4, 2) X(8, 2) X(12, 2) X(16, 2) X(20, 2) X(16, 4)
+
+int batch_fx_bps(int cpl, int grp) {
+#define X(C, G)                                                                                          \
+    if (cpl == C && grp == G) {                                                                          \
+        int nb = 0;                                                                                      \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batched_fx_kernel<C, G>, kThreads, 0);        \
+        return nb > 0 ? nb : 1;                                                                          \
+    }
+    GBPERM_BATCH_FX_SHAPES(X)
+#undef X
+    return 0;
+}
+
+cudaError_t batch_fx_launch(const BArgs& a, int cpl, int grp, int grid, cudaStream_t st) {
+#define X(C, G)                                                 \
+    if (cpl == C && grp == G) {                                 \
+        batched_fx_kernel<C, G><<<grid, kThreads, 0, st>>>(a);  \
+        return cudaGetLastError();                              \
+    }
+    GBPERM_BATCH_FX_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+// lane pairs up to 40 columns (quads on request or above), the smallest CPL
+// with CPL * GROUP >= cols
+void batch_fx_shape(int cols, int group, int* cpl, int* grp) {
+    static const int sfx[][2] = {{4, 2}, {8, 2}, {12, 2}, {16, 2}, {20, 2}, {16, 4}};
+    const int want = (group == 4 || cols > 40) ? 4 : 2;
+    for (auto& s : sfx)
+        if (s[1] == want && s[0] * s[1] >= cols) {
+            *cpl = s[0];
+            *grp = s[1];
+            return;
+        }
+    *cpl = 16;
+    *grp = 4;
+}
+
 // smallest compiled shape covering `cols` columns for the arithmetic
 void batch_shape(int cols, bool df, int group, int* cpl, int* grp) {
     static const int s64[][2] = {{16, 1}, {32, 1}, {48, 1}, {64, 1}};
@@ -501,6 +675,7 @@ struct BatchPlan {
     int64_t count = 0;
     int arith = GBPERM_ARITH_FP64;
     bool df = false;
+    bool fx = false;                 // integer-mantissa worker (batched_fx_kernel)
     bool escalate = true;            // double-float instances above the error bar redone in FP64
     int cpl = 16, grp = 1;
     int grid = 1;
@@ -585,7 +760,8 @@ static cudaError_t plan_enqueue(BatchPlan* p) {
     batched_prepare_kernel<<<pg, 64, 0, p->stream>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    e = batch_launch(a, p->cpl, p->grp, p->df, p->grid, p->stream);
+    e = p->fx ? batch_fx_launch(a, p->cpl, p->grp, p->grid, p->stream)
+              : batch_launch(a, p->cpl, p->grp, p->df, p->grid, p->stream);
     if (e != cudaSuccess) return e;
     batched_finalize_kernel<<<(p->ninst + 3) / 4, 128, 0, p->stream>>>(a);
     e = cudaGetLastError();
@@ -708,7 +884,7 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
     *out_plan = nullptr;
     if (count < 0 || (count > 0 && (!rows || !cols))) return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_create: bad sizes");
     if (count > (int64_t)1 << 28) return fail(GBPERM_ERR_TOO_LARGE, "gbperm_batch_plan_create: too many instances");
-    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32)
+    if (arith != GBPERM_ARITH_FP64 && arith != GBPERM_ARITH_DF32 && arith != GBPERM_ARITH_FX64)
         return fail(GBPERM_ERR_ARG, "gbperm_batch_plan_create: unknown arithmetic");
     BatchPlan* p = new BatchPlan();
     p->count = count;
@@ -754,11 +930,13 @@ int gbperm_batch_plan_create(const int64_t* rows, const int64_t* cols, int64_t c
         plan_free(p);
         return cuda_fail(e, "gbperm_batch_plan_create");
     }
+    p->fx = arith == GBPERM_ARITH_FX64;
     p->df = arith == GBPERM_ARITH_DF32 && maxc <= kDfMaxCols;
     p->escalate = g_opt.df_escalate.load() != 0;
     p->maxc = maxc;
-    batch_shape(maxc, p->df, (int)g_opt.batched_threads.load(), &p->cpl, &p->grp);
-    int bps = batch_bps(p->cpl, p->grp, p->df);
+    if (p->fx) batch_fx_shape(maxc, (int)g_opt.batched_threads.load(), &p->cpl, &p->grp);
+    else batch_shape(maxc, p->df, (int)g_opt.batched_threads.load(), &p->cpl, &p->grp);
+    int bps = p->fx ? batch_fx_bps(p->cpl, p->grp) : batch_bps(p->cpl, p->grp, p->df);
     p->grid = device_sms(p->device) * bps;
     // item target: ~16 items per resident warp over the whole batch
     double warps = (double)p->grid * (kThreads / 32);
@@ -881,7 +1059,7 @@ int gbperm_batch_plan_run(gbperm_batch_plan* plan, const double* packed, double*
         stats->err_est = worst;
         stats->grid = p->grid;
         stats->seg_log2 = (int)p->item_target_log2;
-        stats->arith = p->df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64;
+        stats->arith = p->fx ? GBPERM_ARITH_FX64 : (p->df ? GBPERM_ARITH_DF32 : GBPERM_ARITH_FP64);
     }
     return GBPERM_OK;
 }
@@ -945,7 +1123,7 @@ int gbperm_batch_plan_autotune(gbperm_batch_plan* plan, const double* packed, in
     // item sizes around the size-based default; each is planned, captured and
     // timed on the real batch, the fastest is kept
     const int64_t base = p->item_target_log2;
-    std::vector<int> groups = p->df ? std::vector<int>{2, 4} : std::vector<int>{1};
+    std::vector<int> groups = (p->df || p->fx) ? std::vector<int>{2, 4} : std::vector<int>{1};
     double best = 1e300;
     int best_grp = p->grp;
     int64_t best_log2 = base;
@@ -953,10 +1131,11 @@ int gbperm_batch_plan_autotune(gbperm_batch_plan* plan, const double* packed, in
         for (int64_t dl = -2; dl <= 2; dl += 2) {
             const int64_t l2 = std::min<int64_t>(40, std::max<int64_t>(8, base + dl));
             int cpl = 0, gg = 0;
-            batch_shape(p->maxc, p->df, grp, &cpl, &gg);
+            if (p->fx) batch_fx_shape(p->maxc, grp, &cpl, &gg);
+            else batch_shape(p->maxc, p->df, grp, &cpl, &gg);
             p->cpl = cpl;
             p->grp = gg;
-            p->grid = device_sms(p->device) * batch_bps(cpl, gg, p->df);
+            p->grid = device_sms(p->device) * (p->fx ? batch_fx_bps(cpl, gg) : batch_bps(cpl, gg, p->df));
             p->item_target_log2 = l2;
             int rc = plan_build_items(p);
             if (rc == GBPERM_OK) rc = plan_capture(p);
@@ -978,10 +1157,11 @@ int gbperm_batch_plan_autotune(gbperm_batch_plan* plan, const double* packed, in
         }
     }
     int cpl = 0, gg = 0;
-    batch_shape(p->maxc, p->df, best_grp, &cpl, &gg);
+    if (p->fx) batch_fx_shape(p->maxc, best_grp, &cpl, &gg);
+    else batch_shape(p->maxc, p->df, best_grp, &cpl, &gg);
     p->cpl = cpl;
     p->grp = gg;
-    p->grid = device_sms(p->device) * batch_bps(cpl, gg, p->df);
+    p->grid = device_sms(p->device) * (p->fx ? batch_fx_bps(cpl, gg) : batch_bps(cpl, gg, p->df));
     p->item_target_log2 = best_log2;
     int rc = plan_build_items(p);
     if (rc == GBPERM_OK) rc = plan_capture(p);

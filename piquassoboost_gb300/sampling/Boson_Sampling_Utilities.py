@@ -21,13 +21,13 @@ run the integer-mantissa product: 55-57 significant bits per complex
 multiply, more than the FP64 product's 53 (it does not reach the x87
 extended type's 64).  Lists of states run through one persistent
 multiplicity launch with that product; lists of matrices run through the
-plain batched launch, which has no integer-mantissa product: there "fx" uses
-FP64.
+plain batched launch in the same product.
 
 Every class also takes a keyword-only ``backend``: None (default) keeps the
 arithmetic of its library id, "fp64" selects the FP64 product, "fx" the
 integer-mantissa product and "fast" the double-float product (whose results
-above a 1e-10 error estimate are recomputed in FP64 on the device).  The
+above a 1e-10 error estimate are recomputed on the device: single
+permanents by the integer-mantissa product, plain batches in FP64).  The
 reference has no such argument; an unknown value raises ValueError.
 
 Deliberate deviations: arrays are converted to complex128 / int64 (the
@@ -51,10 +51,6 @@ REPEATED_LIBS = {0: "fp64", 1: "fx", 6: "fp64", 7: "fp64", 8: "fx", 20: "fp64", 
 REPEATED_CONSTRUCT_ONLY = {9}
 BACKENDS = ("fp64", "fast", "fx")
 
-
-def _batched_mode(mode):
-    # the batched launches have no integer-mantissa product
-    return "fp64" if mode == "fx" else mode
 
 # lib 0 (ChinHuhPermanentCalculator) evaluates the Chin-Huh form of the sum
 # (CChinHuhPermanentCalculator.cpp:48-201) on the same kernels
@@ -97,7 +93,7 @@ class GlynnPermanentCalculator_wrapper:
     def calculate(self):
         mode = self.backend or PLAIN_LIBS[self.lib]
         if isinstance(self._matrix, list):
-            return nat.perm_batched([nat.as_matrix(m) for m in self._matrix], mode=_batched_mode(mode))
+            return nat.perm_batched([nat.as_matrix(m) for m in self._matrix], mode=mode)
         if self.lib in (10, 11):
             a = nat.as_matrix(self._matrix)
             if a.shape[0] != a.shape[1] and a.size > 0:

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-10
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fast"])
+@pytest.mark.parametrize("mode", ["fp64", "fast", "fx"])
 def test_batched_uneven_vs_oracle(mode):
     mats = batched_instances(96, seed=5, modes=40, kmin=1, kmax=16)
     vals = nat.perm_batched(mats, mode=mode)
@@ -19,7 +19,7 @@ def test_batched_uneven_vs_oracle(mode):
         assert orc.rel_err(v, q) <= TOL
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fast"])
+@pytest.mark.parametrize("mode", ["fp64", "fast", "fx"])
 def test_batched_matches_single_kernel(mode):
     mats = batched_instances(24, seed=9, modes=60, kmin=16, kmax=22)
     vals = nat.perm_batched(mats, mode=mode)
@@ -28,20 +28,22 @@ def test_batched_matches_single_kernel(mode):
         assert abs(v - ref) <= TOL * abs(ref)
 
 
-def test_batched_trivial_and_rectangular():
+@pytest.mark.parametrize("mode", ["fp64", "fx"])
+def test_batched_trivial_and_rectangular(mode):
     rng = np.random.default_rng(2)
     mats = [np.zeros((0, 0)), np.ones((5, 2)), rng.standard_normal((3, 5)) + 1j, rng.standard_normal((4, 3)),
-            rng.standard_normal((1, 1))]
-    vals = nat.perm_batched(mats, mode="fp64")
+            rng.standard_normal((1, 1)), rng.standard_normal((2, 9)) + 1j, rng.standard_normal((7, 48)) + 0.5j]
+    vals = nat.perm_batched(mats, mode=mode)
     assert vals[0] == 1 and vals[1] == 0
     for m, v in zip(mats[2:], vals[2:]):
         ref, q = orc.bbfg(m, prec=1)
         assert orc.rel_err(v, q) <= TOL
 
 
-def test_batched_nan_instance_isolated():
+@pytest.mark.parametrize("mode", ["fast", "fx"])
+def test_batched_nan_instance_isolated(mode):
     a = np.ones((4, 4)); b = np.ones((4, 4)); b[1, 2] = np.nan
-    vals = nat.perm_batched([a, b, a], mode="fast")
+    vals = nat.perm_batched([a, b, a], mode=mode)
     assert abs(vals[0] - 24) < 1e-9 and abs(vals[2] - 24) < 1e-9
     assert np.isnan(vals[1].real)
 
@@ -75,10 +77,11 @@ def test_dropin_list_branch_uses_batched():
         assert orc.rel_err(v, q) <= TOL
 
 
-def test_batched_autotune_keeps_results():
+@pytest.mark.parametrize("mode", ["fast", "fx"])
+def test_batched_autotune_keeps_results(mode):
     from piquassoboost_gb300.workloads import batched_instances
     mats = batched_instances(96, seed=12, modes=40, kmin=4, kmax=16)
-    plan = nat.BatchPlan([m.shape for m in mats], mode="fast")
+    plan = nat.BatchPlan([m.shape for m in mats], mode=mode)
     before = plan.run(mats)
     ms = plan.autotune(mats)
     assert ms > 0.0
@@ -123,6 +126,9 @@ def test_batched_fast_within_bar_of_fp64():
     d = np.array(nat.perm_batched(mats, mode="fp64"))
     assert np.max(np.abs(f - d) / np.abs(d)) <= 1e-10
     assert 0.0 < st.err_est <= 1e-10
+    x = np.array(nat.perm_batched(mats, mode="fx", stats=st))
+    assert st.arith == nat.ARITH_FX64
+    assert np.max(np.abs(x - d) / np.abs(d)) <= 1e-10
 
 
 # ------------------------------------------------ multiplicity batch plan

@@ -129,8 +129,8 @@ def test_fx_at_least_as_accurate_as_fp64():
 
 def test_dropin_ids_route_to_fx():
     # id 22 and the reference's long-double ids (plain 0, 8, 11; repeated
-    # 1, 8) run the integer-mantissa product; lists under "fx" run the
-    # batched launches in FP64
+    # 1, 8) run the integer-mantissa product, lists of matrices too (one
+    # integer-mantissa batched launch)
     from piquassoboost_gb300.sampling import Boson_Sampling_Utilities as bsu
     from piquassoboost_gb300.workloads import haar_unitary, repeated_instance
 
@@ -146,7 +146,10 @@ def test_dropin_ids_route_to_fx():
                 bsu.BBFGRepeatedPermanentCalculatorLongDouble):
         assert cls(U, cin, rout).calculate() == r, cls.__name__
     mats = [haar_block(k, seed=k) for k in (6, 9, 12)]
+    st = nat.Stats()
     got = bsu.GB300FxPermanent(mats).calculate()
+    nat.perm_batched(mats, mode="fx", stats=st)
+    assert st.arith == nat.ARITH_FX64
     for m, g in zip(mats, got):
         ref = nat.perm(m, mode="fp64")
         assert abs(g - ref) <= TOL * abs(ref)
