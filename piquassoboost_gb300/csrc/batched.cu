@@ -470,15 +470,20 @@ __global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
                 pr = fx_join(ch[0].rh, ch[0].rl);
                 pi = fx_join(ch[0].ih, ch[0].il);
             }
-            // a lane without columns enters the first stage with the value 1
-            // (2^61 in column-factor form, shift count 0); from the second
-            // stage on it holds a product like every other lane
+            // a lane without columns enters the first stage with the value 1,
+            // normalised (2^58 with shift count -3, so that two such lanes'
+            // product stays within fx_norm's range); from the second stage on
+            // it holds a product like every other lane
             bool have = nr > 0;
 #pragma unroll
             for (int m = 1; m < GROUP; m <<= 1) {
                 fxl x;
-                if (have) sig += fx_norm(pr, pi, x);
-                else x = fxl{1 << 30, 0, 0, 0};
+                if (have) {
+                    sig += fx_norm(pr, pi, x);
+                } else {
+                    x = fxl{1 << 27, 0, 0, 0};
+                    sig = -3;
+                }
                 have = true;
                 const fxl y = shfl_xor_fxl(x, m);
                 sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
