@@ -669,9 +669,12 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
 // The same sweep with every product on 64-bit integer mantissas
 // (gbperm_fx.cuh: 31-bit limbs, twelve mad.wide.s32 and a renormalising
 // shift per complex multiply, 55-57 significant bits, no range limit): per
-// step and lane the powers P_c = x_c^(c_c), the lane's partial product, the
-// other lanes' partials by shuffle (limbs and shift count), a suffix chain,
-// and LO_c = others x prefix_c x suffix_c x x_c^(c_c - 1).  Each LO_c is
+// step and lane the prefix products of the powers P_c = x_c^(c_c) (which
+// end in the lane's partial product), the other lanes' partials by shuffle
+// (limbs and shift count), then backwards LO_c = prefix_c x (others x
+// suffix_c) x x_c^(c_c - 1) with P_c recomputed from the column sums: three
+// multiplies per column and step, and no array of powers or suffixes kept
+// in registers (the kernel fits 3 blocks per SM).  Each LO_c is
 // converted to double with integer instructions and accumulated with the
 // step's weight by one FP64 FMA per component, so the FP64 pipe carries 2
 // instructions per column and step where pmf_kernel needs about 14.  The
@@ -714,9 +717,8 @@ __device__ __forceinline__ fxs shfl_fxs(const fxs& v, int src) {
 }
 
 template <int CPL, int G>
-// 3 blocks per SM: a few registers spill, and the extra warps cover the
-// dependent integer chains (11% faster than 2 blocks at 196 registers on the
-// 60-mode / 30-photon layers)
+// 3 blocks per SM (168 registers, no spills): the extra warps cover the
+// dependent integer chains
 __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col_part) {
     constexpr int NP = CPL * G;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -870,45 +872,40 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
                     }
                 }
             }
-            // P_c = x_c^(c_c) of the real columns
-            fxs P[CPL];
+            // prefix products pre[c] = prod_{c' < c} P_c' and the lane's
+            // partial product; P_c = x_c^(c_c) is recomputed from the column
+            // sums in the backward pass instead of being kept
+            fxs pre[CPL];
+            fxs part = fxs_one();
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
                 if (c < nr) {
-                    P[c] = fxs_col(cre[c], cim[c]);
-                    if ((extra >> c) & 1u) P[c] = fxs_mul_pow(P[c], P[c], s_cpow[j0 + c] - 1);
-                } else {
-                    P[c] = fxs_one();
+                    fxs pc = fxs_col(cre[c], cim[c]);
+                    if ((extra >> c) & 1u) pc = fxs_mul_pow(pc, pc, s_cpow[j0 + c] - 1);
+                    pre[c] = part;
+                    part = (c == 0) ? pc : fxs_mul(part, pc);
                 }
             }
-            // the lane's partial product, then the other lanes' partials
-            fxs part = P[0];
-#pragma unroll
-            for (int c = 1; c < CPL; ++c)
-                if (c < nr) part = fxs_mul(part, P[c]);
+            // the other lanes' partials, then backwards:
+            // LO_c = prefix_c x (others x suffix_c) x x_c^(c_c - 1)
             fxs run = shfl_fxs(part, lbase + ((g + 1) % G));
 #pragma unroll
             for (int t = 2; t < G; ++t) run = fxs_mul(run, shfl_fxs(part, lbase + ((g + t) % G)));
-            // suffix products: suf[c] = prod_{c < c' < nr} P_c'
-            fxs suf[CPL];
-#pragma unroll
-            for (int c = CPL - 1; c >= 0; --c) {
-                if (c + 1 < CPL && c + 1 < nr) suf[c] = (c + 2 < nr) ? fxs_mul(suf[c + 1], P[c + 1]) : P[c + 1];
-                else suf[c] = fxs_one();
-            }
-            // leave-one-out: others x prefix x suffix x x_c^(c_c - 1), times
-            // the step's signed weight, into the column's running sums
             const double w = sgn * s_w[widx];
 #pragma unroll
-            for (int c = 0; c < CPL; ++c) {
+            for (int c = CPL - 1; c >= 0; --c) {
                 if (c < nr) {
-                    fxs lo = (c + 1 < nr) ? fxs_mul(run, suf[c]) : run;
+                    fxs lo = (c == 0) ? run : fxs_mul(pre[c], run);
                     if ((extra >> c) & 1u)
                         lo = fxs_mul_pow(lo, fxs_col(cre[c], cim[c]), s_cpow[j0 + c] - 1);
                     const int ex = -61 - lo.s;
                     blk[c].re = fma(w, fx_to_double(fx_join(lo.m.rh, lo.m.rl), ex), blk[c].re);
                     blk[c].im = fma(w, fx_to_double(fx_join(lo.m.ih, lo.m.il), ex), blk[c].im);
-                    if (c + 1 < nr) run = fxs_mul(run, P[c]);
+                    if (c > 0) {
+                        fxs pc = fxs_col(cre[c], cim[c]);
+                        if ((extra >> c) & 1u) pc = fxs_mul_pow(pc, pc, s_cpow[j0 + c] - 1);
+                        run = fxs_mul(run, pc);
+                    }
                 }
             }
         }
