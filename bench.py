@@ -409,13 +409,16 @@ def run_ours(args, rank, world, local):
             continue
         st = nat.Stats()
         ms, vals, esc, ests = [], [], 0, []
+        # the fast mode's size rule (df.max_rows) sends larger square
+        # matrices straight to the integer-mantissa product
+        by_rule = mode == "fast" and n > nat.get_option("df.max_rows")
         for i in idx:
             v = nat.perm(mats[i], mode=mode, stats=st)
             ms.append(st.kernel_ms)
             vals.append(v)
             if mode == "fast":
                 ests.append(st.err_est)
-                esc += int(st.arith != nat.ARITH_DF32)
+                esc += int(not by_rule and st.arith != nat.ARITH_DF32)
         if mode == "fp64":
             ref64 = dict(zip(idx, vals))
             if args.mode == "fp64":
@@ -429,6 +432,10 @@ def run_ours(args, rank, world, local):
                       "frac_of_fp64_peak": d["fp64_equivalent_tflops"] / peaks["fp64"]})
         elif mode == "fx":
             d.update({"dtype": "int64 mantissas (>= f64 accuracy)", "kernel": "plain_fx_kernel"})
+        elif by_rule:
+            d.update({"dtype": "int64 mantissas", "kernel": "plain_fx_kernel",
+                      "note": f"n > df.max_rows ({nat.get_option('df.max_rows')}): the fast mode runs the "
+                              "integer-mantissa product alone"})
         else:
             d.update({"dtype": "f32 pairs (double-float product)", "kernel": "plain_df_kernel",
                       "escalated_steps": esc, "err_est": ests,
