@@ -292,8 +292,12 @@ int rep_fx_bps_t(const RepArgs& a) {
 
 // one lane up to 8 columns; lane pairs with an even column count per lane up
 // to 40; lane quads up to 64.  Every lane keeps at least one real column.
-#define GBPERM_REP_FX_SHAPES(X) \
-    X(8, 1) X(6, 2) X(8, 2) X(10, 2) X(12, 2) X(14, 2) X(16, 2) X(18, 2) X(20, 2) X(12, 4) X(16, 4)
+// lane pairs with CPL = ceil(C / 2) exactly (the unrolled column loop runs
+// CPL slots whatever a lane's share, so a rounded-up CPL costs a slot per
+// step), quads above 40 columns
+#define GBPERM_REP_FX_SHAPES(X)                                                                        \
+    X(8, 1) X(5, 2) X(6, 2) X(7, 2) X(8, 2) X(9, 2) X(10, 2) X(11, 2) X(12, 2) X(13, 2) X(14, 2) X(15, 2) \
+    X(16, 2) X(17, 2) X(18, 2) X(19, 2) X(20, 2) X(12, 4) X(16, 4)
 
 }  // namespace
 
@@ -305,8 +309,7 @@ void repeated_fx_shape(int cols, int* cpl, int* grp) {
     }
     if (cols <= 40) {
         *grp = 2;
-        const int half = (cols + 1) / 2;
-        *cpl = half < 6 ? 6 : (half + 1) / 2 * 2;
+        *cpl = (cols + 1) / 2;  // 5..20
         return;
     }
     *grp = 4;
