@@ -619,36 +619,52 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
                                                                    const int* df_info, const int* col_mode,
                                                                    const double* cin_w,
                                                                    const double2* U, long long ldu, int m,
-                                                                   double* pmf, double2* addends) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    double2* s_perm = reinterpret_cast<double2*>(smem_raw);  // C
+                                                                   double* pmf, double2* addends,
+                                                                   double2* perm_out, unsigned int* done) {
+    // one block per column: the double-double adds run on the FP64 pipe,
+    // which retires under two FMA per clock per SM on GB300, so C blocks on
+    // C SMs instead of one block for all columns (thread t takes blocks t,
+    // t + blockDim, ... in order, then a fixed butterfly and warp order:
+    // deterministic)
+    __shared__ cdd s_warp[kFinThreads / 32];
+    __shared__ bool s_last;
     __shared__ double s_tot;
-    // column j: a warp sums the block partials (lane l takes blocks l, l + 32,
-    // ... in order, then a fixed butterfly: deterministic)
-    const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    for (int j = threadIdx.x >> 5; j < C; j += nwarps) {
-        cdd tot{{0.0, 0.0}, {0.0, 0.0}};
-        for (int b = lane; b < nblocks; b += 32) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
-        tot = warp_sum_cdd(tot);
-        if (lane == 0) {
-            double o[2];
-            // the double-float partials carry the range boost; the FP64
-            // twin's (it ran when the range check or the error estimate sent
-            // the layer to it) do not
-            const bool dfok = df_info && df_info[1];
-            const int ex = dfok ? *exp_in - (col_e[j] - df_info[0]) : *exp_fp64 - col_e[j];
-            write_result(tot, ex, o, nullptr);
-            s_perm[j] = make_double2(o[0], o[1]);
-        }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int j = blockIdx.x;
+    cdd tot{{0.0, 0.0}, {0.0, 0.0}};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
+    tot = warp_sum_cdd(tot);
+    if (lane == 0) s_warp[warp] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cdd all = s_warp[0];
+        for (int w = 1; w < nwarps; ++w) all = cdd_add(all, s_warp[w]);
+        double o[2];
+        // the double-float partials carry the range boost; the FP64 twin's
+        // (it ran when the range check or the error estimate sent the layer
+        // to it) do not
+        const bool dfok = df_info && df_info[1];
+        const int ex = dfok ? *exp_in - (col_e[j] - df_info[0]) : *exp_fp64 - col_e[j];
+        write_result(all, ex, o, nullptr);
+        perm_out[j] = make_double2(o[0], o[1]);
+        __threadfence();
+        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
     }
+    __syncthreads();
+    if (!s_last) return;
+    // the last block: contraction with the interferometer and normalisation,
+    // in the reference's order (input modes ascending, total over modes
+    // ascending)
+    __threadfence();
+    const volatile double* pv = reinterpret_cast<const volatile double*>(perm_out);
     for (int i = threadIdx.x; i < m; i += blockDim.x) addends[i] = make_double2(0.0, 0.0);
     __syncthreads();
-    for (int j = threadIdx.x; j < C; j += blockDim.x) addends[col_mode[j]] = s_perm[j];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) addends[col_mode[c]] = make_double2(pv[2 * c], pv[2 * c + 1]);
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
         double re = 0.0, im = 0.0;
-        for (int j = 0; j < C; ++j) {
-            const double2 u = U[(long long)i * ldu + col_mode[j]];
-            const double pr = cin_w[j] * s_perm[j].x, pi = cin_w[j] * s_perm[j].y;
+        for (int c = 0; c < C; ++c) {
+            const double2 u = U[(long long)i * ldu + col_mode[c]];
+            const double pr = cin_w[c] * pv[2 * c], pi = cin_w[c] * pv[2 * c + 1];
             re += pr * u.x - pi * u.y;
             im += pr * u.y + pi * u.x;
         }
@@ -656,13 +672,14 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int i = 0; i < m; ++i) tot += pmf[i];
-        s_tot = tot;
+        double t = 0.0;
+        for (int i = 0; i < m; ++i) t += pmf[i];
+        s_tot = t;
+        *done = 0u;  // ready for the next layer
     }
     __syncthreads();
-    const double tot = s_tot;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) pmf[i] = pmf[i] / tot;
+    const double t = s_tot;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) pmf[i] = pmf[i] / t;
 }
 
 // ------------------------------------------ integer-mantissa product
@@ -1186,6 +1203,7 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     const size_t o_add = take((size_t)m * sizeof(double2));  // 16-byte elements: own aligned region
     const size_t o_part = take((size_t)grid * C * sizeof(cdd));
     const size_t o_s2 = take((size_t)grid * C * sizeof(double));
+    const size_t o_perm = take((size_t)C * sizeof(double2) + sizeof(unsigned int));
     rc = cx.ensure(off);
     if (rc) return rc;
     char* base = static_cast<char*>(cx.dbuf);
@@ -1280,12 +1298,15 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     }
     double* d_pmf = reinterpret_cast<double*>(base + o_pmf);
     double2* d_add = reinterpret_cast<double2*>(base + o_add);
-    const size_t fsmem = (size_t)C * sizeof(double2);
-    pmf_finalize_kernel<<<1, kFinThreads, fsmem, st>>>(d_part, nblocks, C, d_exp, d_exp + 1, d_ints + i_cole,
-                                                       df ? d_exp + 4 : nullptr, d_ints + i_mode,
-                                                       reinterpret_cast<const double*>(base + o_cw),
-                                                       reinterpret_cast<const double2*>(base + o_U), m, (int)m,
-                                                       d_pmf, d_add);
+    double2* d_perm = reinterpret_cast<double2*>(base + o_perm);
+    unsigned int* d_done = reinterpret_cast<unsigned int*>(d_perm + C);
+    e = cudaMemsetAsync(d_done, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: finalize counter");
+    pmf_finalize_kernel<<<C, kFinThreads, 0, st>>>(d_part, nblocks, C, d_exp, d_exp + 1, d_ints + i_cole,
+                                                   df ? d_exp + 4 : nullptr, d_ints + i_mode,
+                                                   reinterpret_cast<const double*>(base + o_cw),
+                                                   reinterpret_cast<const double2*>(base + o_U), m, (int)m, d_pmf,
+                                                   d_add, d_perm, d_done);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: finalize");
     if (stats) cudaEventRecord(cx.ev1, st);
