@@ -1302,11 +1302,13 @@ extern "C" int gbperm_compute_pmf(const double* U, int64_t m, int64_t ld, const 
     unsigned int* d_done = reinterpret_cast<unsigned int*>(d_perm + C);
     e = cudaMemsetAsync(d_done, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: finalize counter");
-    pmf_finalize_kernel<<<C, kFinThreads, 0, st>>>(d_part, nblocks, C, d_exp, d_exp + 1, d_ints + i_cole,
-                                                   df ? d_exp + 4 : nullptr, d_ints + i_mode,
-                                                   reinterpret_cast<const double*>(base + o_cw),
-                                                   reinterpret_cast<const double2*>(base + o_U), m, (int)m, d_pmf,
-                                                   d_add, d_perm, d_done);
+    // one warp per column: a warp-wide double-double add costs the FP64
+    // pipe the same whatever the partial count, so fewer, fuller warps
+    pmf_finalize_kernel<<<C, 32, 0, st>>>(d_part, nblocks, C, d_exp, d_exp + 1, d_ints + i_cole,
+                                          df ? d_exp + 4 : nullptr, d_ints + i_mode,
+                                          reinterpret_cast<const double*>(base + o_cw),
+                                          reinterpret_cast<const double2*>(base + o_U), m, (int)m, d_pmf, d_add,
+                                          d_perm, d_done);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_compute_pmf: finalize");
     if (stats) cudaEventRecord(cx.ev1, st);
