@@ -46,7 +46,7 @@ __global__ void prepare_kernel(PrepArgs p) {
             double w = p.row_w ? (double)p.row_w[i] : 1.0;
             br += w * fabs(a.x);
             bi += w * fabs(a.y);
-            l2 += w * (a.x * a.x + a.y * a.y);
+            if (p.df) l2 += w * (a.x * a.x + a.y * a.y);
         }
         // a little headroom so that rounding in the bound never lets a sum
         // reach 2^62 in fixed point
@@ -55,7 +55,9 @@ __global__ void prepare_kernel(PrepArgs p) {
         if (b > 0.0) frexp(b, &e);
         s_e[j] = e;
         if (p.col_e_out) p.col_e_out[j] = e;
-        s_typ[j] = b > 0.0 ? log2(sqrt(l2) / ldexp(1.0, e)) : -1e300;
+        // the typical column size only feeds the double-float range boost
+        // (the FP64 pipe is slow on GB300: skip the log2 otherwise)
+        s_typ[j] = (p.df && b > 0.0) ? log2(sqrt(l2) / ldexp(1.0, e)) : -1e300;
         for (int i = 0; i < p.rows; ++i) {
             double2 a = p.A[(long long)i * p.ld + j];
             long long xr = __double2ll_rn(ldexp(a.x, GBPERM_FIX_BITS - e - s_k[i]));
