@@ -935,13 +935,21 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
         }
     }
     __syncthreads();
-    // column j = g*CPL + c is held by the threads t with t % G == g: sum them
-    // in a fixed order
+    // column j = g*CPL + c is held by the threads t with t % G == g: a tree
+    // over t (strides kThreads/2 .. G keep the residue mod G), the (t, c)
+    // pairs of each level spread over the block -- a few dependent
+    // double-double adds per thread instead of kThreads/G in one thread
+    // (FP64 latency dominates this epilogue on GB300); fixed order
+    for (int st = kThreads / 2; st >= G; st >>= 1) {
+        for (int it = threadIdx.x; it < st * CPL; it += blockDim.x) {
+            const int t = it % st, c = it / st;
+            s_acc[c * kThreads + t] = cdd_add(s_acc[c * kThreads + t], s_acc[c * kThreads + t + st]);
+        }
+        __syncthreads();
+    }
     for (int j = threadIdx.x; j < NP; j += blockDim.x) {
         const int gj = j / CPL, c = j % CPL;
-        cdd b = s_acc[c * kThreads + gj];
-        for (int t = gj + G; t < kThreads; t += G) b = cdd_add(b, s_acc[c * kThreads + t]);
-        if (j < C) col_part[(size_t)blockIdx.x * C + j] = b;
+        if (j < C) col_part[(size_t)blockIdx.x * C + j] = s_acc[c * kThreads + gj];
     }
 }
 
