@@ -633,7 +633,16 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
     const int j = blockIdx.x;
     cdd tot{{0.0, 0.0}, {0.0, 0.0}};
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) tot = cdd_add(tot, col_part[(size_t)b * C + j]);
-    tot = warp_sum_cdd(tot);
+    // a tree over the lanes that hold partials only (ceil(log2 nblocks)
+    // levels; a small layer's few blocks skip most of the butterfly)
+    const int used = nblocks < 32 ? nblocks : 32;
+    int span = 1;
+    while (span < used) span <<= 1;
+    for (int s = span >> 1; s > 0; s >>= 1) {
+        cdd o{{__shfl_down_sync(0xffffffffu, tot.re.hi, s), __shfl_down_sync(0xffffffffu, tot.re.lo, s)},
+              {__shfl_down_sync(0xffffffffu, tot.im.hi, s), __shfl_down_sync(0xffffffffu, tot.im.lo, s)}};
+        if (lane + s < span) tot = cdd_add(tot, o);
+    }
     if (lane == 0) s_warp[warp] = tot;
     __syncthreads();
     if (threadIdx.x == 0) {
