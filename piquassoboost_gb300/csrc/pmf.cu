@@ -68,6 +68,23 @@ __device__ __noinline__ cd cpow_pos(cd x, int e) {
     return acc;
 }
 
+// Sum each column's per-thread partials -- column g*CPL + c is held by the
+// threads t with t % G == g, at s_acc[c * kThreads + t] -- by a tree over t
+// (strides kThreads/2 .. G keep the residue mod G) with the (t, c) pairs of
+// each level spread over the block; the sum ends at s_acc[c * kThreads + g].
+// A few dependent double-double adds per thread instead of kThreads/G in
+// one thread: FP64 latency dominates this epilogue on GB300.  Fixed order.
+template <int CPL, int G>
+__device__ __forceinline__ void column_tree(cdd* s_acc) {
+    for (int st = kThreads / 2; st >= G; st >>= 1) {
+        for (int it = threadIdx.x; it < st * CPL; it += blockDim.x) {
+            const int t = it % st, c = it / st;
+            s_acc[c * kThreads + t] = cdd_add(s_acc[c * kThreads + t], s_acc[c * kThreads + t + st]);
+        }
+        __syncthreads();
+    }
+}
+
 template <int CPL, int G>
 __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part) {
     constexpr int NP = CPL * G;
@@ -264,13 +281,10 @@ __global__ void __launch_bounds__(kThreads) pmf_kernel(RepArgs p, cdd* col_part)
         }
     }
     __syncthreads();
-    // column j = g*CPL + c is held by the threads t with t % G == g: sum them
-    // in a fixed order
+    column_tree<CPL, G>(s_acc);
     for (int j = threadIdx.x; j < NP; j += blockDim.x) {
         const int gj = j / CPL, c = j % CPL;
-        cdd b = s_acc[c * kThreads + gj];
-        for (int t = gj + G; t < kThreads; t += G) b = cdd_add(b, s_acc[c * kThreads + t]);
-        if (j < C) col_part[(size_t)blockIdx.x * C + j] = b;
+        if (j < C) col_part[(size_t)blockIdx.x * C + j] = s_acc[c * kThreads + gj];
     }
 }
 
@@ -944,18 +958,7 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
         }
     }
     __syncthreads();
-    // column j = g*CPL + c is held by the threads t with t % G == g: a tree
-    // over t (strides kThreads/2 .. G keep the residue mod G), the (t, c)
-    // pairs of each level spread over the block -- a few dependent
-    // double-double adds per thread instead of kThreads/G in one thread
-    // (FP64 latency dominates this epilogue on GB300); fixed order
-    for (int st = kThreads / 2; st >= G; st >>= 1) {
-        for (int it = threadIdx.x; it < st * CPL; it += blockDim.x) {
-            const int t = it % st, c = it / st;
-            s_acc[c * kThreads + t] = cdd_add(s_acc[c * kThreads + t], s_acc[c * kThreads + t + st]);
-        }
-        __syncthreads();
-    }
+    column_tree<CPL, G>(s_acc);
     for (int j = threadIdx.x; j < NP; j += blockDim.x) {
         const int gj = j / CPL, c = j % CPL;
         if (j < C) col_part[(size_t)blockIdx.x * C + j] = s_acc[c * kThreads + gj];
