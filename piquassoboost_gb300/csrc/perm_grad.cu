@@ -872,11 +872,28 @@ static GradPlan plan_grad(int n, int count, bool fx = false) {
     return gp;
 }
 
+// The integer-mantissa twin behind a double-float batch recomputes only the
+// matrices handed over (usually a few: near-vanishing permanents), so its
+// launch is planned as if for count / spread matrices: a handed-over
+// matrix gets `spread` times the blocks the double-float sweep gave it,
+// while the blocks of the others return at once.  spread <= 16, and the
+// twin's per-warp tiles are kept within 64 MiB.
+static GradPlan plan_grad_twin(int n, int count) {
+    int spread = 16;
+    GradPlan gp = plan_grad(n, std::max(1, count / spread), true);
+    while (spread > 1 && (double)count * gp.nwarps * n * n * sizeof(float4) > 64.0 * 1024 * 1024) {
+        spread >>= 1;
+        gp = plan_grad(n, std::max(1, count / spread), true);
+    }
+    gp.count = count;
+    return gp;
+}
+
 struct GradWs {
     size_t a1, a2, exp, exp64, dfi, cole, rowk, warp_g, part, warp_s2, est, total;
 };
 
-static GradWs grad_ws_layout(int n, const GradPlan& gp) {
+static GradWs grad_ws_layout(int n, const GradPlan& gp, const GradPlan* twin = nullptr) {
     GradWs w;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -892,8 +909,10 @@ static GradWs grad_ws_layout(int n, const GradPlan& gp) {
     w.dfi = take(c * 2 * sizeof(int));
     w.cole = take(c * n * sizeof(int));
     w.rowk = take(c * n * sizeof(int));
-    w.warp_g = take(c * gp.nwarps * n * n * sizeof(float4));
-    w.part = take(c * gp.nchunks * n * n * sizeof(float4));
+    const size_t tw = twin ? std::max(gp.nwarps, twin->nwarps) : gp.nwarps;
+    const size_t tc = twin ? std::max(gp.nchunks, twin->nchunks) : gp.nchunks;
+    w.warp_g = take(c * tw * n * n * sizeof(float4));
+    w.part = take(c * tc * n * n * sizeof(float4));
     w.warp_s2 = take(c * gp.nwarps * sizeof(double));
     w.est = take(c * sizeof(double));
     w.total = off;
@@ -904,7 +923,8 @@ static size_t grad_ws_bytes(int n, int count) {
     size_t most = 256;
     for (int done = 0; done < count; done += kMaxBatchLaunch) {
         const int c = std::min(kMaxBatchLaunch, count - done);
-        most = std::max(most, grad_ws_layout(n, plan_grad(n, c, false)).total);
+        const GradPlan twin = plan_grad_twin(n, c);
+        most = std::max(most, grad_ws_layout(n, plan_grad(n, c, false), &twin).total);
         most = std::max(most, grad_ws_layout(n, plan_grad(n, c, true)).total);
         if (count > kMaxBatchLaunch) break;  // all full launches have the same layout; the last is smaller
     }
@@ -929,7 +949,9 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         const int c = std::min(kMaxBatchLaunch, count - done);
         GradPlan gp = plan_grad(n, c, fx_only);
         if (used) *used = gp;
-        const GradWs w = grad_ws_layout(n, gp);
+        // the twin's own launch shape (the same as gp when it runs alone)
+        const GradPlan gt = fx_only ? gp : plan_grad_twin(n, c);
+        const GradWs w = grad_ws_layout(n, gp, fx_only ? nullptr : &gt);
         if (ws_bytes < w.total) return fail(GBPERM_ERR_ARG, "gbperm_perm_grad: workspace too small");
         char* base = static_cast<char*>(ws);
         longlong2* a1 = reinterpret_cast<longlong2*>(base + w.a1);
@@ -998,14 +1020,17 @@ static int run_grad_dev(const double2* dA, long long ld, long long stride, int n
         // range check or the error estimate handed over
         g.warp_s2 = nullptr;
         g.gate = fx_only ? nullptr : df_info;
-        if (gp.cpl == 4) grad_fx_kernel<4><<<grid, kThreads, grad_smem<4>(n), st>>>(g);
-        else grad_fx_kernel<8><<<grid, kThreads, grad_smem<8>(n), st>>>(g);
+        g.seg_log2 = gt.seg_log2;
+        g.nseg = gt.nseg;
+        const dim3 grid_t(gt.grid, c);
+        if (gt.cpl == 4) grad_fx_kernel<4><<<grid_t, kThreads, grad_smem<4>(n), st>>>(g);
+        else grad_fx_kernel<8><<<grid_t, kThreads, grad_smem<8>(n), st>>>(g);
         e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(e, "gbperm_perm_grad: fx kernel");
         double2* part2 = reinterpret_cast<double2*>(fin_part);
-        grad_partial_fx_kernel<<<dim3((ne + 127) / 128, gp.nchunks, c), 128, 0, st>>>(
-            reinterpret_cast<const double2*>(warp_g), gp.nwarps, n, part2, g.gate);
-        grad_finalize_fx_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(part2, gp.nchunks, n, exp64, col_e,
+        grad_partial_fx_kernel<<<dim3((ne + 127) / 128, gt.nchunks, c), 128, 0, st>>>(
+            reinterpret_cast<const double2*>(warp_g), gt.nwarps, n, part2, g.gate);
+        grad_finalize_fx_kernel<<<dim3((ne + 127) / 128, c), 128, 0, st>>>(part2, gt.nchunks, n, exp64, col_e,
                                                                            row_k, g.gate, gout);
         grad_perm_kernel<<<c, 32, 0, st>>>(Ab, ld, stride, n, gout, fx_only ? nullptr : df_info, pout, p4, nullptr,
                                            0, nullptr, nullptr, 0);
