@@ -14,7 +14,8 @@
 //
 // Value convention: a mantissa m with shift count sigma stands for
 //     m * 2^(-61 - sigma).
-// A column sum C (unit 2^-62, |C| < 2^62 per component) enters as y = C >> 1
+// A column sum C (unit 2^-62, |C| <= 2^62 per component; 2^62 is the exact
+// value 1 a padding column carries) enters as y = C >> 1
 // with sigma = 0.  fx_mul returns R = x y / 2^62 (sigma_R = sigma_x +
 // sigma_y - 1); fx_norm shifts R left by s (sigma += s).  A chain of k
 // multiplies over factors with sigma = 0 therefore ends with
@@ -22,7 +23,7 @@
 //
 // Range invariants (what keeps every intermediate inside int64):
 //   * normalised operands: |component| <= 2^59, so |h| <= 2^28;
-//   * column factors: |component| < 2^61, so |h| < 2^30;
+//   * column factors: |component| <= 2^61, so |h| <= 2^30;
 //   * the cross sum of fx_mul is at most 2^30 + 2 * 2^59 + 2 * 2^61 < 2^63;
 //   * |x y| / 2^62 <= (sqrt2 2^59)(sqrt2 2^61) / 2^62 = 2^59, so R's
 //     components are at most 2^59 + 2 and its high word at most 2^27,
@@ -36,7 +37,7 @@ struct fxl {  // limbs of a complex mantissa: re = rh 2^31 + rl, im = ih 2^31 + 
     int rh, rl, ih, il;
 };
 
-// Limbs of the column factor y = C >> 1 (C: int64 column sum, |C| < 2^62):
+// Limbs of the column factor y = C >> 1 (C: int64 column sum, |C| <= 2^62):
 // the high limb is C's high word, the low limb C's low word shifted right by
 // one (bits 1..31 of C).
 __device__ __forceinline__ fxl fx_col(long long cr, long long ci) {
@@ -103,12 +104,12 @@ __device__ __forceinline__ int fx_norm(long long re, long long im, fxl& x) {
     return 26 - f;
 }
 
-// Normalise a column factor y = C >> 1 (|component| < 2^61) as the first
-// factor of a product chain: same target as fx_norm, shift s in [-2, 27].
+// Normalise a column factor y = C >> 1 (|component| <= 2^61) as the first
+// factor of a product chain: same target as fx_norm, shift s in [-3, 27].
 __device__ __forceinline__ int fx_norm_col(long long cr, long long ci, fxl& x) {
     const long long yr = cr >> 1, yi = ci >> 1;
     const int hr = (int)(yr >> 32), hi = (int)(yi >> 32);
-    const int f = fx_lead2(hr, hi);    // <= 28
+    const int f = fx_lead2(hr, hi);    // <= 29
     const int s = 26 - f;
     long long vr, vi;
     if (s >= 0) {

@@ -335,7 +335,7 @@ static int run_repeated(const double* A, int64_t rows, int64_t cols, int64_t ld,
     int xcpl = 0, xgrp = 0, grid_fx = 1;
     if (fx) repeated_fx_shape(h.C, &xcpl, &xgrp);
     if (df) deal_columns_by_power(&h, dgrp, dcpl);
-    else if (fx) deal_columns_by_power(&h, xgrp, (h.C + xgrp - 1) / xgrp);
+    else if (fx) deal_columns_by_power(&h, xgrp, xcpl);
     int dev = 0;
     cudaGetDevice(&dev);
     const unsigned long long sms = (unsigned long long)device_sms(dev);

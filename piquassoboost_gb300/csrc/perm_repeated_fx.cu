@@ -61,20 +61,19 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
     __syncthreads();
 
     const int g = threadIdx.x % GROUP;
-    // the columns split evenly over the group (the warp runs the longest
-    // lane's columns)
-    const int cpl_i = (C + GROUP - 1) / GROUP;
-    const int j0 = g * cpl_i;
-    // real columns of this lane: contiguous from its first column (>= 1:
-    // C > (GROUP - 1) ceil(C / GROUP) for every shape the host picks)
-    const int nr = C - j0 < cpl_i ? C - j0 : cpl_i;
+    // lane g owns columns [g CPL, (g + 1) CPL); the host picks CPL =
+    // ceil(C / 2) for lane pairs, so only the last lane may hold padding
+    // columns, which carry the exact value 1 (column sum 2^62 at every step)
+    // and are multiplied like the others: no per-column predicate
+    const int j0 = g * CPL;
     // bit c: this lane's column c has power > 1 (the step loop runs the
     // common power-1 multiply unconditionally); power 0 among the real
-    // columns cannot occur (the host drops empty columns)
+    // columns cannot occur (the host drops empty columns), padding columns
+    // have power 0 and value 1
     unsigned int extra = 0u;
 #pragma unroll
     for (int c = 0; c < CPL; ++c)
-        if (c < nr && s_cpow[j0 + c] > 1) extra |= 1u << c;
+        if (s_cpow[j0 + c] > 1) extra |= 1u << c;
     const bool leader = (g == 0);
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
@@ -107,7 +106,7 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
         }
 #pragma unroll
         for (int c = 0; c < CPL; ++c) {
-            cre[c] = 0;
+            cre[c] = j0 + c < C ? 0 : (1ll << GBPERM_FIX_BITS);
             cim[c] = 0;
         }
         int gsum = 0;
@@ -173,43 +172,37 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
                     bim = 0.0;
                 }
             }
-            // prod_c colsum_c^(power_c) of this lane's real columns, in two
-            // chains; sig: shift count (shifts minus multiplies)
+            // prod_c colsum_c^(power_c) of this lane's columns (padding
+            // columns: 1), in two chains; sig: shift count (shifts minus
+            // multiplies)
             fxl ch[2];
             int sig = 0;
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
-                if (c < nr) {
-                    // a column of power e multiplies its chain e times by the
-                    // same column factor (the host lays the columns out so
-                    // that column c of every lane group has nearly the same
-                    // power: the extra multiplies diverge little)
-                    const fxl y = fx_col(cre[c], cim[c]);
-                    if (c < 2) {
-                        sig += fx_norm_col(cre[c], cim[c], ch[c]);
-                    } else {
+                // a column of power e multiplies its chain e times by the
+                // same column factor (the host lays the columns out so that
+                // column c of every lane group has nearly the same power: the
+                // extra multiplies diverge little)
+                const fxl y = fx_col(cre[c], cim[c]);
+                if (c < 2) {
+                    sig += fx_norm_col(cre[c], cim[c], ch[c]);
+                } else {
+                    long long rr, ri;
+                    fx_mul(ch[c & 1], y, rr, ri);
+                    sig += fx_norm(rr, ri, ch[c & 1]) - 1;
+                }
+                if ((extra >> c) & 1u) {
+                    const int e = s_cpow[j0 + c];
+                    for (int t = 1; t < e; ++t) {
                         long long rr, ri;
                         fx_mul(ch[c & 1], y, rr, ri);
                         sig += fx_norm(rr, ri, ch[c & 1]) - 1;
                     }
-                    if ((extra >> c) & 1u) {
-                        const int e = s_cpow[j0 + c];
-                        for (int t = 1; t < e; ++t) {
-                            long long rr, ri;
-                            fx_mul(ch[c & 1], y, rr, ri);
-                            sig += fx_norm(rr, ri, ch[c & 1]) - 1;
-                        }
-                    }
                 }
             }
             long long pr, pi;
-            if (nr >= 2) {
-                fx_mul(ch[0], ch[1], pr, pi);
-                sig -= 1;
-            } else {
-                pr = fx_join(ch[0].rh, ch[0].rl);
-                pi = fx_join(ch[0].ih, ch[0].il);
-            }
+            fx_mul(ch[0], ch[1], pr, pi);  // every shape has CPL >= 5
+            sig -= 1;
 #pragma unroll
             for (int m = 1; m < GROUP; m <<= 1) {
                 fxl x;
