@@ -802,13 +802,14 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
     const int g = lane % G;
     const int lbase = lane - g;
     const int j0 = g * CPL;
-    // this lane's real columns (the padding columns of the last lanes come
-    // after them)
-    const int nr = max(0, min(CPL, C - j0));
+    // the padding columns of the last lanes (j >= C) carry the exact value
+    // 1 (column sum 2^62, power 0) and go through the products like the
+    // others -- no per-column predicate; their leave-one-out sums are not
+    // written
     unsigned int extra = 0u;  // bit c: column c has power > 1
 #pragma unroll
     for (int c = 0; c < CPL; ++c)
-        if (c < nr && s_cpow[j0 + c] > 1) extra |= 1u << c;
+        if (s_cpow[j0 + c] > 1) extra |= 1u << c;
     cdd* my_acc = s_acc + threadIdx.x;  // column c at my_acc[c * kThreads]
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / G;
     const unsigned long long lane_seg = (unsigned long long)(lane / G);
@@ -840,7 +841,7 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
         }
 #pragma unroll
         for (int c = 0; c < CPL; ++c) {
-            cre[c] = 0;
+            cre[c] = j0 + c < C ? 0 : (1ll << GBPERM_FIX_BITS);
             cim[c] = 0;
         }
         int gsum = 0;
@@ -919,12 +920,10 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
             fxs part = fxs_one();
 #pragma unroll
             for (int c = 0; c < CPL; ++c) {
-                if (c < nr) {
-                    fxs pc = fxs_col(cre[c], cim[c]);
-                    if ((extra >> c) & 1u) pc = fxs_mul_pow(pc, pc, s_cpow[j0 + c] - 1);
-                    pre[c] = part;
-                    part = (c == 0) ? pc : fxs_mul(part, pc);
-                }
+                fxs pc = fxs_col(cre[c], cim[c]);
+                if ((extra >> c) & 1u) pc = fxs_mul_pow(pc, pc, s_cpow[j0 + c] - 1);
+                pre[c] = part;
+                part = (c == 0) ? pc : fxs_mul(part, pc);
             }
             // the other lanes' partials, then backwards:
             // LO_c = prefix_c x (others x suffix_c) x x_c^(c_c - 1)
@@ -934,18 +933,15 @@ __global__ void __launch_bounds__(kThreads, 3) pmf_fx_kernel(RepArgs p, cdd* col
             const double w = sgn * s_w[widx];
 #pragma unroll
             for (int c = CPL - 1; c >= 0; --c) {
-                if (c < nr) {
-                    fxs lo = (c == 0) ? run : fxs_mul(pre[c], run);
-                    if ((extra >> c) & 1u)
-                        lo = fxs_mul_pow(lo, fxs_col(cre[c], cim[c]), s_cpow[j0 + c] - 1);
-                    const int ex = -61 - lo.s;
-                    blk[c].re = fma(w, fx_to_double(fx_join(lo.m.rh, lo.m.rl), ex), blk[c].re);
-                    blk[c].im = fma(w, fx_to_double(fx_join(lo.m.ih, lo.m.il), ex), blk[c].im);
-                    if (c > 0) {
-                        fxs pc = fxs_col(cre[c], cim[c]);
-                        if ((extra >> c) & 1u) pc = fxs_mul_pow(pc, pc, s_cpow[j0 + c] - 1);
-                        run = fxs_mul(run, pc);
-                    }
+                fxs lo = (c == 0) ? run : fxs_mul(pre[c], run);
+                if ((extra >> c) & 1u) lo = fxs_mul_pow(lo, fxs_col(cre[c], cim[c]), s_cpow[j0 + c] - 1);
+                const int ex = -61 - lo.s;
+                blk[c].re = fma(w, fx_to_double(fx_join(lo.m.rh, lo.m.rl), ex), blk[c].re);
+                blk[c].im = fma(w, fx_to_double(fx_join(lo.m.ih, lo.m.il), ex), blk[c].im);
+                if (c > 0) {
+                    fxs pc = fxs_col(cre[c], cim[c]);
+                    if ((extra >> c) & 1u) pc = fxs_mul_pow(pc, pc, s_cpow[j0 + c] - 1);
+                    run = fxs_mul(run, pc);
                 }
             }
         }
