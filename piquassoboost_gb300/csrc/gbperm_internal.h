@@ -78,11 +78,13 @@ struct PlainArgs {
     // 2^40) and the relative rounding-error estimate of the result
     double* block_s2 = nullptr;
     double* err_out = nullptr;
-    int* df_ok = nullptr;  // writable df_info[1]: cleared to hand the result to the FP64 twin
+    int* df_ok = nullptr;  // writable df_info[1]: cleared to hand the result to the twin
 };
 
 // A double-float result whose estimated relative rounding error exceeds this
-// (the 1e-10 accuracy bar) is recomputed by the FP64 twin kernel.  The
+// (the 1e-10 accuracy bar) is recomputed by the twin kernel (integer-mantissa
+// for plain and repeated permanents and the gradient, FP64 for pmf layers
+// and the plain batch plans).  The
 // estimate sat above the measured error in every case checked (2-8x
 // typically; Haar, rescaled, Gaussian and positive matrices, n = 16-36).
 constexpr double kDfEscalate = 1e-10;
@@ -187,8 +189,8 @@ __device__ __forceinline__ void write_result(cdd v, int e, double* out2, double*
 //     sqrt(nfac) 2^-46 sqrt(sum |term|^2) / |sum|
 // of its relative rounding error (each term carries ~2^-46 sqrt(nfac)
 // relative error, independent between terms), and when that is above
-// kDfEscalate (or not finite) clears *df_ok so that the FP64 twin launched
-// next on the stream recomputes and overwrites the result.
+// kDfEscalate (or not finite) clears *df_ok so that the twin launched next
+// on the stream recomputes and overwrites the result.
 template <int THREADS>
 __device__ __forceinline__ void df_grid_finish(cdd acc, double s2, cdd* block_part, double* block_s2,
                                                unsigned int* done, const int* exp_in, double* out2, double* out4,

@@ -15,8 +15,9 @@
 //
 // Accuracy guard: the leaders also sum |term|^2, and the grid finish
 // (df_grid_finish) turns it into an estimate of the result's relative
-// rounding error; above 1e-10 it clears the range-check flag, so the FP64
-// twin (perm_plain.cu), launched next on the same stream, recomputes.
+// rounding error; above 1e-10 it clears the range-check flag, so the
+// integer-mantissa twin (perm_plain_fx.cu), launched next on the same
+// stream, recomputes.
 #include "gbperm_internal.h"
 
 namespace gbperm {

@@ -9,8 +9,8 @@
 // the weights and signs need no exchange.  Segment loops run over warp-sized
 // blocks of segments so all 32 lanes always reach the shuffles.  As in
 // perm_plain_df.cu the sweep ends with a rounding-error estimate that hands
-// the result to the FP64 twin when it is above 1e-10 (at 30 photons most
-// bunched outputs are).
+// the result to the integer-mantissa twin when it is above 1e-10 (at 30
+// photons most bunched outputs are; the host then skips this kernel).
 #include "gbperm_internal.h"
 
 namespace gbperm {
