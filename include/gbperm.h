@@ -87,7 +87,8 @@ const char* gbperm_last_error(void);
 /* Number of visible CUDA devices (0 when none); never fails. */
 int gbperm_device_count(void);
 /* Tuning knobs (process-wide).  Keys:
- *   "plain.seg_log2"      force log2 segment length of the plain kernel (-1 = auto)
+ *   "plain.seg_log2"      force log2 segment length of the plain kernel (-1 = auto;
+ *                         at most 31 is used)
  *   "plain.grid"          force the plain grid size (0 = auto)
  *   "repeated.low_digits" force the digits handled inside a repeated segment (-1 = auto)
  *   "batched.threads"     lanes sharing one Gray segment in a double-float batch plan

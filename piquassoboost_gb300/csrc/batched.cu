@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
 // double with integer instructions.  No range check and no redo pass.
 template <int CPL, int GROUP>
 __global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
+    static_assert(GROUP >= 2, "lanes 0 and 1 of a group convert the two components");
     const int lane = threadIdx.x & 31;
     const int g = lane % GROUP;
     const int grp = lane / GROUP;
@@ -415,7 +416,9 @@ __global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
         }
         cdd acc{{0.0, 0.0}, {0.0, 0.0}};
         unsigned long long sbit = (unsigned long long)(__popcll(g0) & 1) << 63;
-        double bre = 0.0, bim = 0.0;
+        // every lane of a group ends the butterfly with the same product:
+        // lane 0 converts and sums its real part, lane 1 its imaginary part
+        double b0 = 0.0;
         for (unsigned long long k = 0; k < L; ++k) {
             if (k != 0) {
                 const int b = __ffsll((long long)k) - 1;
@@ -441,10 +444,8 @@ __global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
                 }
                 sbit ^= 0x8000000000000000ull;
                 if ((k & 255ull) == 0) {
-                    acc.re = dd_add_d(acc.re, bre);
-                    acc.im = dd_add_d(acc.im, bim);
-                    bre = 0.0;
-                    bim = 0.0;
+                    acc.re = dd_add_d(acc.re, b0);
+                    b0 = 0.0;
                 }
             }
             // the lane's partial product in two chains (sig: shift count)
@@ -489,14 +490,16 @@ __global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
                 sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
                 fx_mul(x, y, pr, pi);
             }
-            if (g == 0 && active) {
+            if (g < 2 && active) {  // every shape has GROUP >= 2
                 const int e = -61 - sig;
-                bre += __longlong_as_double(__double_as_longlong(fx_to_double(pr, e)) ^ (long long)sbit);
-                bim += __longlong_as_double(__double_as_longlong(fx_to_double(pi, e)) ^ (long long)sbit);
+                b0 += __longlong_as_double(__double_as_longlong(fx_to_double(g == 0 ? pr : pi, e)) ^ (long long)sbit);
             }
         }
-        acc.re = dd_add_d(acc.re, bre);
-        acc.im = dd_add_d(acc.im, bim);
+        acc.re = dd_add_d(acc.re, b0);
+        if (g == 1) {  // lane 1 summed the imaginary part
+            acc.im = acc.re;
+            acc.re = dd{0.0, 0.0};
+        }
         acc = warp_sum_cdd(acc);
         if (lane == 0) {
             p.item_part[it] = acc;

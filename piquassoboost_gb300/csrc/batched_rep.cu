@@ -238,8 +238,12 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
         __syncwarp();  // strides written by lane 0 (the same for every lane: one instance per item)
         unsigned long long sbit = (unsigned long long)(gsum & 1) << 63;
         cdd acc{{0.0, 0.0}, {0.0, 0.0}};
-        double bre = 0.0, bim = 0.0;
-        for (unsigned long long k = 0; k < in.P; ++k) {
+        // every lane of a group ends the butterfly with the same product:
+        // with GROUP >= 2 lane 0 converts and sums its real part in b0 and
+        // lane 1 its imaginary part
+        double b0 = 0.0, b1 = 0.0;
+        const unsigned int P = (unsigned int)in.P;  // at most 4096 (low-digit table)
+        for (unsigned int k = 0; k < P; ++k) {
             if (k != 0) {
                 const int d = __ldg(&sq[k]);  // warp-uniform (one instance per item)
                 const bool up = (dir >> d) & 1u;  // warp-uniform (one parity per item)
@@ -268,11 +272,13 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
                         }
                 }
                 sbit ^= 0x8000000000000000ull;
-                if ((k & 255ull) == 0) {
-                    acc.re = dd_add_d(acc.re, bre * whigh);
-                    acc.im = dd_add_d(acc.im, bim * whigh);
-                    bre = 0.0;
-                    bim = 0.0;
+                if ((k & 255u) == 0) {
+                    acc.re = dd_add_d(acc.re, b0 * whigh);
+                    b0 = 0.0;
+                    if (GROUP == 1) {
+                        acc.im = dd_add_d(acc.im, b1 * whigh);
+                        b1 = 0.0;
+                    }
                 }
             }
             // this lane's partial product in two chains; a lane without
@@ -329,17 +335,25 @@ __global__ void __launch_bounds__(kThreads) rep_batched_kernel(RArgs p) {
                 sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
                 fx_mul(x, y, pr, pi);
             }
-            if (g == 0 && active) {
+            if (active && (GROUP == 1 || g < 2)) {
                 const int ex = -61 - sig;
                 const double w = __ldg(&wl[widx]);
-                const double tr = __longlong_as_double(__double_as_longlong(fx_to_double(pr, ex)) ^ (long long)sbit);
-                const double ti = __longlong_as_double(__double_as_longlong(fx_to_double(pi, ex)) ^ (long long)sbit);
-                bre = fma(w, tr, bre);
-                bim = fma(w, ti, bim);
+                const long long v0 = GROUP == 1 || g == 0 ? pr : pi;
+                const double t0 = __longlong_as_double(__double_as_longlong(fx_to_double(v0, ex)) ^ (long long)sbit);
+                b0 = fma(w, t0, b0);
+                if (GROUP == 1) {
+                    const double t1 =
+                        __longlong_as_double(__double_as_longlong(fx_to_double(pi, ex)) ^ (long long)sbit);
+                    b1 = fma(w, t1, b1);
+                }
             }
         }
-        acc.re = dd_add_d(acc.re, bre * whigh);
-        acc.im = dd_add_d(acc.im, bim * whigh);
+        acc.re = dd_add_d(acc.re, b0 * whigh);
+        if (GROUP == 1) acc.im = dd_add_d(acc.im, b1 * whigh);
+        if (GROUP > 1 && g == 1) {  // lane 1 summed the imaginary part
+            acc.im = acc.re;
+            acc.re = dd{0.0, 0.0};
+        }
         acc = warp_sum_cdd(acc);
         if (lane == 0) p.item_part[it] = acc;
     }

@@ -145,6 +145,7 @@ static void plain_geometry(int rows, int grid_full, int seg_threads, int* grid, 
     if (l < 0) l = 0;
     int64_t force = g_opt.plain_seg_log2.load();
     if (force >= 0) l = (int)(force > slog ? slog : force);
+    if (l > 31) l = 31;  // the integer-mantissa kernel counts steps in 32 bits
     unsigned long long nseg = 1ull << (slog - l);
     unsigned long long per_block = 128ull / seg_threads;
     unsigned long long need = (nseg + per_block - 1) / per_block;

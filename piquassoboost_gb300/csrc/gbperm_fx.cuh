@@ -95,10 +95,10 @@ __device__ __forceinline__ int fx_norm(long long re, long long im, fxl& x) {
     const unsigned int lr = (unsigned int)re, li = (unsigned int)im;
     const int hr = (int)(re >> 32), hi = (int)(im >> 32);
     const int f = fx_lead2(hr, hi);    // -1 when both high words are 0 or -1
-    const int rs = f + 5;              // 31 - s, in [4, 32]
     const int ls = 27 - f;             // s + 1, in [0, 28]
-    x.rh = (int)__funnelshift_rc(lr, (unsigned int)hr, rs);
-    x.ih = (int)__funnelshift_rc(li, (unsigned int)hi, rs);
+    // high limb = (R << s) >> 31 = the high word of R << (s + 1)
+    x.rh = (int)__funnelshift_l(lr, (unsigned int)hr, ls);
+    x.ih = (int)__funnelshift_l(li, (unsigned int)hi, ls);
     x.rl = (int)((lr << ls) >> 1);
     x.il = (int)((li << ls) >> 1);
     return 26 - f;

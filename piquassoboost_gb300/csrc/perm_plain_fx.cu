@@ -12,10 +12,10 @@
 // Lane groups as in perm_plain_df.cu: GROUP consecutive lanes share one Gray
 // segment, lane g owns columns [g*CPL, (g+1)*CPL), forms their partial
 // product in kChains interleaved chains, and a shuffle butterfly multiplies
-// the GROUP partials.  The leader converts the term to double with integer
-// instructions and sums terms in double (256 steps) folded into a
-// double-double accumulator; the grid reduction is the double-double,
-// fixed-order one of the other plain kernels.
+// the GROUP partials.  Lanes 0 and 1 of the group convert the term's real
+// and imaginary parts to double with integer instructions and sum them in
+// double (256 steps) folded into a double-double accumulator; the grid
+// reduction is the double-double, fixed-order one of the other plain kernels.
 #include "gbperm_fx.cuh"
 #include "gbperm_internal.h"
 
@@ -50,9 +50,8 @@ __global__ void __launch_bounds__(kThreads, (CPL <= 16 ? 4 : 3)) plain_fx_kernel
 
     const int g = threadIdx.x % GROUP;
     const int j0 = g * CPL;
-    const bool leader = (g == 0);
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
-    const unsigned long long L = 1ull << p.seg_log2;
+    const unsigned int L = 1u << p.seg_log2;  // seg_log2 <= 31 (plain_geometry)
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
     long long cre[CPL], cim[CPL];
     // warp-sized blocks of segments: every lane makes the same number of
@@ -82,14 +81,18 @@ __global__ void __launch_bounds__(kThreads, (CPL <= 16 ? 4 : 3)) plain_fx_kernel
             }
         }
         unsigned long long sbit = (unsigned long long)(__popcll(g0) & 1) << 63;
-        double bre = 0.0, bim = 0.0;
-        for (unsigned long long k = 0; k < L; ++k) {
+        // the lanes of a group end the butterfly with the same product: with
+        // GROUP >= 2 lane 0 converts and sums its real part in b0 and lane 1
+        // its imaginary part (half the conversions of one lane doing both)
+        double b0 = 0.0, b1 = 0.0;
+        for (unsigned int k = 0; k < L; ++k) {
             if (k != 0) {
-                const int b = __ffsll((long long)k) - 1;  // warp-uniform
+                const int b = __ffs((int)k) - 1;  // warp-uniform
                 const longlong2* a = s_a2 + (rows - 1 - b) * NP + j0;
                 if (b + 1 < p.seg_log2) {
-                    // below the segment boundary bit the new delta depends on k alone
-                    const bool sub = ((k >> b) ^ (k >> (b + 1))) & 1ull;
+                    // below the segment boundary bit the new delta depends on
+                    // k alone: Gray bit b becomes 1 ^ (bit b + 1 of k)
+                    const bool sub = !((k >> (b + 1)) & 1u);
                     if (sub) {
 #pragma unroll
                         for (int c = 0; c < CPL; ++c) {
@@ -117,11 +120,13 @@ __global__ void __launch_bounds__(kThreads, (CPL <= 16 ? 4 : 3)) plain_fx_kernel
                     }
                 }
                 sbit ^= 0x8000000000000000ull;
-                if ((k & 255ull) == 0) {
-                    acc.re = dd_add_d(acc.re, bre);
-                    acc.im = dd_add_d(acc.im, bim);
-                    bre = 0.0;
-                    bim = 0.0;
+                if ((k & 255u) == 0) {
+                    acc.re = dd_add_d(acc.re, b0);
+                    b0 = 0.0;
+                    if (GROUP == 1) {
+                        acc.im = dd_add_d(acc.im, b1);
+                        b1 = 0.0;
+                    }
                 }
             }
             // partial product of this lane's columns in kChains chains; sig
@@ -151,16 +156,22 @@ __global__ void __launch_bounds__(kThreads, (CPL <= 16 ? 4 : 3)) plain_fx_kernel
                 sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
                 fx_mul(x, y, pr, pi);
             }
-            if (leader && active) {
+            if (active && (GROUP == 1 || g < 2)) {
                 const int e = -61 - sig;
-                const double tr = fx_to_double(pr, e);
-                const double ti = fx_to_double(pi, e);
-                bre += __longlong_as_double(__double_as_longlong(tr) ^ (long long)sbit);
-                bim += __longlong_as_double(__double_as_longlong(ti) ^ (long long)sbit);
+                const double t0 = fx_to_double(GROUP == 1 || g == 0 ? pr : pi, e);
+                b0 += __longlong_as_double(__double_as_longlong(t0) ^ (long long)sbit);
+                if (GROUP == 1) {
+                    const double t1 = fx_to_double(pi, e);
+                    b1 += __longlong_as_double(__double_as_longlong(t1) ^ (long long)sbit);
+                }
             }
         }
-        acc.re = dd_add_d(acc.re, bre);
-        acc.im = dd_add_d(acc.im, bim);
+        acc.re = dd_add_d(acc.re, b0);
+        if (GROUP == 1) acc.im = dd_add_d(acc.im, b1);
+    }
+    if (GROUP > 1 && g == 1) {  // lane 1 summed the imaginary part
+        acc.im = acc.re;
+        acc.re = dd{0.0, 0.0};
     }
 
     // block reduction (double-double, fixed order), then the last block sums

@@ -8,9 +8,9 @@
 // walk one segment, lane g owns columns [g*CPL, (g+1)*CPL), forms their
 // partial product in two interleaved chains, and a shuffle butterfly
 // multiplies the GROUP partials.  Every lane of a group tracks the same Gray
-// digits, so the weights and signs need no exchange.  The leader converts the
-// term to double with integer instructions and accumulates weight x term
-// with one FP64 FMA per component.  No range check, error estimate or FP64
+// digits, so the weights and signs need no exchange.  Lanes 0 and 1 of the
+// group convert the term's real and imaginary parts to double with integer
+// instructions and accumulate weight x term with one FP64 FMA each.  No range check, error estimate or FP64
 // twin: each multiply keeps 55-57 significant bits.
 #include "gbperm_fx.cuh"
 #include "gbperm_internal.h"
@@ -74,7 +74,6 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
 #pragma unroll
     for (int c = 0; c < CPL; ++c)
         if (s_cpow[j0 + c] > 1) extra |= 1u << c;
-    const bool leader = (g == 0);
     cdd acc{{0.0, 0.0}, {0.0, 0.0}};
     const unsigned long long T = ((unsigned long long)gridDim.x * blockDim.x) / GROUP;
     const unsigned long long lane_seg = (threadIdx.x & 31) / GROUP;
@@ -136,8 +135,12 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
             }
         }
         unsigned long long sbit = (unsigned long long)(gsum & 1) << 63;
-        double bre = 0.0, bim = 0.0;
-        for (unsigned long long k = 0; k < p.P; ++k) {
+        // the lanes of a group end the butterfly with the same product: with
+        // GROUP >= 2 lane 0 converts and sums its real part in b0 and lane 1
+        // its imaginary part
+        double b0 = 0.0, b1 = 0.0;
+        const unsigned int P = (unsigned int)p.P;  // at most 4096 (low-digit table)
+        for (unsigned int k = 0; k < P; ++k) {
             if (k != 0) {
                 const int d = s_seq[k];  // warp-uniform
                 const bool up = (dir >> d) & 1u;
@@ -165,11 +168,13 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
                     }
                 }
                 sbit ^= 0x8000000000000000ull;
-                if ((k & 255ull) == 0) {
-                    acc.re = dd_add_d(acc.re, bre * whigh);
-                    acc.im = dd_add_d(acc.im, bim * whigh);
-                    bre = 0.0;
-                    bim = 0.0;
+                if ((k & 255u) == 0) {
+                    acc.re = dd_add_d(acc.re, b0 * whigh);
+                    b0 = 0.0;
+                    if (GROUP == 1) {
+                        acc.im = dd_add_d(acc.im, b1 * whigh);
+                        b1 = 0.0;
+                    }
                 }
             }
             // prod_c colsum_c^(power_c) of this lane's columns (padding
@@ -211,17 +216,25 @@ __global__ void __launch_bounds__(kThreads) repeated_fx_kernel(RepArgs p) {
                 sig += __shfl_xor_sync(0xffffffffu, sig, m) - 1;
                 fx_mul(x, y, pr, pi);
             }
-            if (leader && active) {
+            if (active && (GROUP == 1 || g < 2)) {
                 const int ex = -61 - sig;
                 const double w = s_w[widx];
-                const double tr = __longlong_as_double(__double_as_longlong(fx_to_double(pr, ex)) ^ (long long)sbit);
-                const double ti = __longlong_as_double(__double_as_longlong(fx_to_double(pi, ex)) ^ (long long)sbit);
-                bre = fma(w, tr, bre);
-                bim = fma(w, ti, bim);
+                const long long v0 = GROUP == 1 || g == 0 ? pr : pi;
+                const double t0 = __longlong_as_double(__double_as_longlong(fx_to_double(v0, ex)) ^ (long long)sbit);
+                b0 = fma(w, t0, b0);
+                if (GROUP == 1) {
+                    const double t1 =
+                        __longlong_as_double(__double_as_longlong(fx_to_double(pi, ex)) ^ (long long)sbit);
+                    b1 = fma(w, t1, b1);
+                }
             }
         }
-        acc.re = dd_add_d(acc.re, bre * whigh);
-        acc.im = dd_add_d(acc.im, bim * whigh);
+        acc.re = dd_add_d(acc.re, b0 * whigh);
+        if (GROUP == 1) acc.im = dd_add_d(acc.im, b1 * whigh);
+    }
+    if (GROUP > 1 && g == 1) {  // lane 1 summed the imaginary part
+        acc.im = acc.re;
+        acc.re = dd{0.0, 0.0};
     }
 
     // block reduction (double-double, fixed order); the last block sums the
