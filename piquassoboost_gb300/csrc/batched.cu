@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(kThreads) batched_kernel(BArgs p) {
 // instance's columns split evenly over the GROUP lanes of a walk (a lane
 // holds ceil(cols / GROUP) of them), two product chains per lane on 31-bit
 // limbs, a shuffle butterfly over the group, and the term converted to
-// double with integer instructions.  No range check and no redo pass.
+// double (fx_to_double).  No range check and no redo pass.
 template <int CPL, int GROUP>
 __global__ void __launch_bounds__(kThreads) batched_fx_kernel(BArgs p) {
     static_assert(GROUP >= 2, "lanes 0 and 1 of a group convert the two components");

@@ -555,8 +555,8 @@ __global__ void __launch_bounds__(kThreads, 3) grad_fx_kernel(GradArgs p) {
                     }
                     if (active) {
                         const int e = -61 - sw;
-                        Q[c].x += __longlong_as_double(__double_as_longlong(fx_to_double(wr, e)) ^ (long long)sbit);
-                        Q[c].y += __longlong_as_double(__double_as_longlong(fx_to_double(wi, e)) ^ (long long)sbit);
+                        Q[c].x += __longlong_as_double(__double_as_longlong(fx_to_double_alu(wr, e)) ^ (long long)sbit);
+                        Q[c].y += __longlong_as_double(__double_as_longlong(fx_to_double_alu(wi, e)) ^ (long long)sbit);
                     }
                     if (c > 0) {
                         long long rr, ri;

@@ -13,8 +13,8 @@
 // segment, lane g owns columns [g*CPL, (g+1)*CPL), forms their partial
 // product in kChains interleaved chains, and a shuffle butterfly multiplies
 // the GROUP partials.  Lanes 0 and 1 of the group convert the term's real
-// and imaginary parts to double with integer instructions and sum them in
-// double (256 steps) folded into a double-double accumulator; the grid
+// and imaginary parts to double (fx_to_double) and sum them in double
+// (256 steps) folded into a double-double accumulator; the grid
 // reduction is the double-double, fixed-order one of the other plain kernels.
 #include "gbperm_fx.cuh"
 #include "gbperm_internal.h"

@@ -9,8 +9,8 @@
 // partial product in two interleaved chains, and a shuffle butterfly
 // multiplies the GROUP partials.  Every lane of a group tracks the same Gray
 // digits, so the weights and signs need no exchange.  Lanes 0 and 1 of the
-// group convert the term's real and imaginary parts to double with integer
-// instructions and accumulate weight x term with one FP64 FMA each.  No range check, error estimate or FP64
+// group convert the term's real and imaginary parts to double (fx_to_double)
+// and accumulate weight x term with one FP64 FMA each.  No range check, error estimate or FP64
 // twin: each multiply keeps 55-57 significant bits.
 #include "gbperm_fx.cuh"
 #include "gbperm_internal.h"

@@ -715,9 +715,10 @@ __global__ void __launch_bounds__(kFinThreads) pmf_finalize_kernel(const cdd* co
 // suffix_c) x x_c^(c_c - 1) with P_c recomputed from the column sums: three
 // multiplies per column and step, and no array of powers or suffixes kept
 // in registers (the kernel fits 3 blocks per SM).  Each LO_c is
-// converted to double with integer instructions and accumulated with the
-// step's weight by one FP64 FMA per component, so the FP64 pipe carries 2
-// instructions per column and step where pmf_kernel needs about 14.  The
+// converted to double (fx_to_double: one FP64-pipe conversion per
+// component) and accumulated with the step's weight by one FP64 FMA per
+// component, so the FP64 pipe carries 4 instructions per column and step
+// where pmf_kernel needs about 14.  The
 // row tables are interleaved by lane as in pmf_df_kernel.  No twin: the
 // product needs no range check and is at least as accurate as FP64.
 
