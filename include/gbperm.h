@@ -363,8 +363,11 @@ size_t gbperm_perm_noalloc_scratch_bytes(void);
 /* Measured pipe peak of the current device: kind 0 = FP64 FMA, kind 1 =
  * FP32 FMA, kind 2 = FP64 tensor MMA (mma.sync m8n8k4), all in TFLOP/s
  * (FMA = 2 flops); kind 3 = 32x32->64-bit integer multiply-add
- * (mad.wide.s32), kind 4 = 32-bit integer multiply-add (mad.lo.s32), both
- * in tera lane-operations/s.  Runs ~0.1 s of probe kernels. */
+ * (mad.wide.s32), kind 4 = 32-bit integer multiply-add (mad.lo.s32),
+ * kind 5 = variable funnel shift (shf.l.wrap.b32), kind 6 = 64-bit add
+ * (add.s64), kind 7 = leading-bit search (bfind.s32), kind 8 = 32-bit add
+ * (add.s32), kinds 3-8 in tera lane-operations/s.  Runs ~0.1 s of probe
+ * kernels. */
 int gbperm_probe_peak(int kind, double* tflops);
 
 #ifdef __cplusplus

@@ -467,13 +467,15 @@ class Sampler:
             pass
 
 
-_PROBES = {"fp64": 0, "fp32": 1, "dmma": 2, "imad_wide": 3, "imad": 4}
+_PROBES = {"fp64": 0, "fp32": 1, "dmma": 2, "imad_wide": 3, "imad": 4, "shf": 5, "add64": 6, "bfind": 7,
+           "iadd": 8}
 
 
 def probe_peak(kind: str) -> float:
     """Measured pipe peak: "fp64" / "fp32" FMA and "dmma" (FP64 tensor MMA)
-    in TFLOP/s; "imad_wide" (mad.wide.s32) and "imad" (mad.lo.s32) in tera
-    lane-operations/s."""
+    in TFLOP/s; "imad_wide" (mad.wide.s32), "imad" (mad.lo.s32), "shf"
+    (shf.l.wrap.b32), "add64" (add.s64), "bfind" (bfind.s32) and "iadd"
+    (add.s32) in tera lane-operations/s."""
     v = ctypes.c_double()
     check(load().gbperm_probe_peak(_PROBES[kind], ctypes.byref(v)))
     return v.value

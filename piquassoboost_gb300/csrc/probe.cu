@@ -11,6 +11,12 @@
 //   2  FP64 tensor MMA (mma.sync m8n8k4)  TFLOP/s, 2*8*8*4 flops per warp MMA
 //   3  32x32->64 multiply-add (mad.wide.s32, IMAD.WIDE)   tera-ops/s (lane ops)
 //   4  32-bit multiply-add (mad.lo.s32, IMAD)             tera-ops/s (lane ops)
+//   5  variable funnel shift (shf.l.wrap.b32)             tera-ops/s (lane ops)
+//   6  64-bit add (add.s64)                               tera-ops/s (lane ops)
+//   7  leading-bit search (bfind.s32)                     tera-ops/s (lane ops)
+//   8  32-bit add (add.s32)                               tera-ops/s (lane ops)
+// Kinds 5-8 price the integer-mantissa product's non-multiply instructions
+// (renormalising shifts, column-sum updates, leading-bit searches).
 #include "gbperm.h"
 #include "gbperm_capi_internal.h"
 
@@ -100,6 +106,41 @@ __global__ void probe_imad(int* out, int a, int b) {
     if (s == 123456789) out[0] = s;
 }
 
+// Integer ALU probes: OP 0 = shf.l.wrap.b32, 1 = bfind.s32, 2 = add.s32.
+template <int OP>
+__global__ void probe_alu32(int* out, int a, int b) {
+    unsigned int x[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) x[i] = threadIdx.x * 7u + i;
+    const unsigned int y = (unsigned int)a, z = (unsigned int)b;
+    for (int it = 0; it < 4 * kProbeIters; ++it) {
+#pragma unroll
+        for (int i = 0; i < kChains; ++i) {
+            if (OP == 0) asm volatile("shf.l.wrap.b32 %0, %1, %0, %2;" : "+r"(x[i]) : "r"(z), "r"(y));
+            if (OP == 1) asm volatile("bfind.s32 %0, %0;" : "+r"(x[i]));
+            if (OP == 2) asm volatile("add.s32 %0, %0, %1;" : "+r"(x[i]) : "r"(y));
+        }
+    }
+    unsigned int s = 0;
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) s ^= x[i];
+    if (s == 123456789u) out[0] = (int)s;
+}
+
+__global__ void probe_add64(long long* out, long long a) {
+    long long x[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) x[i] = threadIdx.x * 7ll + i;
+    for (int it = 0; it < 4 * kProbeIters; ++it) {
+#pragma unroll
+        for (int i = 0; i < kChains; ++i) asm volatile("add.s64 %0, %0, %1;" : "+l"(x[i]) : "l"(a));
+    }
+    long long s = 0;
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) s ^= x[i];
+    if (s == 123456789) out[0] = s;
+}
+
 }  // namespace
 }  // namespace gbperm
 
@@ -107,9 +148,10 @@ using namespace gbperm;
 
 extern "C" int gbperm_probe_peak(int kind, double* tflops) {
     if (!tflops) return fail(GBPERM_ERR_ARG, "gbperm_probe_peak: null output");
-    if (kind < 0 || kind > 4)
+    if (kind < 0 || kind > 8)
         return fail(GBPERM_ERR_ARG,
-                    "gbperm_probe_peak: kind must be 0 (FP64), 1 (FP32), 2 (FP64 MMA), 3 (IMAD.WIDE) or 4 (IMAD)");
+                    "gbperm_probe_peak: kind must be 0 (FP64), 1 (FP32), 2 (FP64 MMA), 3 (IMAD.WIDE), 4 (IMAD), "
+                    "5 (funnel shift), 6 (64-bit add), 7 (bfind) or 8 (32-bit add)");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "gbperm_probe_peak");
@@ -128,7 +170,11 @@ extern "C" int gbperm_probe_peak(int kind, double* tflops) {
         else if (kind == 1) probe_ffma<<<blocks, threads>>>((float*)buf, 1.0000001f, 1e-9f);
         else if (kind == 2) probe_dmma<<<blocks, threads>>>((double*)buf, 1.0000001, 1e-9);
         else if (kind == 3) probe_imad_wide<<<blocks, threads>>>((long long*)buf, 3, 5);
-        else probe_imad<<<blocks, threads>>>((int*)buf, 3, 5);
+        else if (kind == 4) probe_imad<<<blocks, threads>>>((int*)buf, 3, 5);
+        else if (kind == 5) probe_alu32<0><<<blocks, threads>>>((int*)buf, 3, 5);
+        else if (kind == 6) probe_add64<<<blocks, threads>>>((long long*)buf, 977);
+        else if (kind == 7) probe_alu32<1><<<blocks, threads>>>((int*)buf, 3, 5);
+        else probe_alu32<2><<<blocks, threads>>>((int*)buf, 3, 5);
         cudaEventRecord(e1);
         e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) break;

@@ -200,3 +200,10 @@ def test_new_entry_points_need_a_gpu():
         with pytest.raises(nat.GBPermError) as e:
             call()
         assert e.value.code == nat.GBPERM_ERR_NO_DEVICE
+
+
+def test_probe_kind_is_validated_before_the_device(lib):
+    v = ctypes.c_double()
+    assert lib.gbperm_probe_peak(9, ctypes.byref(v)) == nat.GBPERM_ERR_ARG
+    assert lib.gbperm_probe_peak(-1, ctypes.byref(v)) == nat.GBPERM_ERR_ARG
+    assert set(nat._PROBES.values()) == set(range(9))
