@@ -240,29 +240,32 @@ void repeated_low_digits(RepHost* h, const std::function<unsigned long long(unsi
     h->P = P;
     h->nseg = T / P;
     // low-digit tables: binomial weight of each low-digit combination and the
-    // digit that moves at each step of the reflected mixed-radix Gray walk
+    // digit that moves at each step of the reflected mixed-radix Gray walk.
+    // An odometer over the q low digits (g[i] in [0, D_i], digit 0 fastest)
+    // gives both without divisions: the digit that moves at step k is the
+    // number of digits that wrap when k - 1 becomes k, and only the suffix
+    // products of the digits that changed are recomputed.  Every weight is
+    // an integer below 2^45 (D_i <= 15 and prod (D_i + 1) <= 4096 bound
+    // sum D_i by 45, and C(D, g) <= 2^D), so the products are exact in any
+    // order.
     h->wlow.assign(P, 1.0);
     h->seq.assign(P, 0);
     const std::vector<double>& bt = binom_table();
+    int g[16] = {0};      // q <= 16
+    double suf[17];       // suf[i] = prod_{j >= i} C(D_j, g_j)
+    suf[q] = 1.0;
+    for (int i = q - 1; i >= 0; --i) suf[i] = suf[i + 1] * bt[h->D[i] * kBinomStride];
     for (unsigned long long k = 0; k < P; ++k) {
-        unsigned long long rem = k;
-        double w = 1.0;
-        for (int i = 0; i < q; ++i) {
-            unsigned long long L = (unsigned long long)(h->D[i] + 1);
-            int g = (int)(rem % L);
-            rem /= L;
-            w *= bt[h->D[i] * kBinomStride + g];
-        }
-        h->wlow[k] = w;
         if (k > 0) {
-            unsigned long long kk = k;
             int d = 0;
-            while (d < q && kk % (unsigned long long)(h->D[d] + 1) == 0) {
-                kk /= (unsigned long long)(h->D[d] + 1);
+            while (++g[d] > h->D[d]) {  // k < P: some digit below q takes the carry
+                g[d] = 0;
                 ++d;
             }
             h->seq[k] = (unsigned char)d;
+            for (int i = d; i >= 0; --i) suf[i] = suf[i + 1] * bt[h->D[i] * kBinomStride + g[i]];
         }
+        h->wlow[k] = suf[0];
     }
 }
 
